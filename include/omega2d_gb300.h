@@ -1,0 +1,121 @@
+/*
+ * omega2d_gb300.h -- C ABI of the GB300 direct Biot-Savart engine (libomega2d_gb300.so).
+ *
+ * Drop-in for the O(N^2) influence path of Omega2D.  Every entry point names the reference
+ * function it replaces (paths are relative to the Omega2D source tree).  Conventions:
+ *
+ *   - Arrays are structure-of-arrays, FP32 unless the name says otherwise, caller-owned.
+ *     "Host" entry points take host pointers, copy in/out and synchronize before returning;
+ *     "_dev" entry points take device pointers and run asynchronously on the context's stream.
+ *   - Influence sums are UNSCALED and ACCUMULATED (out += sum), like the reference drivers
+ *     (src/Influence.h:207-208, 359-360).  OBS_FLAG_FINALIZE additionally applies the
+ *     reference's finalize step, out = fs + out/(2 pi) (src/ElementBase.h:215-234).
+ *   - Every call returns an int status: OBS_OK (0) or a negative OBS_ERR_* code.  Nothing
+ *     aborts the host process; a failed call leaves the caller's outputs unspecified only for
+ *     _dev calls (host calls leave them untouched).
+ *   - A context is thread-compatible, not re-entrant: one host thread at a time.
+ */
+#ifndef OMEGA2D_GB300_H
+#define OMEGA2D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes */
+#define OBS_OK 0
+#define OBS_ERR_ARG (-1)        /* invalid argument (null pointer, negative size, bad enum)  */
+#define OBS_ERR_ALLOC (-2)      /* device or host allocation failed                         */
+#define OBS_ERR_CUDA (-3)       /* a CUDA runtime call failed                                */
+#define OBS_ERR_TIMEOUT (-4)    /* a bounded device-side wait gave up                        */
+#define OBS_ERR_NO_DEVICE (-5)  /* no usable CUDA device                                     */
+#define OBS_ERR_SINGULAR (-6)   /* dense solve met a zero pivot                              */
+#define OBS_ERR_UNSUPPORTED (-7)
+
+/* ---- core functions (src/CoreFunc.h:35-322 selects one at compile time; here at run time) */
+#define OBS_CORE_RM 1           /* Rosenhead-Moore, src/CoreFunc.h:42-82                     */
+#define OBS_CORE_GAUSSIAN 2     /* "exponential" = Gaussian blob, src/CoreFunc.h:85-181      */
+#define OBS_CORE_V2 3           /* Vatistas n=2 (the reference default), :233-275            */
+#define OBS_CORE_WL 4           /* Winckelmans-Leonard, :184-230                              */
+#define OBS_CORE_V3 5           /* Vatistas n=3, :278-322                                     */
+#define OBS_CORE_SINGULAR 6     /* point vortex 1/d^2 (RM with zero radii), self pair = 0   */
+#define OBS_CORE_COMPACT_EXP 7  /* (1 - exp(-(d/s)^3))/d^2; not in the reference            */
+
+/* ---- result types: same values as results_t (src/ResultsType.h:26-32) */
+#define OBS_VELONLY 1
+#define OBS_VELANDGRAD 2        /* extra0..3 = du/dx, dv/dx, du/dy, dv/dy                    */
+#define OBS_PSIONLY 3           /* extra0 = streamfunction; velocity untouched               */
+#define OBS_VELANDVORT 4        /* extra0 = vorticity                                         */
+#define OBS_VELANDSHEAR 5       /* extra0 = shear rate                                        */
+
+/* ---- accumulation modes */
+#define OBS_PLAIN_F32 0         /* FP32 accumulators: the plain drop-in                      */
+#define OBS_COMPENSATED 1       /* FP32 pair math, two-sum per 32-source block, FP64 reduce  */
+
+/* ---- flags */
+#define OBS_FLAG_FINALIZE 1     /* out = fs + (out + sum)/(2 pi); extras *= 1/(2 pi)          */
+
+typedef struct obs_context obs_context;
+
+/* Context: CUDA device binding, one stream, device work buffers that grow on demand. */
+int obs_create(obs_context** ctx, int device);
+int obs_destroy(obs_context* ctx);
+/* Use an external cudaStream_t (passed as void*) for _dev calls; NULL restores the own stream. */
+int obs_set_stream(obs_context* ctx, void* cuda_stream);
+int obs_synchronize(obs_context* ctx);
+/* Enable CUDA-event timing of the main kernel of each subsequent call (default off). */
+int obs_enable_timing(obs_context* ctx, int on);
+/* Main-kernel and whole-call device time of the most recent timed call, in milliseconds. */
+int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
+/* Number of engine kernel launches issued by this context since creation. */
+long long obs_launch_count(obs_context* ctx);
+const char* obs_status_string(int status);
+/* Algorithmic flops per interaction the reference attaches to a kernel (src/Kernels.h flops*,
+ * src/CoreFunc.h flops_*), or -1 when the reference has none for that combination. */
+int obs_flops_per_pair(int core, int result, int thick_targets);
+
+/*
+ * points_affect_points -- replaces src/Influence.h:56-416 (x86 and Vc branches).
+ * Sources: ns particles (sx, sy, sr = core radius, ss = circulation).
+ * Targets: nt points; tr == NULL selects field points (the "0p" kernels, src/Influence.h:114-250),
+ *          otherwise thick targets with core radius tr (the "0b" kernels, :255-406).
+ * Outputs: tu, tv (+ extra0..3 per result type) accumulated; flops (optional) receives the
+ *          reference's flop count for the call (src/Influence.h:362 convention).
+ */
+int obs_points_affect_points(obs_context* ctx, int core, int result, int accum, int flags,
+                             double fsx, double fsy,
+                             int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                             int nt, const float* tx, const float* ty, const float* tr,
+                             float* tu, float* tv,
+                             float* extra0, float* extra1, float* extra2, float* extra3,
+                             double* flops);
+int obs_points_affect_points_dev(obs_context* ctx, int core, int result, int accum, int flags,
+                                 double fsx, double fsy,
+                                 int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                 int nt, const float* tx, const float* ty, const float* tr,
+                                 float* tu, float* tv,
+                                 float* extra0, float* extra1, float* extra2, float* extra3,
+                                 double* flops);
+
+/*
+ * Source-compatible replacements for the reference's external direct-solver hook
+ * (src/Influence.h:31-38, called at :74-98 when built with -DEXTERNAL_VEL_SOLVE).
+ * Same argument order (note ss before sr), counts by pointer, velocities ACCUMULATED and
+ * unscaled; the return value is the flop count, or a negative value on error (outputs are
+ * then untouched).  They use a process-wide context on device 0 with the core and mode set by
+ * obs_external_configure (default: Vatistas n=2, compensated).
+ */
+float external_vel_solver_f_(int* ns, const float* sx, const float* sy, const float* ss, const float* sr,
+                             int* nt, const float* tx, const float* ty, float* tu, float* tv);
+float external_vel_solver_tr_f_(int* ns, const float* sx, const float* sy, const float* ss, const float* sr,
+                                int* nt, const float* tx, const float* ty, const float* tr,
+                                float* tu, float* tv);
+float external_vel_solver_d_(int* ns, const double* sx, const double* sy, const double* ss, const double* sr,
+                             int* nt, const double* tx, const double* ty, double* tu, double* tv);
+int obs_external_configure(int core, int accum);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OMEGA2D_GB300_H */

@@ -1,0 +1,82 @@
+// obs_context.h -- host-side engine state shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/omega2d_gb300.h"
+
+namespace obs {
+
+// Device buffer that only grows.  Growing synchronizes the owning stream first so no queued
+// kernel can still be using the old allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes, cudaStream_t st);
+  void release();
+  template <class T> T* as(size_t byte_offset = 0) const {
+    return reinterpret_cast<T*>(static_cast<char*>(p) + byte_offset);
+  }
+};
+
+// Fixed header at the start of the work buffer (zeroed before every pairwise launch).
+struct WorkHeader {
+  int counter;          // dynamic item counter
+  unsigned meta[4];     // radius extrema (see P2PArgs::meta)
+  int pad[3];
+};
+static_assert(sizeof(WorkHeader) == 32, "header layout");
+
+struct Timing {
+  bool on = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float main_ms = 0.0f;
+  float call_ms = 0.0f;
+  bool pending = false;
+};
+
+}  // namespace obs
+
+struct obs_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  obs::DevBuf work;      // header | packed sources | split partials | other scratch
+  obs::DevBuf io;        // staging for host-pointer calls
+  int* d_status = nullptr;   // device-side error bits (DEV_ERR_*), sticky until read
+  obs::Timing timing;
+  long long launches = 0;
+};
+
+namespace obs {
+
+// Map a CUDA error to an engine status (and clear the sticky last-error where possible).
+int cuda_status(cudaError_t e);
+// Bind the context's device on the calling thread.
+int bind(obs_context* ctx);
+// Read and clear the device error bits (synchronizes the stream).
+int take_device_status(obs_context* ctx);
+// Event helpers around the main kernel of a call.
+void timing_begin(obs_context* ctx);
+void timing_main_begin(obs_context* ctx);
+void timing_main_end(obs_context* ctx);
+void timing_end(obs_context* ctx);
+
+// One particle-on-particle request on device arrays (see obs_points_affect_points_dev).
+struct P2PRequest {
+  int core, result, accum, flags;
+  double fsx, fsy;
+  int ns;
+  const float *sx, *sy, *sr, *ss;
+  int nt;
+  const float *tx, *ty, *tr;
+  float *tu, *tv;
+  float* extra[4];
+};
+int run_p2p(obs_context* ctx, const P2PRequest& rq);
+double p2p_flops(int core, int result, bool thick, long long ns, long long nt);
+
+}  // namespace obs

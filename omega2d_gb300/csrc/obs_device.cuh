@@ -1,0 +1,166 @@
+// obs_device.cuh -- device-side building blocks of the direct Biot-Savart engine (sm_103a).
+//
+// Core functions, hardware-approximation wrappers, compensated (two-sum) accumulation and the
+// TMA bulk-copy / mbarrier primitives used by every pairwise kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace obs {
+
+// core-function ids (same values as OBS_CORE_* in include/omega2d_gb300.h)
+enum : int { CORE_RM = 1, CORE_GAUSS = 2, CORE_V2 = 3, CORE_WL = 4, CORE_V3 = 5, CORE_SING = 6, CORE_CEXP = 7 };
+// result types (same values as the reference's results_t, src/ResultsType.h:26-32)
+enum : int { RES_VEL = 1, RES_GRAD = 2, RES_PSI = 3, RES_VORT = 4, RES_SHEAR = 5 };
+
+// status bits written by kernels (read back by the host)
+enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2 };
+
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kPadCoord = 3.0e18f;   // padded sources sit here with zero strength
+
+// ---------------------------------------------------------------- PTX approximations
+// Documented PTX forms; maximum errors per the PTX ISA: rcp 1 ulp, sqrt/rsqrt ~2 ulp,
+// ex2 2 ulp over the full range, lg2 2^-22 absolute.
+__device__ __forceinline__ float rcp_a(float x) { float r; asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r; }
+__device__ __forceinline__ float rsqrt_a(float x) { float r; asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r; }
+__device__ __forceinline__ float sqrt_a(float x) { float r; asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r; }
+__device__ __forceinline__ float ex2_a(float x) { float r; asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r; }
+__device__ __forceinline__ float lg2_a(float x) { float r; asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r; }
+
+// ---------------------------------------------------------------- per-core source/target term
+// Each source/target carries one precomputed radius term z so that the pair only combines
+// them.  The forms follow the non-singular-target core functions of src/CoreFunc.h:
+//   RM, Gaussian, WL, compact-exp : z = r^2          (sr*sr + tr*tr)
+//   Vatistas n=2                  : z = (r^2)^2      (s2*s2 + t2*t2)
+//   Vatistas n=3                  : z = (r^2)^3      (s2*s2*s2 + t2*t2*t2)
+//   singular                      : unused
+// The streamfunction (kernelp, src/Kernels.h:52-74) always uses z = r^2.
+__host__ __device__ __forceinline__ float radius_term(int core, float r) {
+  const float s2 = r * r;
+  if (core == CORE_V2) return s2 * s2;
+  if (core == CORE_V3) return s2 * s2 * s2;
+  return s2;
+}
+
+// ---------------------------------------------------------------- core functions
+// K(d^2) such that one pair contributes strength*K*(-dy, dx), and (GRAD) B = 2 dK/d(d^2) as
+// the reference's "bbb".  zs/zt: radius terms; THICK selects the two-radius form.  UNIF: all
+// radii equal, so s2 = us2 and 1/s2 = ucf are hoisted out of the pair loop.
+template <int CORE, bool THICK, bool GRAD, bool UNIF>
+__device__ __forceinline__ void core_eval(float d2, float zs, float zt, float us2, float ucf,
+                                          float& K, float& B) {
+  if constexpr (CORE == CORE_RM) {
+    // src/CoreFunc.h:47-80: 1/(d^2 + s^2), bbb = -2 K^2
+    const float s2 = UNIF ? us2 : (THICK ? zs + zt : zs);
+    K = rcp_a(d2 + s2);
+    if constexpr (GRAD) B = -2.0f * K * K;
+  } else if constexpr (CORE == CORE_GAUSS) {
+    // src/CoreFunc.h:111-181 ("exponential" core): reld2 = d^2/s^2;
+    // reld2 > 16 -> 1/d^2, reld2 < 0.001 -> 1/s^2, else (1 - e^-reld2)/d^2
+    const float cf = UNIF ? ucf : rcp_a(THICK ? zs + zt : zs);
+    const float ood2 = rcp_a(d2);
+    const float x = d2 * cf;
+    const float e = ex2_a(x * -kLog2e);
+    float k = fmaf(-ood2, e, ood2);
+    k = (x > 16.0f) ? ood2 : k;
+    k = (x < 0.001f) ? cf : k;
+    K = k;
+    if constexpr (GRAD) B = (d2 == 0.0f) ? 0.0f : (2.0f * cf * e - 2.0f * k) * ood2;
+  } else if constexpr (CORE == CORE_V2) {
+    // src/CoreFunc.h:238-274: 1/sqrt(d^4 + s^4 (+ t^4)), bbb = -2 K^3 d^2
+    const float a = fmaf(d2, d2, THICK ? zs + zt : zs);
+    K = rsqrt_a(a);
+    if constexpr (GRAD) B = -2.0f * K * K * K * d2;
+  } else if constexpr (CORE == CORE_WL) {
+    // src/CoreFunc.h:189-229: (d2 + s2 + s2)/(d2 + s2)^2, bbb = (2 - 4 K dd)/dd^2
+    const float s2 = UNIF ? us2 : (THICK ? zs + zt : zs);
+    const float dd = d2 + s2;
+    const float o = rcp_a(dd * dd);
+    K = (dd + s2) * o;
+    if constexpr (GRAD) B = (2.0f - 4.0f * K * dd) * o;
+  } else if constexpr (CORE == CORE_V3) {
+    // src/CoreFunc.h:283-321: (d^6 + s^6 (+ t^6))^(-1/3), bbb = -2 d^4 K / a = -2 d^4 K^4
+    const float a = fmaf(d2 * d2, d2, THICK ? zs + zt : zs);
+    K = ex2_a(lg2_a(a) * (-1.0f / 3.0f));
+    if constexpr (GRAD) { const float k2 = K * K; B = -2.0f * d2 * d2 * k2 * k2; }
+  } else if constexpr (CORE == CORE_SING) {
+    // point vortex: 1/d^2, the coincident pair contributes nothing
+    K = (d2 > 0.0f) ? rcp_a(d2) : 0.0f;
+    if constexpr (GRAD) B = -2.0f * K * K;
+  } else {  // CORE_CEXP
+    // compact exponential: y = (d^2/s^2)^(3/2); y > 16 -> 1/d^2; y < 0.001 -> (d/s^3)(1 - y/2);
+    // else (1 - e^-y)/d^2.  bbb = (3 y e^-y / d^2 - 2K)/d^2.
+    const float cf = UNIF ? ucf : rcp_a(THICK ? zs + zt : zs);
+    const float x = d2 * cf;
+    const float sx = sqrt_a(x);
+    const float y = x * sx;
+    const float ood2 = rcp_a(d2);
+    const float e = ex2_a(y * -kLog2e);
+    float k = fmaf(-ood2, e, ood2);
+    k = (y > 16.0f) ? ood2 : k;
+    k = (y < 0.001f) ? sx * cf * fmaf(-0.5f, y, 1.0f) : k;
+    K = k;
+    if constexpr (GRAD) {
+      float b = (3.0f * y * e * ood2 - 2.0f * k) * ood2;
+      b = (y > 16.0f) ? -2.0f * ood2 * ood2 : b;
+      B = (d2 == 0.0f) ? 0.0f : b;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- compensated accumulation
+// Knuth two-sum: hi + lo accumulates b exactly up to the rounding of lo itself.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float b) {
+  const float s = hi + b;
+  const float bp = s - hi;
+  const float ap = s - bp;
+  const float err = (hi - ap) + (b - bp);
+  hi = s;
+  lo += err;
+}
+
+// ---------------------------------------------------------------- TMA bulk copy + mbarrier
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               :: "r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// one-dimensional bulk copy global -> shared (TMA engine); 16-byte aligned, size % 16 == 0
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n\t.reg .pred p;\n\t"
+               "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+               "selp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: gives up after max_tries polls (each try_wait may itself suspend for a
+// hardware-defined interval) and reports false so the caller can flag a timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_tries) {
+  for (uint32_t i = 0; i < max_tries; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+}  // namespace obs

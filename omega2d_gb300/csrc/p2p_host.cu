@@ -1,0 +1,184 @@
+// p2p_host.cu -- launch planning for the particle-on-particle kernels (points_affect_points).
+#include <algorithm>
+#include <cstring>
+
+#include "obs_context.h"
+#include "p2p_dispatch.cuh"
+
+namespace obs {
+
+namespace {
+
+// Warp-reduce radius extrema (as bit patterns; radii are non-negative) and fold them into
+// meta[k] = ~min, meta[k+1] = max with one atomic per warp.
+__device__ __forceinline__ void fold_extrema(bool active, float r, unsigned* meta) {
+  unsigned rmin = active ? __float_as_uint(r) : ~0u;
+  unsigned rmax = active ? __float_as_uint(r) : 0u;
+  int any = active ? 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) {
+    rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+    rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    any |= __shfl_xor_sync(0xffffffffu, any, o);
+  }
+  if ((threadIdx.x & 31) == 0 && any) {
+    atomicMax(&meta[0], ~rmin);
+    atomicMax(&meta[1], rmax);
+  }
+}
+
+// Pack the caller's SoA sources into float4 (x, y, radius term, strength), padded to whole
+// tiles with zero-strength sources far away, and record the radius extrema in meta[0..1].
+__global__ void pack_sources_kernel(const float* __restrict__ sx, const float* __restrict__ sy,
+                                    const float* __restrict__ sr, const float* __restrict__ ss,
+                                    int ns, int ns_pad, int core, float4* __restrict__ out,
+                                    unsigned* __restrict__ meta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const float r = (i < ns && sr) ? sr[i] : 0.0f;
+  if (i < ns) {
+    out[i] = make_float4(sx[i], sy[i], radius_term(core, r), ss[i]);
+  } else if (i < ns_pad) {
+    out[i] = make_float4(kPadCoord, kPadCoord, 1.0f, 0.0f);
+  }
+  fold_extrema(i < ns, r, meta);
+}
+
+__global__ void target_meta_kernel(const float* __restrict__ tr, int nt, unsigned* __restrict__ meta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  fold_extrema(i < nt, i < nt ? tr[i] : 0.0f, meta + 2);
+}
+
+int ncomp_of(int res) {
+  switch (res) {
+    case RES_VEL: return 2;
+    case RES_GRAD: return 5;
+    case RES_PSI: return 1;
+    default: return 3;
+  }
+}
+
+cudaError_t dispatch(int core, bool thick, int res, bool comp, const P2PArgs* a, int grid,
+                     cudaStream_t st, int* occ) {
+  if (res == RES_PSI) return p2p_dispatch_psi(thick, comp, a, grid, st, occ);
+  switch (core) {
+    case CORE_RM: return p2p_dispatch<CORE_RM>(thick, res, comp, a, grid, st, occ);
+    case CORE_GAUSS: return p2p_dispatch<CORE_GAUSS>(thick, res, comp, a, grid, st, occ);
+    case CORE_V2: return p2p_dispatch<CORE_V2>(thick, res, comp, a, grid, st, occ);
+    case CORE_WL: return p2p_dispatch<CORE_WL>(thick, res, comp, a, grid, st, occ);
+    case CORE_V3: return p2p_dispatch<CORE_V3>(thick, res, comp, a, grid, st, occ);
+    case CORE_SING: return p2p_dispatch<CORE_SING>(thick, res, comp, a, grid, st, occ);
+    case CORE_CEXP: return p2p_dispatch<CORE_CEXP>(thick, res, comp, a, grid, st, occ);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+// Reference flop counts: flopsu_0v_0b = 10 + flops_tv_nograds, flopsu_0v_0p = 10 +
+// flops_tp_nograds, flopsug_0v_0b = 25 + flops_tv_grads, flopsuw = 19 + .._grads, flopsue = 23
+// + .._grads, flopsp = 10 + .._nograds (src/Kernels.h:50-190; src/CoreFunc.h flops_*).
+// Cores the reference lacks reuse the nearest reference form (singular: RM, compact exp:
+// Gaussian); the field-point gradient uses the thick-target rule with the 0p core count.
+double p2p_flops(int core, int result, bool thick, long long ns, long long nt) {
+  //                       RM  GAUSS V2  WL  V3  SING CEXP
+  static const int tvn[8] = {0, 5, 9, 9, 7, 12, 5, 9};
+  static const int tpn[8] = {0, 3, 7, 6, 5, 8, 3, 7};
+  static const int tvg[8] = {0, 9, 16, 13, 12, 16, 9, 16};
+  static const int tpg[8] = {0, 9, 14, 10, 10, 12, 9, 14};
+  if (core < 1 || core > 7) return -1.0;
+  int per = 0, extra_per_target = 2;
+  switch (result) {
+    case RES_VEL: per = 10 + (thick ? tvn[core] : tpn[core]); break;
+    case RES_GRAD: per = 25 + (thick ? tvg[core] : tpg[core]); break;
+    case RES_PSI: per = 10 + (thick ? tvn[core] : tpn[core]); extra_per_target = 1; break;
+    case RES_VORT: per = 19 + (thick ? tvg[core] : tpg[core]); extra_per_target = 3; break;
+    case RES_SHEAR: per = 23 + (thick ? tvg[core] : tpg[core]); extra_per_target = 3; break;
+    default: return -1.0;
+  }
+  return (double)nt * ((double)extra_per_target + (double)per * (double)ns);
+}
+
+int run_p2p(obs_context* ctx, const P2PRequest& rq) {
+  const bool thick = rq.tr != nullptr;
+  const bool comp = rq.accum == OBS_COMPENSATED;
+  if (rq.ns == 0 || rq.nt == 0) return OBS_OK;
+  const int res = rq.result;
+  const int kcore = (res == RES_PSI) ? CORE_RM : rq.core;
+  cudaStream_t st = ctx->stream;
+
+  // ---- plan the split
+  int occ = 0;
+  cudaError_t e = dispatch(rq.core, thick, res, comp, nullptr, 0, st, &occ);
+  if (e != cudaSuccess) return cuda_status(e);
+  occ = std::max(occ, 1);
+  const int slots = occ * ctx->num_sms;
+  const int tb = P2P_THREADS * p2p_tpt(res);
+  const int ntb = (rq.nt + tb - 1) / tb;
+  const int nst = (rq.ns + SRC_TILE - 1) / SRC_TILE;
+  const int want_items = 24 * slots;
+  int nsplit = std::max(1, (want_items + ntb - 1) / ntb);
+  nsplit = std::min(nsplit, std::max(1, nst / 4));
+  const int tps = (nst + nsplit - 1) / nsplit;
+  nsplit = (nst + tps - 1) / tps;
+  const int nitems = ntb * nsplit;
+  const int grid = std::min(nitems, slots);
+  const int nc = ncomp_of(res);
+
+  // ---- work buffer: header | packed sources | partials
+  const size_t hdr = 256;
+  const size_t src_bytes = (size_t)nst * SRC_TILE * sizeof(float4);
+  const size_t part_bytes = nsplit > 1 ? (size_t)nc * nsplit * rq.nt * (comp ? sizeof(double) : sizeof(float)) : 0;
+  int s = ctx->work.ensure(hdr + src_bytes + part_bytes, st);
+  if (s) return s;
+  WorkHeader* h = ctx->work.as<WorkHeader>(0);
+  float4* src = ctx->work.as<float4>(hdr);
+  void* part = part_bytes ? ctx->work.as<char>(hdr + src_bytes) : nullptr;
+
+  timing_begin(ctx);
+  e = cudaMemsetAsync(h, 0, sizeof(WorkHeader), st);
+  if (e != cudaSuccess) return cuda_status(e);
+  {
+    const int threads = 256;
+    const int ns_pad = nst * SRC_TILE;
+    pack_sources_kernel<<<(ns_pad + threads - 1) / threads, threads, 0, st>>>(
+        rq.sx, rq.sy, rq.sr, rq.ss, rq.ns, ns_pad, kcore, src, h->meta);
+    ctx->launches++;
+    if (thick) {
+      target_meta_kernel<<<(rq.nt + threads - 1) / threads, threads, 0, st>>>(rq.tr, rq.nt, h->meta);
+      ctx->launches++;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+
+  P2PArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.src = src;
+  a.nst = nst;
+  a.tx = rq.tx; a.ty = rq.ty; a.tr = rq.tr;
+  a.nt = rq.nt; a.ntb = ntb;
+  a.nsplit = nsplit; a.tiles_per_split = tps; a.nitems = nitems;
+  a.counter = &h->counter;
+  a.meta = h->meta;
+  a.status = ctx->d_status;
+  a.out[0] = rq.tu; a.out[1] = rq.tv;
+  for (int k = 0; k < 4; ++k) a.out[2 + k] = rq.extra[k];
+  a.part = part;
+  a.direct = nsplit == 1;
+  a.finalize = (rq.flags & OBS_FLAG_FINALIZE) ? 1 : 0;
+  a.fsx = rq.fsx; a.fsy = rq.fsy;
+
+  timing_main_begin(ctx);
+  e = dispatch(rq.core, thick, res, comp, &a, grid, st, nullptr);
+  ctx->launches++;
+  timing_main_end(ctx);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (nsplit > 1) {
+    e = p2p_reduce(res, comp, a, st);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  timing_end(ctx);
+  return OBS_OK;
+}
+
+}  // namespace obs

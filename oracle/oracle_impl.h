@@ -1,0 +1,436 @@
+/* oracle_impl.h -- body of the CPU restatement, included twice by oracle.c.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle is the checker for the CUDA path and the timed CPU
+ * baseline ("port"); it is never linked into or called by the product library.
+ *
+ * Before inclusion the includer defines
+ *   R      pair-arithmetic type (float for the reference's non-Vc build, double for FP64)
+ *   A      accumulator type (double in both instantiations, src/Simulation.h:44-50)
+ *   SFX(n) name decoration (n##_f or n##_d)
+ *
+ * Conventions shared with the reference (cited per function):
+ *   - every influence sum is left unscaled: the 1/(2 pi) factor and the freestream are applied
+ *     by the finalize step (src/ElementBase.h:215-234);
+ *   - drivers ACCUMULATE into the target arrays (+=), like src/Influence.h:207-208, 359-360;
+ *   - "thick" targets carry a core radius and use the two-radius core forms
+ *     (src/CoreFunc.h, "non-singular targets"); tr == NULL means field points (0p forms).
+ */
+
+/* ---------------------------------------------------------------- core functions */
+
+/* Velocity-only core value K(d^2) such that the pair velocity is ss*K*(-dy, dx).
+ * core ids follow omega2d_gb300.h (OBS_CORE_*). */
+static inline R SFX(core_vel)(int core, R d2, R sr, R tr, int thick) {
+  switch (core) {
+  case 1: { /* Rosenhead-Moore, src/CoreFunc.h:47-59 */
+    R r2 = thick ? d2 + sr*sr + tr*tr : d2 + sr*sr;
+    return (R)1.0 / r2;
+  }
+  case 2: { /* Gaussian-blob ("exponential") core with cut-offs, src/CoreFunc.h:111-153 */
+    R ood2 = (R)1.0 / d2;
+    R corefac = (R)1.0 / (thick ? sr*sr + tr*tr : sr*sr);
+    R reld2 = corefac / ood2;
+    if (reld2 > (R)16.0) return ood2;
+    if (reld2 < (R)0.001) return corefac;
+    return ood2 * ((R)1.0 - EXP(-reld2));
+  }
+  case 3: { /* Vatistas n=2, src/CoreFunc.h:238-252 */
+    R s2 = sr*sr, t2 = tr*tr;
+    return thick ? (R)1.0 / SQRT(d2*d2 + s2*s2 + t2*t2) : (R)1.0 / SQRT(d2*d2 + s2*s2);
+  }
+  case 4: { /* Winckelmans-Leonard, src/CoreFunc.h:189-203 */
+    R s2 = thick ? sr*sr + tr*tr : sr*sr;
+    R dd = d2 + s2;
+    return (dd + s2) / (dd*dd);
+  }
+  case 5: { /* Vatistas n=3, src/CoreFunc.h:283-297 */
+    R s2 = sr*sr, t2 = tr*tr;
+    R a = thick ? d2*d2*d2 + s2*s2*s2 + t2*t2*t2 : d2*d2*d2 + s2*s2*s2;
+    return (R)1.0 / CBRT(a);
+  }
+  case 6: /* singular point vortex: RM with zero radii, coincident pair excluded */
+    return d2 > (R)0 ? (R)1.0 / d2 : (R)0;
+  case 7: { /* compact exponential (no counterpart in the reference):
+             * K = (1 - exp(-y)) / d^2 with y = (d^2/s^2)^(3/2), s^2 = sr^2 (+ tr^2);
+             * y > 16 -> 1/d^2; y < 0.001 -> (d/s^3)(1 - y/2) (two-term series). */
+    R s2 = thick ? sr*sr + tr*tr : sr*sr;
+    R x = d2 / s2;
+    R y = x * SQRT(x);
+    if (y > (R)16.0) return (R)1.0 / d2;
+    if (y < (R)0.001) return SQRT(d2) / (s2 * SQRT(s2)) * ((R)1.0 - (R)0.5 * y);
+    return ((R)1.0 - EXP(-y)) / d2;
+  }
+  default:
+    return (R)0;
+  }
+}
+
+/* Core value plus bbb = 2 dK/d(d^2), the gradient form used by kernelug/kerneluw/kernelue.
+ * Reference forms: RM src/CoreFunc.h:64-80, Gaussian :145-181, WL :208-229, V2 :257-274,
+ * V3 :302-321.  Coincident pairs (d2 == 0) return bbb = 0 so that no 0*inf appears (the
+ * reference's Gaussian form yields NaN there); the pair's r2 term is still the core's value
+ * at the origin, which is the limit of the smooth kernel. */
+static inline void SFX(core_grad)(int core, R d2, R sr, R tr, int thick, R* r2, R* bbb) {
+  switch (core) {
+  case 1: {
+    R td2 = thick ? d2 + sr*sr + tr*tr : d2 + sr*sr;
+    *r2 = (R)1.0 / td2;
+    *bbb = (R)(-2.0) * (*r2) * (*r2);
+    return;
+  }
+  case 2: {
+    R ood2 = (R)1.0 / d2;
+    R corefac = (R)1.0 / (thick ? sr*sr + tr*tr : sr*sr);
+    R reld2 = corefac / ood2;
+    if (reld2 > (R)16.0) *r2 = ood2;
+    else if (reld2 < (R)0.001) *r2 = corefac;
+    else *r2 = ood2 * ((R)1.0 - EXP(-reld2));
+    if (d2 == (R)0) { *bbb = (R)0; return; }
+    *bbb = (R)(-2.0) * (*r2) * ood2 + (R)2.0 * corefac * ood2 * EXP(-reld2);
+    return;
+  }
+  case 3: {
+    R s2 = sr*sr, t2 = tr*tr;
+    *r2 = thick ? (R)1.0 / SQRT(d2*d2 + s2*s2 + t2*t2) : (R)1.0 / SQRT(d2*d2 + s2*s2);
+    *bbb = (R)(-2.0) * (*r2) * (*r2) * (*r2) * d2;
+    return;
+  }
+  case 4: {
+    R s2 = thick ? sr*sr + tr*tr : sr*sr;
+    R dd = d2 + s2;
+    R ood2s = (R)1.0 / (dd*dd);
+    *r2 = (dd + s2) * ood2s;
+    *bbb = ((R)2.0 - (R)4.0 * (*r2) * dd) * ood2s;
+    return;
+  }
+  case 5: {
+    R s2 = sr*sr, t2 = tr*tr;
+    R ds6 = thick ? d2*d2*d2 + s2*s2*s2 + t2*t2*t2 : d2*d2*d2 + s2*s2*s2;
+    *r2 = (R)1.0 / CBRT(ds6);
+    *bbb = (R)(-2.0) * d2*d2 * (*r2) / ds6;
+    return;
+  }
+  case 6:
+    if (d2 > (R)0) { *r2 = (R)1.0 / d2; *bbb = (R)(-2.0) * (*r2) * (*r2); }
+    else { *r2 = (R)0; *bbb = (R)0; }
+    return;
+  case 7: {
+    R s2 = thick ? sr*sr + tr*tr : sr*sr;
+    if (d2 == (R)0) { *r2 = (R)0; *bbb = (R)0; return; }
+    R x = d2 / s2;
+    R y = x * SQRT(x);
+    R ood2 = (R)1.0 / d2;
+    if (y > (R)16.0) { *r2 = ood2; *bbb = (R)(-2.0) * ood2 * ood2; return; }
+    R e = EXP(-y);
+    *r2 = (y < (R)0.001) ? SQRT(d2) / (s2 * SQRT(s2)) * ((R)1.0 - (R)0.5 * y) : ((R)1.0 - e) * ood2;
+    /* 2 dK/d(d^2) = (3 y e^{-y} / d^2 - 2 K) / d^2 */
+    *bbb = ((R)3.0 * y * e * ood2 - (R)2.0 * (*r2)) * ood2;
+    return;
+  }
+  default:
+    *r2 = (R)0; *bbb = (R)0;
+  }
+}
+
+/* ---------------------------------------------------------------- points on points */
+
+/* points_affect_points, src/Influence.h:56-416 (x86 branches); restype as results_t
+ * (src/ResultsType.h:26-32): 1 velonly, 2 velandgrad, 3 psionly, 4 velandvort, 5 velandshear.
+ * extra: velandgrad -> e0..e3 = (ux, vx, uy, vy); psionly -> e0 = psi; vort -> e0 = w;
+ * shear -> e0 = e.  Pair kernels: kernelu_0v_0b/0p (src/Kernels.h:81-106), kernelug_0v_0b
+ * (:112-133, with a field-point twin), kerneluw (:139-179), kernelue (:185-231),
+ * kernelp (:52-74). */
+void SFX(o_points_affect_points)(int core, int restype,
+                                 int ns, const R* sx, const R* sy, const R* sr, const R* ss,
+                                 int nt, const R* tx, const R* ty, const R* tr,
+                                 R* tu, R* tv, R* e0, R* e1, R* e2, R* e3) {
+  const int thick = (tr != 0);
+  #pragma omp parallel for schedule(static)
+  for (int i = 0; i < nt; ++i) {
+    A au = 0, av = 0, a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const R xi = tx[i], yi = ty[i], ri = thick ? tr[i] : (R)0;
+    for (int j = 0; j < ns; ++j) {
+      const R dx = xi - sx[j];
+      const R dy = yi - sy[j];
+      const R d2 = dx*dx + dy*dy;
+      if (restype == 1) {
+        const R r2 = ss[j] * SFX(core_vel)(core, d2, sr[j], ri, thick);
+        au -= r2 * dy;
+        av += r2 * dx;
+      } else if (restype == 3) {
+        /* kernelp_0v_0b / 0v_0p: -ss * 0.5*log(d^2 + sr^2 (+ tr^2)) */
+        const R a = thick ? d2 + sr[j]*sr[j] + ri*ri : d2 + sr[j]*sr[j];
+        a0 -= ss[j] * ((R)0.5 * LOG(a));
+      } else {
+        R r2, bbb;
+        SFX(core_grad)(core, d2, sr[j], ri, thick, &r2, &bbb);
+        r2 *= ss[j];
+        bbb *= ss[j];
+        au -= r2 * dy;
+        av += r2 * dx;
+        if (restype == 2) {
+          a0 += -bbb*dx*dy;          /* du/dx */
+          a1 +=  bbb*dx*dx + r2;     /* dv/dx */
+          a2 += -bbb*dy*dy - r2;     /* du/dy */
+          a3 +=  bbb*dx*dy;          /* dv/dy */
+        } else if (restype == 4) {
+          const R dudy = -bbb*dy*dy - r2;
+          const R dvdx =  bbb*dx*dx + r2;
+          a0 += dvdx - dudy;
+        } else if (restype == 5) {
+          const R dudx = -bbb*dx*dy;
+          const R asym = bbb*(dx*dx - dy*dy);
+          a0 += SQRT(dudx*dudx + (R)0.25*asym*asym);
+        }
+      }
+    }
+    if (restype != 3) {
+      tu[i] = (R)((A)tu[i] + au);
+      tv[i] = (R)((A)tv[i] + av);
+    }
+    if (restype == 2) {
+      e0[i] = (R)((A)e0[i] + a0); e1[i] = (R)((A)e1[i] + a1);
+      e2[i] = (R)((A)e2[i] + a2); e3[i] = (R)((A)e3[i] + a3);
+    } else if (restype >= 3) {
+      e0[i] = (R)((A)e0[i] + a0);
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- panels */
+
+/* get_ustar, src/Kernels.h:256-268 (non-Vc): angle subtended by the panel, wrapped to [-pi, pi] */
+static inline R SFX(ustar)(R dx0, R dy0, R dx1, R dy1) {
+  R u = ATAN2(dx1, dy1) - ATAN2(dx0, dy0);
+  if ((double)u < -M_PI) u = (R)((double)u + 2.0 * M_PI);
+  if ((double)u > M_PI) u = (R)((double)u - 2.0 * M_PI);
+  return u;
+}
+
+/* kernelu_1v_0p, src/Kernels.h:311-354: constant-strength vortex panel on a point */
+static inline void SFX(k1v)(R sx0, R sy0, R sx1, R sy1, R str, R tx, R ty, R* u, R* v) {
+  const R dx0 = tx - sx0, dy0 = ty - sy0, dx1 = tx - sx1, dy1 = ty - sy1;
+  const R px = sx1 - sx0, py = sy1 - sy0;
+  const R rij2 = dx0*dx0 + dy0*dy0, rij12 = dx1*dx1 + dy1*dy1, panl = px*px + py*py;
+  const R us = SFX(ustar)(dx0, dy0, dx1, dy1);
+  const R vs = (R)0.5 * LOG(rij2 / rij12);
+  const R velx = us*px - vs*py, vely = us*py + vs*px;
+  const R mult = str * ((R)1.0 / SQRT(panl));
+  *u = mult * velx;
+  *v = mult * vely;
+}
+
+/* kernelu_1vs_0p, src/Kernels.h:362-405: vortex (vs) + source (ss) panel on a point */
+static inline void SFX(k1vs)(R sx0, R sy0, R sx1, R sy1, R vstr, R sstr, R tx, R ty, R* u, R* v) {
+  const R dx0 = tx - sx0, dy0 = ty - sy0, dx1 = tx - sx1, dy1 = ty - sy1;
+  R px = sx1 - sx0, py = sy1 - sy0;
+  const R rij2 = dx0*dx0 + dy0*dy0, rij12 = dx1*dx1 + dy1*dy1, panl = px*px + py*py;
+  const R mult = (R)1.0 / SQRT(panl);
+  px *= mult; py *= mult;
+  const R us = SFX(ustar)(dx0, dy0, dx1, dy1);
+  const R vs = (R)0.5 * LOG(rij2 / rij12);
+  *u = vstr * (us*px - vs*py) + sstr * (us*py + vs*px);
+  *v = vstr * (us*py + vs*px) + sstr * (vs*py - us*px);
+}
+
+/* kernelu_1vos_0p, src/Kernels.h:412-458: vortex and source parts kept separate (unit strengths) */
+static inline void SFX(k1vos)(R sx0, R sy0, R sx1, R sy1, R tx, R ty, R* vu, R* vv, R* su, R* sv) {
+  const R dx0 = tx - sx0, dy0 = ty - sy0, dx1 = tx - sx1, dy1 = ty - sy1;
+  R px = sx1 - sx0, py = sy1 - sy0;
+  const R rij2 = dx0*dx0 + dy0*dy0, rij12 = dx1*dx1 + dy1*dy1, panl = px*px + py*py;
+  const R mult = (R)1.0 / SQRT(panl);
+  px *= mult; py *= mult;
+  const R us = SFX(ustar)(dx0, dy0, dx1, dy1);
+  const R vs = (R)0.5 * LOG(rij2 / rij12);
+  *vu = us*px - vs*py;
+  *vv = us*py + vs*px;
+  *su = us*py + vs*px;
+  *sv = vs*py - us*px;
+}
+
+/* panels_affect_points, src/Influence.h:422-614 (x86 branch): ss == NULL selects the
+ * vortex-only kernelu_1v_0p loop (:576-594), otherwise kernelu_1vs_0p (:558-575). */
+void SFX(o_panels_affect_points)(const R* nx, const R* ny, int npan, const unsigned* idx,
+                                 const R* vs, const R* ss,
+                                 int nt, const R* tx, const R* ty, R* tu, R* tv) {
+  #pragma omp parallel for schedule(static)
+  for (int i = 0; i < nt; ++i) {
+    A au = 0, av = 0;
+    for (int j = 0; j < npan; ++j) {
+      const unsigned j0 = idx[2*j], j1 = idx[2*j+1];
+      R ru, rv;
+      if (ss) SFX(k1vs)(nx[j0], ny[j0], nx[j1], ny[j1], vs[j], ss[j], tx[i], ty[i], &ru, &rv);
+      else    SFX(k1v)(nx[j0], ny[j0], nx[j1], ny[j1], vs[j], tx[i], ty[i], &ru, &rv);
+      au += ru; av += rv;
+    }
+    tu[i] = (R)((A)tu[i] + au);
+    tv[i] = (R)((A)tv[i] + av);
+  }
+}
+
+/* points_affect_panels, src/Influence.h:633-771 (x86 branch): the panel is the "source" of
+ * kernelu_1v_0p and the particle the "target", so the sum is subtracted and scaled by the
+ * inverse panel length (ta = panel length, src/Surfaces.h:702-706). Particle radii unused. */
+void SFX(o_points_affect_panels)(int ns, const R* sx, const R* sy, const R* ss,
+                                 const R* nx, const R* ny, int npan, const unsigned* idx,
+                                 R* pu, R* pv) {
+  #pragma omp parallel for schedule(static)
+  for (int i = 0; i < npan; ++i) {
+    const unsigned i0 = idx[2*i], i1 = idx[2*i+1];
+    const R lx = nx[i1] - nx[i0], ly = ny[i1] - ny[i0];
+    const R ta = SQRT(lx*lx + ly*ly);
+    const A plen = (A)1.0 / (A)ta;
+    A au = 0, av = 0;
+    for (int j = 0; j < ns; ++j) {
+      R ru, rv;
+      SFX(k1v)(nx[i0], ny[i0], nx[i1], ny[i1], ss[j], sx[j], sy[j], &ru, &rv);
+      au += ru; av += rv;
+    }
+    pu[i] = (R)((A)pu[i] - plen * au);
+    pv[i] = (R)((A)pv[i] - plen * av);
+  }
+}
+
+/* panel bases, src/Surfaces.h:682-724: unit tangent node0->node1, normal to its left, length */
+static inline void SFX(panel_basis)(const R* nx, const R* ny, const unsigned* idx, int i,
+                                    R* tx, R* ty, R* nxo, R* nyo, R* len) {
+  const unsigned i0 = idx[2*i], i1 = idx[2*i+1];
+  R x1 = nx[i1] - nx[i0], y1 = ny[i1] - ny[i0];
+  const R base = SQRT(x1*x1 + y1*y1);
+  x1 = (R)((double)x1 * (1.0 / (double)base));
+  y1 = (R)((double)y1 * (1.0 / (double)base));
+  *tx = x1; *ty = y1; *nxo = -y1; *nyo = x1; *len = base;
+}
+
+/* panels_on_panels_coeff, src/Coefficients.h:155-427 (x86 branch, use_two_way = true):
+ * column-major nrows x ncols block (targets are rows), scaled by 1/(2 pi).  nunk = 2 is the
+ * reference's vortex+source system (src/Surfaces.h:69); nunk = 1 the vortex-only branch
+ * (:366-385).  self != 0 sets the self-influence diagonal pi (:389-401) before scaling. */
+void SFX(o_panels_on_panels_coeff)(int nunk, int self,
+                                   const R* snx, const R* sny, int nsrc, const unsigned* sidx,
+                                   const R* tnx, const R* tny, int ntarg, const unsigned* tidx,
+                                   R* out) {
+  const size_t nrows = (size_t)ntarg * nunk;
+  #pragma omp parallel for schedule(static)
+  for (int j = 0; j < nsrc; ++j) {
+    const unsigned s0 = sidx[2*j], s1 = sidx[2*j+1];
+    const R sx0 = snx[s0], sy0 = sny[s0], sx1 = snx[s1], sy1 = sny[s1];
+    R stx, sty, snx_, sny_, sa;
+    SFX(panel_basis)(snx, sny, sidx, j, &stx, &sty, &snx_, &sny_, &sa);
+    R* col1 = out + (size_t)j * nunk * nrows;
+    R* col2 = col1 + nrows;
+    for (int i = 0; i < ntarg; ++i) {
+      const unsigned t0 = tidx[2*i], t1 = tidx[2*i+1];
+      const R tx0 = tnx[t0], ty0 = tny[t0], tx1 = tnx[t1], ty1 = tny[t1];
+      R ttx, tty, tnx_, tny_, ta;
+      SFX(panel_basis)(tnx, tny, tidx, i, &ttx, &tty, &tnx_, &tny_, &ta);
+      const R xi = (R)0.5 * (tx1 + tx0), yi = (R)0.5 * (ty1 + ty0);
+      if (nunk == 2) {
+        R vu, vv, su, sv;
+        SFX(k1vos)(sx0, sy0, sx1, sy1, xi, yi, &vu, &vv, &su, &sv);
+        R c11 = vu*ttx + vv*tty, c12 = vu*tnx_ + vv*tny_;
+        R c21 = su*ttx + sv*tty, c22 = su*tnx_ + sv*tny_;
+        SFX(k1vos)(tx0, ty0, tx1, ty1, (R)0.5*(sx0+sx1), (R)0.5*(sy0+sy1), &vu, &vv, &su, &sv);
+        const R fact = sa / ta;
+        c11 -= fact * (vu*ttx + vv*tty);
+        c12 -= fact * (vu*tnx_ + vv*tny_);
+        c21 -= fact * (su*ttx + sv*tty);
+        c22 -= fact * (su*tnx_ + sv*tny_);
+        col1[2*i] = c11 * (R)0.5; col1[2*i+1] = c12 * (R)0.5;
+        col2[2*i] = c21 * (R)0.5; col2[2*i+1] = c22 * (R)0.5;
+      } else {
+        R vu, vv;
+        SFX(k1v)(sx0, sy0, sx1, sy1, (R)1.0, xi, yi, &vu, &vv);
+        R c = vu*ttx + vv*tty;
+        SFX(k1v)(tx0, ty0, tx1, ty1, (R)1.0, (R)0.5*(sx0+sx1), (R)0.5*(sy0+sy1), &vu, &vv);
+        c -= (vu*ttx + vv*tty) * (sa / ta);
+        col1[i] = c * (R)0.5;
+      }
+    }
+    if (self) {
+      if (nunk == 2) {
+        col1[2*j] = (R)M_PI; col1[2*j+1] = (R)0;
+        col2[2*j] = (R)0;    col2[2*j+1] = (R)M_PI;
+      } else {
+        col1[j] = (R)M_PI;
+      }
+    }
+    const R fac = (R)(1.0 / (2.0 * M_PI));
+    for (size_t k = 0; k < (size_t)nunk * nrows; ++k) col1[k] *= fac;
+  }
+}
+
+/* vels_to_rhs_panels, src/RHS.h:54-115 */
+void SFX(o_vels_to_rhs_panels)(int nunk, const R* nx, const R* ny, int npan, const unsigned* idx,
+                               const R* pu, const R* pv, const R* bcn, R* rhs) {
+  for (int i = 0; i < npan; ++i) {
+    R ttx, tty, tnx_, tny_, len;
+    SFX(panel_basis)(nx, ny, idx, i, &ttx, &tty, &tnx_, &tny_, &len);
+    if (nunk == 1) {
+      rhs[i] = -(pu[i]*ttx + pv[i]*tty);
+    } else {
+      rhs[2*i] = -(pu[i]*ttx + pv[i]*tty);
+      rhs[2*i+1] = -(pu[i]*tnx_ + pv[i]*tny_) + (bcn ? bcn[i] : (R)0);
+    }
+  }
+}
+
+/* ElementBase::finalize_vels, src/ElementBase.h:215-234: u = fs + u/(2 pi) */
+void SFX(o_finalize_vels)(int n, R* u, R* v, double fsx, double fsy) {
+  const double factor = 0.5 / M_PI;
+  for (int i = 0; i < n; ++i) {
+    u[i] = (R)(fsx + u[i] * factor);
+    v[i] = (R)(fsy + v[i] * factor);
+  }
+}
+
+/* One velocity evaluation of particles on themselves, finalized (src/Convection.h:172-223). */
+static void SFX(self_vels)(int core, int n, const R* x, const R* y, const R* r, const R* s,
+                           double fsx, double fsy, R* u, R* v) {
+  for (int i = 0; i < n; ++i) { u[i] = 0; v[i] = 0; }
+  SFX(o_points_affect_points)(core, 1, n, x, y, r, s, n, x, y, r, u, v, 0, 0, 0, 0);
+  SFX(o_finalize_vels)(n, u, v, fsx, fsy);
+}
+
+/* Convection::advect_1st without bodies (src/Convection.h:274-303, ElementBase.h:276-296) */
+void SFX(o_advect_1st)(int core, int n, R* x, R* y, const R* r, const R* s,
+                       double fsx, double fsy, double dt, int nsteps) {
+  R* u = (R*)malloc(sizeof(R) * (size_t)n);
+  R* v = (R*)malloc(sizeof(R) * (size_t)n);
+  for (int k = 0; k < nsteps; ++k) {
+    SFX(self_vels)(core, n, x, y, r, s, fsx, fsy, u, v);
+    for (int i = 0; i < n; ++i) {
+      x[i] += (R)dt * (R)(1.0 * u[i]);
+      y[i] += (R)dt * (R)(1.0 * v[i]);
+    }
+  }
+  free(u); free(v);
+}
+
+/* Convection::advect_2nd_ralston without bodies (src/Convection.h:390-466,
+ * ElementBase.h:299-327): u = 1/4 u(x) + 3/4 u(x + 2/3 dt u(x)); x += dt u */
+void SFX(o_advect_2nd_ralston)(int core, int n, R* x, R* y, const R* r, const R* s,
+                               double fsx, double fsy, double dt, int nsteps) {
+  R* u1 = (R*)malloc(sizeof(R) * (size_t)n);
+  R* v1 = (R*)malloc(sizeof(R) * (size_t)n);
+  R* u2 = (R*)malloc(sizeof(R) * (size_t)n);
+  R* v2 = (R*)malloc(sizeof(R) * (size_t)n);
+  R* x2 = (R*)malloc(sizeof(R) * (size_t)n);
+  R* y2 = (R*)malloc(sizeof(R) * (size_t)n);
+  const double tt = 2.0 / 3.0;
+  for (int k = 0; k < nsteps; ++k) {
+    SFX(self_vels)(core, n, x, y, r, s, fsx, fsy, u1, v1);
+    for (int i = 0; i < n; ++i) {
+      x2[i] = x[i] + (R)(tt * dt) * (R)(1.0 * u1[i]);
+      y2[i] = y[i] + (R)(tt * dt) * (R)(1.0 * v1[i]);
+    }
+    SFX(self_vels)(core, n, x2, y2, r, s, fsx, fsy, u2, v2);
+    for (int i = 0; i < n; ++i) {
+      const R uu = (R)(0.25 * u1[i] + 0.75 * u2[i]);
+      const R vv = (R)(0.25 * v1[i] + 0.75 * v2[i]);
+      x[i] += (R)dt * uu;
+      y[i] += (R)dt * vv;
+    }
+  }
+  free(u1); free(v1); free(u2); free(v2); free(x2); free(y2);
+}

@@ -1,0 +1,374 @@
+// ref_harness.cpp -- C-ABI wrapper around the reference's own influence code (test infrastructure).
+//
+// This file is compiled, by oracle/build_ref.py, against the reference's unmodified headers
+// (src/Influence.h, src/Kernels.h, src/CoreFunc.h, src/Coefficients.h, src/RHS.h, src/Points.h,
+// src/Surfaces.h, src/ElementBase.h), once per core-function macro (src/CoreFunc.h:35-39).
+// The resulting libraries live in oracle/_ref/ and are used ONLY as a checker by the tests and
+// by tests/golden/make_golden.py; nothing in the product path links or loads them.
+//
+// Every entry point below builds the reference's own element containers from flat SoA arrays,
+// calls the reference driver, and copies the result back out.  Where the reference has no
+// driver for a kernel (kernelug_0v_0b, kernelu_1v_0p-only panels), the loop mirrors the
+// velocity-only driver loop it sits beside and calls the reference kernel function per pair.
+
+#include "Omega2D.h"
+#include "Collection.h"
+#include "Influence.h"
+#include "Coefficients.h"
+#include "RHS.h"
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <unistd.h>
+#include <fcntl.h>
+
+namespace {
+
+// The reference prints several lines per driver call (std::cout and printf).  Silence both for
+// the duration of a call so test output and timing stay clean.
+struct Quiet {
+  int saved_fd;
+  std::streambuf* saved_buf;
+  Quiet() {
+    fflush(stdout);
+    saved_fd = dup(1);
+    int devnull = open("/dev/null", O_WRONLY);
+    if (devnull >= 0) { dup2(devnull, 1); close(devnull); }
+    saved_buf = std::cout.rdbuf(nullptr);
+  }
+  ~Quiet() {
+    fflush(stdout);
+    std::cout.rdbuf(saved_buf);
+    if (saved_fd >= 0) { dup2(saved_fd, 1); close(saved_fd); }
+  }
+};
+
+template <class S>
+Points<S> make_points(int n, const S* x, const S* y, const S* r, const S* s, bool is_field_point) {
+  std::vector<S> xy(2 * (size_t)n);
+  for (int i = 0; i < n; ++i) { xy[2*i] = x[i]; xy[2*i+1] = y[i]; }
+  std::vector<S> val;
+  if (!is_field_point) val.assign(s, s + n);
+  ElementPacket<S> pk(xy, std::vector<Int>(), val, (size_t)n, 0);
+  Points<S> p(pk, is_field_point ? inert : active, lagrangian, nullptr, 1.0f);
+  if (!is_field_point) {
+    Vector<S>& rr = p.get_rad();
+    for (int i = 0; i < n; ++i) rr[i] = r[i];
+  }
+  return p;
+}
+
+template <class S>
+Surfaces<S> make_surfaces(int nnodes, const S* nx, const S* ny, int npan, const unsigned* idx,
+                          const S* v0, const S* v1, elem_t etype) {
+  std::vector<float> xy(2 * (size_t)nnodes);
+  for (int i = 0; i < nnodes; ++i) { xy[2*i] = (float)nx[i]; xy[2*i+1] = (float)ny[i]; }
+  std::vector<Int> id(idx, idx + 2 * (size_t)npan);
+  std::vector<float> val(2 * (size_t)npan, 0.0f);
+  for (int i = 0; i < npan; ++i) {
+    val[2*i]   = v0 ? (float)v0[i] : 0.0f;
+    val[2*i+1] = v1 ? (float)v1[i] : 0.0f;
+  }
+  ElementPacket<float> pk(xy, id, val, (size_t)npan, 1);
+  return Surfaces<S>(pk, etype, fixed, nullptr);
+}
+
+template <class S>
+void copy_in_vel(Points<S>& p, int n, const S* u, const S* v) {
+  auto& vel = p.get_vel();
+  for (int i = 0; i < n; ++i) { vel[0][i] = u[i]; vel[1][i] = v[i]; }
+}
+
+template <class S>
+void copy_out_vel(const Points<S>& p, int n, S* u, S* v) {
+  const auto& vel = p.get_vel();
+  for (int i = 0; i < n; ++i) { u[i] = vel[0][i]; v[i] = vel[1][i]; }
+}
+
+// points_affect_points (src/Influence.h:56-416), x86 branch; restype as results_t
+template <class S, class A>
+int ppts(int ns, const S* sx, const S* sy, const S* sr, const S* ss,
+         int nt, const S* tx, const S* ty, const S* tr, int restype,
+         S* tu, S* tv, S* textra) {
+  Quiet q;
+  Points<S> src = make_points<S>(ns, sx, sy, sr, ss, false);
+  std::vector<S> dummy_s(nt, S(0));
+  Points<S> targ = make_points<S>(nt, tx, ty, tr, dummy_s.data(), tr == nullptr);
+  copy_in_vel(targ, nt, tu, tv);
+  if (restype == velandvort) {
+    Vector<S>& w = targ.get_vort();
+    for (int i = 0; i < nt; ++i) w[i] = textra[i];
+  } else if (restype == velandshear) {
+    Vector<S>& e = targ.get_shear();
+    for (int i = 0; i < nt; ++i) e[i] = textra[i];
+  }
+  points_affect_points<S, A>(src, targ, ResultsType((results_t)restype), ExecEnv(true, direct, cpu_x86));
+  copy_out_vel(targ, nt, tu, tv);
+  if (restype == velandvort) {
+    const Vector<S>& w = targ.get_vort();
+    for (int i = 0; i < nt; ++i) textra[i] = w[i];
+  } else if (restype == velandshear) {
+    const Vector<S>& e = targ.get_shear();
+    for (int i = 0; i < nt; ++i) textra[i] = e[i];
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ref_points_affect_points_f(int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                               int nt, const float* tx, const float* ty, const float* tr, int restype,
+                               float* tu, float* tv, float* textra) {
+  return ppts<float, double>(ns, sx, sy, sr, ss, nt, tx, ty, tr, restype, tu, tv, textra);
+}
+
+int ref_points_affect_points_d(int ns, const double* sx, const double* sy, const double* sr, const double* ss,
+                               int nt, const double* tx, const double* ty, const double* tr, int restype,
+                               double* tu, double* tv, double* textra) {
+  return ppts<double, double>(ns, sx, sy, sr, ss, nt, tx, ty, tr, restype, tu, tv, textra);
+}
+
+// kernelug_0v_0b (src/Kernels.h:112-133) has no driver in the reference; this loop mirrors the
+// velonly x86 loop of src/Influence.h:347-363 with the gradient kernel in its place.
+// grads: [ux, vx, uy, vy] accumulated (+=) like the velocity.
+int ref_velgrad_thick_f(int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                        int nt, const float* tx, const float* ty, const float* tr,
+                        float* tu, float* tv, float* tux, float* tvx, float* tuy, float* tvy) {
+  #pragma omp parallel for
+  for (int i = 0; i < nt; ++i) {
+    double au = 0, av = 0, aux = 0, avx = 0, auy = 0, avy = 0;
+    for (int j = 0; j < ns; ++j) {
+      kernelug_0v_0b<float, double>(sx[j], sy[j], sr[j], ss[j], tx[i], ty[i], tr[i],
+                                    &au, &av, &aux, &avx, &auy, &avy);
+    }
+    tu[i] += au; tv[i] += av; tux[i] += aux; tvx[i] += avx; tuy[i] += auy; tvy[i] += avy;
+  }
+  return 0;
+}
+
+int ref_velgrad_thick_d(int ns, const double* sx, const double* sy, const double* sr, const double* ss,
+                        int nt, const double* tx, const double* ty, const double* tr,
+                        double* tu, double* tv, double* tux, double* tvx, double* tuy, double* tvy) {
+  #pragma omp parallel for
+  for (int i = 0; i < nt; ++i) {
+    double au = 0, av = 0, aux = 0, avx = 0, auy = 0, avy = 0;
+    for (int j = 0; j < ns; ++j) {
+      kernelug_0v_0b<double, double>(sx[j], sy[j], sr[j], ss[j], tx[i], ty[i], tr[i],
+                                     &au, &av, &aux, &avx, &auy, &avy);
+    }
+    tu[i] += au; tv[i] += av; tux[i] += aux; tvx[i] += avx; tuy[i] += auy; tvy[i] += avy;
+  }
+  return 0;
+}
+
+// panels_affect_points (src/Influence.h:422-614): active panels carrying vortex (vs) and
+// source (ss) sheet strengths; the reference always takes the kernelu_1vs_0p branch here
+// because active Surfaces always hold both strength arrays (src/Surfaces.h:86-92, 139-156).
+int ref_panels_affect_points_f(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                               const float* vs, const float* ss,
+                               int nt, const float* tx, const float* ty, float* tu, float* tv) {
+  Quiet q;
+  Surfaces<float> src = make_surfaces<float>(nnodes, nx, ny, npan, idx, vs, ss, active);
+  Points<float> targ = make_points<float>(nt, tx, ty, nullptr, nullptr, true);
+  copy_in_vel(targ, nt, tu, tv);
+  panels_affect_points<float, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  copy_out_vel(targ, nt, tu, tv);
+  return 0;
+}
+
+int ref_panels_affect_points_d(int nnodes, const double* nx, const double* ny, int npan, const unsigned* idx,
+                               const double* vs, const double* ss,
+                               int nt, const double* tx, const double* ty, double* tu, double* tv) {
+  Quiet q;
+  Surfaces<double> src = make_surfaces<double>(nnodes, nx, ny, npan, idx, vs, ss, active);
+  // node positions pass through the float ElementPacket; restore them at full precision
+  auto& px = src.get_pos();
+  for (int i = 0; i < nnodes; ++i) { px[0][i] = nx[i]; px[1][i] = ny[i]; }
+  auto& pv = src.get_str();
+  for (int i = 0; i < npan; ++i) pv[i] = vs[i];
+  auto& ps = src.get_src_str();
+  for (int i = 0; i < npan; ++i) ps[i] = ss ? ss[i] : 0.0;
+  Points<double> targ = make_points<double>(nt, tx, ty, nullptr, nullptr, true);
+  copy_in_vel(targ, nt, tu, tv);
+  panels_affect_points<double, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  copy_out_vel(targ, nt, tu, tv);
+  return 0;
+}
+
+// vortex-only panel branch of src/Influence.h:576-594 (kernelu_1v_0p per pair)
+int ref_panels_affect_points_vortex_f(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                      const float* vs, int nt, const float* tx, const float* ty,
+                                      float* tu, float* tv) {
+  #pragma omp parallel for
+  for (int i = 0; i < nt; ++i) {
+    double au = 0, av = 0, ru = 0, rv = 0;
+    for (int j = 0; j < npan; ++j) {
+      const unsigned j0 = idx[2*j], j1 = idx[2*j+1];
+      kernelu_1v_0p<float, double>(nx[j0], ny[j0], nx[j1], ny[j1], vs[j], tx[i], ty[i], &ru, &rv);
+      au += ru; av += rv;
+    }
+    tu[i] += au; tv[i] += av;
+  }
+  return 0;
+}
+
+// points_affect_panels (src/Influence.h:633-771): mean velocity on each reactive target panel
+int ref_points_affect_panels_f(int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                               int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                               float* pu, float* pv) {
+  Quiet q;
+  Points<float> src = make_points<float>(ns, sx, sy, sr, ss, false);
+  Surfaces<float> targ = make_surfaces<float>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  auto& vel = targ.get_vel();
+  for (int i = 0; i < npan; ++i) { vel[0][i] = pu[i]; vel[1][i] = pv[i]; }
+  points_affect_panels<float, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  for (int i = 0; i < npan; ++i) { pu[i] = vel[0][i]; pv[i] = vel[1][i]; }
+  return 0;
+}
+
+int ref_points_affect_panels_d(int ns, const double* sx, const double* sy, const double* sr, const double* ss,
+                               int nnodes, const double* nx, const double* ny, int npan, const unsigned* idx,
+                               double* pu, double* pv) {
+  Quiet q;
+  Points<double> src = make_points<double>(ns, sx, sy, sr, ss, false);
+  Surfaces<double> targ = make_surfaces<double>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  auto& px = targ.get_pos();
+  for (int i = 0; i < nnodes; ++i) { px[0][i] = nx[i]; px[1][i] = ny[i]; }
+  targ.transform(0.0);   // recompute bases and areas from the full-precision nodes
+  auto& vel = targ.get_vel();
+  for (int i = 0; i < npan; ++i) { vel[0][i] = pu[i]; vel[1][i] = pv[i]; }
+  points_affect_panels<double, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  for (int i = 0; i < npan; ++i) { pu[i] = vel[0][i]; pv[i] = vel[1][i]; }
+  return 0;
+}
+
+// panels_on_panels_coeff (src/Coefficients.h:155-573), self block (src == targ): column-major
+// (2*npan) x (2*npan) matrix, already scaled by 1/(2 pi), self terms pi/(2 pi).
+int ref_panels_on_panels_coeff_f(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                 float* out) {
+  Quiet q;
+  Surfaces<float> s = make_surfaces<float>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  Vector<float> c = panels_on_panels_coeff<float>(s, s);
+  std::memcpy(out, c.data(), c.size() * sizeof(float));
+  return (int)c.size();
+}
+
+int ref_panels_on_panels_coeff_d(int nnodes, const double* nx, const double* ny, int npan, const unsigned* idx,
+                                 double* out) {
+  Quiet q;
+  Surfaces<double> s = make_surfaces<double>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  auto& px = s.get_pos();
+  for (int i = 0; i < nnodes; ++i) { px[0][i] = nx[i]; px[1][i] = ny[i]; }
+  s.transform(0.0);
+  Vector<double> c = panels_on_panels_coeff<double>(s, s);
+  std::memcpy(out, c.data(), c.size() * sizeof(double));
+  return (int)c.size();
+}
+
+// off-diagonal block: distinct source and target collections (no self term)
+int ref_panels_on_panels_coeff_pair_f(int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                                      int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                                      float* out) {
+  Quiet q;
+  Surfaces<float> s = make_surfaces<float>(snn, snx, sny, snp, sidx, nullptr, nullptr, reactive);
+  Surfaces<float> t = make_surfaces<float>(tnn, tnx, tny, tnp, tidx, nullptr, nullptr, reactive);
+  Vector<float> c = panels_on_panels_coeff<float>(s, t);
+  std::memcpy(out, c.data(), c.size() * sizeof(float));
+  return (int)c.size();
+}
+
+// vels_to_rhs_panels (src/RHS.h:54-115) with 2 unknowns per panel
+int ref_vels_to_rhs_panels_f(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                             const float* pu, const float* pv, const float* bct, const float* bcn, float* rhs) {
+  Quiet q;
+  Surfaces<float> s = make_surfaces<float>(nnodes, nx, ny, npan, idx, bct, bcn, reactive);
+  auto& vel = s.get_vel();
+  for (int i = 0; i < npan; ++i) { vel[0][i] = pu[i]; vel[1][i] = pv[i]; }
+  std::vector<float> r = vels_to_rhs_panels<float>(s);
+  std::memcpy(rhs, r.data(), r.size() * sizeof(float));
+  return (int)r.size();
+}
+
+// Surfaces::finalize_vels (src/Surfaces.h:764-774) on panel-centre velocities
+int ref_finalize_panel_vels_f(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                              double fsx, double fsy, float* pu, float* pv) {
+  Quiet q;
+  Surfaces<float> s = make_surfaces<float>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  auto& vel = s.get_vel();
+  for (int i = 0; i < npan; ++i) { vel[0][i] = pu[i]; vel[1][i] = pv[i]; }
+  s.finalize_vels({fsx, fsy});
+  for (int i = 0; i < npan; ++i) { pu[i] = vel[0][i]; pv[i] = vel[1][i]; }
+  return 0;
+}
+
+// ElementBase::finalize_vels (src/ElementBase.h:215-234)
+int ref_finalize_vels_f(int n, float* u, float* v, double fsx, double fsy) {
+  Quiet q;
+  std::vector<float> x(n, 0.0f), r(n, 1.0f), s(n, 0.0f);
+  Points<float> p = make_points<float>(n, x.data(), x.data(), r.data(), s.data(), false);
+  copy_in_vel(p, n, u, v);
+  p.finalize_vels({fsx, fsy});
+  copy_out_vel(p, n, u, v);
+  return 0;
+}
+
+// Convection::advect_1st (src/Convection.h:274-303) without bodies: per step
+// zero_vels -> points_affect_points(p, p) -> finalize_vels(fs) -> move(dt)
+int ref_advect_1st_f(int n, float* x, float* y, const float* r, const float* s,
+                     double fsx, double fsy, double dt, int nsteps) {
+  Quiet q;
+  Points<float> p = make_points<float>(n, x, y, r, s, false);
+  double t = 0.0;
+  for (int k = 0; k < nsteps; ++k) {
+    p.zero_vels();
+    points_affect_points<float, double>(p, p, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p.finalize_vels({fsx, fsy});
+    p.move(t, dt, 1.0, p);
+    t += dt;
+  }
+  const auto& px = p.get_pos();
+  for (int i = 0; i < n; ++i) { x[i] = px[0][i]; y[i] = px[1][i]; }
+  return 0;
+}
+
+// Convection::advect_2nd_ralston (src/Convection.h:390-466) without bodies
+int ref_advect_2nd_ralston_f(int n, float* x, float* y, const float* r, const float* s,
+                             double fsx, double fsy, double dt, int nsteps) {
+  Quiet q;
+  Points<float> p = make_points<float>(n, x, y, r, s, false);
+  double t = 0.0;
+  const double twothirds = 2.0 / 3.0;
+  for (int k = 0; k < nsteps; ++k) {
+    p.zero_vels();
+    points_affect_points<float, double>(p, p, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p.finalize_vels({fsx, fsy});
+    Points<float> p2 = p;
+    p2.move(t, twothirds * dt, 1.0, p2);
+    p2.zero_vels();
+    points_affect_points<float, double>(p2, p2, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p2.finalize_vels({fsx, fsy});
+    p.move(t, dt, 0.25, p, 0.75, p2);
+    t += dt;
+  }
+  const auto& px = p.get_pos();
+  for (int i = 0; i < n; ++i) { x[i] = px[0][i]; y[i] = px[1][i]; }
+  return 0;
+}
+
+// flop counts the reference attaches to each kernel (src/Kernels.h flops*, src/CoreFunc.h flops_*)
+int ref_flop_counts(int* out) {
+  out[0] = (int)flopsu_0v_0b<float, double>();
+  out[1] = (int)flopsu_0v_0p<float, double>();
+  out[2] = (int)flopsug_0v_0b<float, double>();
+  out[3] = (int)flopsuw_0v_0b<float, double>();
+  out[4] = (int)flopsue_0v_0b<float, double>();
+  out[5] = (int)flopsu_1v_0p<float, double>();
+  out[6] = (int)flopsu_1vs_0p<float, double>();
+  out[7] = (int)flopsu_1vos_0p<float, double>();
+  return 8;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference's own compiled code.
+
+Run in a checkout that has the reference tree (it builds oracle/_ref first):
+
+    python tests/golden/make_golden.py
+
+Every fixture stores its seeded inputs and the reference outputs (float32 storage, double
+accumulators: the reference's default non-Vc build).  The reference itself has no tests or
+fixtures for this path; these vectors are produced by compiling its src/Influence.h,
+src/Kernels.h, src/CoreFunc.h, src/Coefficients.h and src/RHS.h unmodified (see
+oracle/build_ref.py) and calling its drivers through oracle/ref_harness.cpp.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import build_ref, pyoracle as po  # noqa: E402
+
+CORES = {"rm": po.RM, "exp": po.GAUSS, "v2": po.V2, "wl": po.WL, "v3": po.V3}
+
+
+def particles(rng, n, lo=-1.0, hi=1.0, rmin=0.02, rmax=0.08):
+    x = rng.uniform(lo, hi, n).astype(np.float32)
+    y = rng.uniform(lo, hi, n).astype(np.float32)
+    r = rng.uniform(rmin, rmax, n).astype(np.float32)
+    s = rng.normal(0.0, 1.0 / np.sqrt(n), n).astype(np.float32)
+    return x, y, r, s
+
+
+def circle_panels(npan, diameter=1.0):
+    """Clockwise circle nodes (fluid to the left walking node0 -> node1), as
+    SolidCircle builds them (src/BoundaryFeature.cpp:489-531)."""
+    th = -2.0 * np.pi * np.arange(npan) / npan
+    nx = (0.5 * diameter * np.cos(th)).astype(np.float32)
+    ny = (0.5 * diameter * np.sin(th)).astype(np.float32)
+    idx = np.stack([np.arange(npan), (np.arange(npan) + 1) % npan], 1).ravel().astype(np.uint32)
+    return nx, ny, idx
+
+
+def make_p2p(out):
+    rng = np.random.default_rng(20240601)
+    ns, nt = 257, 193
+    sx, sy, sr, ss = particles(rng, ns)
+    # targets: 40 coincide with sources (self pairs), the rest are fresh points
+    tx, ty, tr, _ = particles(rng, nt)
+    tx[:40], ty[:40], tr[:40] = sx[:40], sy[:40], sr[:40]
+    tu0 = rng.normal(0, 0.1, nt).astype(np.float32)   # non-zero: the drivers accumulate
+    tv0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    ex0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    d = dict(sx=sx, sy=sy, sr=sr, ss=ss, tx=tx, ty=ty, tr=tr, tu0=tu0, tv0=tv0, ex0=ex0)
+    for name, core in CORES.items():
+        ref = po.Reference(core)
+        for restype in (po.VELONLY, po.VELANDVORT, po.VELANDSHEAR):
+            for thick in (True, False):
+                tu, tv, ex = ref.points_affect_points(restype, sx, sy, sr, ss, tx, ty, tr if thick else None,
+                                                      tu=tu0, tv=tv0, extra=ex0)
+                key = f"{name}_r{restype}_{'b' if thick else 'p'}"
+                d[key + "_u"], d[key + "_v"] = tu, tv
+                if restype != po.VELONLY:
+                    d[key + "_e"] = ex
+        g = ref.velgrad_thick(sx, sy, sr, ss, tx, ty, tr)
+        for k, nm in enumerate(["u", "v", "ux", "vx", "uy", "vy"]):
+            d[f"{name}_grad_{nm}"] = g[k]
+        d[f"{name}_flops"] = np.array(list(ref.flop_counts().values()), np.int32)
+    np.savez_compressed(out, **d)
+
+
+def make_panels(out):
+    rng = np.random.default_rng(20240602)
+    npan = 64
+    nx, ny, idx = circle_panels(npan)
+    vs = rng.normal(0, 1, npan).astype(np.float32)
+    ss = rng.normal(0, 1, npan).astype(np.float32)
+    nt = 150
+    rr = np.sqrt(rng.uniform(0.55 ** 2, 3.0 ** 2, nt))
+    aa = rng.uniform(0, 2 * np.pi, nt)
+    tx = (rr * np.cos(aa)).astype(np.float32)
+    ty = (rr * np.sin(aa)).astype(np.float32)
+    tr = np.full(nt, 0.01, np.float32)
+    tg = rng.normal(0, 1e-2, nt).astype(np.float32)
+    ref = po.Reference(po.V2)
+    d = dict(nx=nx, ny=ny, idx=idx, vs=vs, ss=ss, tx=tx, ty=ty, tr=tr, tg=tg)
+    d["p2pt_1vs_u"], d["p2pt_1vs_v"] = ref.panels_affect_points(nx, ny, idx, vs, ss, tx, ty)
+    d["p2pt_1v_u"], d["p2pt_1v_v"] = ref.panels_affect_points(nx, ny, idx, vs, None, tx, ty)
+    d["pt2p_u"], d["pt2p_v"] = ref.points_affect_panels(tx, ty, tr, tg, nx, ny, idx)
+    d["coeff"] = ref.panels_on_panels_coeff(nx, ny, idx)
+    pu = rng.normal(0, 1, npan).astype(np.float32)
+    pv = rng.normal(0, 1, npan).astype(np.float32)
+    bcn = rng.normal(0, 0.1, npan).astype(np.float32)
+    d["pu"], d["pv"], d["bcn"] = pu, pv, bcn
+    d["rhs"] = ref.vels_to_rhs_panels(nx, ny, idx, pu, pv, np.zeros(npan, np.float32), bcn)
+    d["fin_u"], d["fin_v"] = ref.finalize_vels(pu, pv, (1.0, -0.5))
+    np.savez_compressed(out, **d)
+
+
+def make_advect(out):
+    rng = np.random.default_rng(20240603)
+    n = 300
+    x, y, _, s = particles(rng, n)
+    r = np.full(n, 0.05, np.float32)
+    d = dict(x=x, y=y, r=r, s=s)
+    d["euler_x"], d["euler_y"] = po.Reference(po.RM).advect(1, x, y, r, s, (1.0, 0.0), 0.01, 10)
+    d["rk2_x"], d["rk2_y"] = po.Reference(po.GAUSS).advect(2, x, y, r, s, (0.0, 0.0), 0.01, 4)
+    np.savez_compressed(out, **d)
+
+
+def main():
+    if not build_ref.available():
+        raise SystemExit("the reference tree is needed to generate golden vectors")
+    build_ref.build()
+    make_p2p(os.path.join(HERE, "p2p.npz"))
+    make_panels(os.path.join(HERE, "panels.npz"))
+    make_advect(os.path.join(HERE, "advect.npz"))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,77 @@
+"""CPU tests of the C ABI surface: the engine library loads, exports every function declared in
+include/*.h, and rejects bad arguments without touching a GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "defined"):
+                names.add(name)
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("obs_create", "obs_points_affect_points", "external_vel_solver_f_",
+                 "external_vel_solver_tr_f_", "external_vel_solver_d_"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    missing = [n for n in declared_functions() if not hasattr(engine_lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings(engine_lib):
+    engine_lib.obs_status_string.restype = ctypes.c_char_p
+    assert engine_lib.obs_status_string(0) == b"ok"
+    assert engine_lib.obs_status_string(-1) == b"invalid argument"
+    assert engine_lib.obs_status_string(-4) == b"device wait timed out"
+
+
+def test_null_context_is_rejected(engine_lib):
+    assert engine_lib.obs_destroy(None) == -1
+    assert engine_lib.obs_synchronize(None) == -1
+    z = np.zeros(4, np.float32)
+    p = z.ctypes.data_as(ctypes.c_void_p)
+    st = engine_lib.obs_points_affect_points(None, 1, 1, 0, 0, ctypes.c_double(0), ctypes.c_double(0),
+                                             4, p, p, p, p, 4, p, p, None, p, p, None, None, None, None, None)
+    assert st == -1
+
+
+def test_create_without_device_reports_no_device(engine_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    h = ctypes.c_void_p()
+    assert engine_lib.obs_create(ctypes.byref(h), 0) == -5
+
+
+def test_flops_per_pair_matches_reference_counts(engine_lib, golden):
+    g = golden("p2p")
+    # thick-target velocity, field-point velocity, thick-target gradient (src/Kernels.h flops*)
+    for name, core in (("rm", 1), ("exp", 2), ("v2", 3), ("wl", 4), ("v3", 5)):
+        ref = list(g[f"{name}_flops"])
+        assert engine_lib.obs_flops_per_pair(core, 1, 1) == ref[0]
+        assert engine_lib.obs_flops_per_pair(core, 1, 0) == ref[1]
+        assert engine_lib.obs_flops_per_pair(core, 2, 1) == ref[2]
+        assert engine_lib.obs_flops_per_pair(core, 4, 1) == ref[3]
+        assert engine_lib.obs_flops_per_pair(core, 5, 1) == ref[4]
+
+
+def test_external_solver_rejects_null_counts(engine_lib):
+    engine_lib.external_vel_solver_f_.restype = ctypes.c_float
+    assert engine_lib.external_vel_solver_f_(None, None, None, None, None, None, None, None, None, None) < 0
