@@ -263,8 +263,9 @@ int obs_points_affect_points(obs_context* ctx, int core, int result, int accum, 
   const bool vel = result != OBS_PSIONLY;
   // staging layout (floats): sx sy sr ss | tx ty tr | tu tv | extras
   const size_t S = (size_t)ns, T = (size_t)nt;
-  const size_t nfloat = 4 * S + 3 * T + 2 * T + 4 * T;
-  s = ctx->io.ensure(nfloat * sizeof(float) + 64 * 16, ctx->stream);
+  // 13 sub-arrays, each rounded up to a multiple of 64 floats
+  const size_t nfloat = 4 * S + 3 * T + 2 * T + 4 * T + 13 * 64;
+  s = ctx->io.ensure(nfloat * sizeof(float), ctx->stream);
   if (s) return s;
   float* base = ctx->io.as<float>();
   auto align = [](size_t n) { return (n + 63) & ~(size_t)63; };
