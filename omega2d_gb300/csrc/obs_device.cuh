@@ -19,7 +19,6 @@ enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2 };
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;
-constexpr float kPadCoord = 3.0e18f;   // padded sources sit here with zero strength
 
 // ---------------------------------------------------------------- PTX approximations
 // Documented PTX forms; maximum errors per the PTX ISA: rcp 1 ulp, sqrt/rsqrt ~2 ulp,

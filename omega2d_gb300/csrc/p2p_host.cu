@@ -27,7 +27,8 @@ __device__ __forceinline__ void fold_extrema(bool active, float r, unsigned* met
 }
 
 // Pack the caller's SoA sources into float4 (x, y, radius term, strength), padded to whole
-// tiles with zero-strength sources far away, and record the radius extrema in meta[0..1].
+// tiles with zero-strength sources at the origin (radius term 1 keeps every core and every
+// gradient form finite there, so 0 * K stays 0), and record the radius extrema in meta[0..1].
 __global__ void pack_sources_kernel(const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ sr, const float* __restrict__ ss,
                                     int ns, int ns_pad, int core, float4* __restrict__ out,
@@ -37,7 +38,7 @@ __global__ void pack_sources_kernel(const float* __restrict__ sx, const float* _
   if (i < ns) {
     out[i] = make_float4(sx[i], sy[i], radius_term(core, r), ss[i]);
   } else if (i < ns_pad) {
-    out[i] = make_float4(kPadCoord, kPadCoord, 1.0f, 0.0f);
+    out[i] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
   }
   fold_extrema(i < ns, r, meta);
 }
