@@ -1,0 +1,333 @@
+"""Benchmark: direct Biot-Savart velocity, 1,000,000 particles, Gaussian core (one GB300).
+
+Workload (the precision configuration): 1M particles, positions ~ N(0, 0.25^2 I) in FP32,
+strength proportional to exp(-r^2/0.125) normalised to total 1, core radius 0.005, Gaussian
+("exponential") core, thick targets = the particles themselves.  One step = one full
+N x N velocity evaluation (10^12 interactions, self pair included) through the engine.
+
+  value : compensated-FP32 Ginteractions/s, device-resident inputs, main + reduce kernels,
+          CUDA events on the launching stream, L2 flushed between steps;
+  e2e   : the same evaluation through the host-pointer C ABI call (host arrays in, host
+          arrays out, copies inside the timed region);
+  plain : the plain-FP32 drop-in kernel measured the same way;
+  precision : max / RMS relative error of both modes against the FP64 oracle on a seeded
+          1024-target subset (measured outside the timed region).
+
+``--impl reference`` times the reference's CPU implementation of the same call (its own
+compiled code where available, else the C restatement with the same arithmetic: float pairs,
+double accumulators, OpenMP over targets) on all host cores, on a bounded target subset.
+Under torchrun each rank evaluates its own copy of the workload (targets shard naturally;
+no collective on the data path) and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 1_000_000
+SIGMA = 0.005
+SEED = 2
+METRIC = "Ginteractions/s @N=1M, Gaussian core, compensated FP32 (err<=1e-6 vs FP64)"
+UNIT = "Ginteractions/s"
+FLOPS_PER_PAIR = 19        # flopsu_0v_0b for the exponential core (src/Kernels.h:79 + src/CoreFunc.h:145)
+FMA_PER_CLK_PER_SM = 128   # FP32 lanes per SM per clock
+
+
+def make_workload(seed=SEED, n=N):
+    rng = np.random.default_rng(seed)
+    x, y = rng.normal(0.0, 0.25, (2, n)).astype(np.float32)
+    g = np.exp(-(x.astype(np.float64) ** 2 + y.astype(np.float64) ** 2) / 0.125)
+    s = (g / g.sum()).astype(np.float32)
+    r = np.full(n, SIGMA, np.float32)
+    return x, y, r, s
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [q.strip() for q in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def profiled_traffic():
+    """Per-launch DRAM traffic of the main kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("p2p_gauss_comp_1M_bytes_per_launch"):
+            return float(line.split("=")[1])
+    return None
+
+
+def rel_errs(ref64, got):
+    e = np.abs(np.asarray(got, np.float64) - ref64)
+    return float(e.max() / np.abs(ref64).max()), float(np.sqrt((e ** 2).sum() / (ref64 ** 2).sum()))
+
+
+def cpu_sample(kind_pref, x, y, r, s, sample, threads):
+    """Time the reference CPU path on `sample` targets against all sources; returns (sec, kind)."""
+    from oracle import pyoracle as po
+    idx = np.random.default_rng(99).choice(x.size, sample, replace=False)
+    tx, ty, tr = x[idx], y[idx], r[idx]
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    if kind_pref == "reference" and po.Reference.available(po.GAUSS):
+        ref = po.Reference(po.GAUSS)
+        t0 = time.perf_counter()
+        ref.points_affect_points(po.VELONLY, x, y, r, s, tx, ty, tr)
+        return time.perf_counter() - t0, "reference"
+    orc = po.Restatement()
+    t0 = time.perf_counter()
+    orc.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, tx, ty, tr)
+    return time.perf_counter() - t0, "port"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    x, y, r, s = make_workload()
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_sample("reference", x, y, r, s, 256, threads)
+    tot, kind = 0.0, "port"
+    for _ in range(args.steps):
+        dt, kind = cpu_sample("reference", x, y, r, s, sample, threads)
+        tot += dt
+    v = args.steps * sample * x.size / tot / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs, f64 accum",
+            "data": "synthetic", "config": {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian",
+                                            "sigma": SIGMA, "targets_per_step": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{sample} seeded targets x {N} sources per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import torch
+    import omega2d_gb300 as og
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    x, y, r, s = make_workload(SEED + rank)      # each rank: its own 1M-target shard problem
+    ctx = og.Context(local)
+    stream = torch.cuda.Stream(dev)            # kernels and CUDA events share this stream
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    X, Y, R, S = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
+    TU = torch.zeros(N, device=dev)
+    TV = torch.zeros(N, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
+    pairs = float(N) * float(N)
+
+    def step(accum):
+        TU.zero_()
+        TV.zero_()
+        og.points_affect_points_dev(ctx, og.CORE_GAUSSIAN, og.VELONLY, accum, X, Y, R, S, X, Y, R, TU, TV)
+
+    def timed(accum, steps, warmup):
+        ctx.enable_timing(True)
+        for _ in range(warmup):
+            step(accum)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        tot, main = 0.0, 0.0
+        launches0 = ctx.launches
+        for _ in range(steps):
+            flush.fill_(1.0)                     # evict L2 between timed steps
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(accum)
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+            main += ctx.last_timing()[0]
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        launches = ctx.launches - launches0
+        if ws > 1:
+            t = torch.tensor([tot], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.barrier()
+            tot = float(t.item())
+        return tot / steps, main / steps, launches
+
+    with ClockSampler(local) as clk:
+        ms_comp, main_comp, launches = timed(og.COMPENSATED, args.steps, args.warmup)
+        ms_plain, main_plain, _ = timed(og.PLAIN_F32, max(1, args.steps // 2), 1)
+    clocks = clk.summary()
+
+    # end to end through the host-pointer C ABI call (copies in the timed region)
+    e2e_ms = []
+    hp_src = og.Points(x, y, r, s)
+    for k in range(1 + max(1, args.steps // 2)):
+        hp_t = og.Points(x, y, r, None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        og.points_affect_points(hp_src, hp_t, og.VELONLY, og.ExecEnv(og.CORE_GAUSSIAN, og.COMPENSATED, ctx))
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_ms.append(1e3 * (t1 - t0))
+    h2d = 4 * N * 4 + 3 * N * 4 + 2 * N * 4
+    d2h = 2 * N * 4
+
+    value = ws * pairs / (ms_comp * 1e-3) / 1e9
+    plain_value = ws * pairs / (ms_plain * 1e-3) / 1e9
+    e2e_value = ws * pairs / (np.mean(e2e_ms) * 1e-3) / 1e9
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # precision vs the FP64 oracle on a seeded target subset (outside the timed region)
+    from oracle import pyoracle as po
+    orc = po.Restatement()
+    sub = np.random.default_rng(1234).choice(N, 1024, replace=False)
+    u64, v64, _ = orc.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, x[sub], y[sub], r[sub], fp64=True)
+    ref64 = np.concatenate([u64, v64])
+    prec = {"subset_targets": 1024}
+    for name, accum in (("compensated", og.COMPENSATED), ("plain", og.PLAIN_F32)):
+        step(accum)
+        torch.cuda.synchronize()
+        got = np.concatenate([TU.cpu().numpy()[sub], TV.cpu().numpy()[sub]])
+        mx, rms = rel_errs(ref64, got)
+        prec[name] = {"max_rel": mx, "rms_rel": rms}
+
+    # CPU baseline: the reference's CPU path on a bounded sample, all host cores
+    threads = os.cpu_count() or 1
+    cpu_s, kind = cpu_sample("reference", x, y, r, s, args.cpu_sample, threads)
+    cpu_v = args.cpu_sample * N / cpu_s / 1e9
+
+    peaks = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = 2.0 * FMA_PER_CLK_PER_SM * nsm * sm_max * 1e6 / 1e12     # TFLOP/s
+    achieved = pairs * FLOPS_PER_PAIR / (main_comp * 1e-3) / 1e12
+    traffic = profiled_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_comp, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pairs, compensated f32 + f64 reduce", "data": "synthetic",
+        "config": {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian", "sigma": SIGMA,
+                   "targets": "thick (the particles)", "seed": SEED, "l2": "flushed between steps (256 MB write)"},
+        "plain_fp32": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
+                       "compensated_over_plain": value / plain_value},
+        "precision": prec,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": float(np.mean(e2e_ms))},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": traffic,
+                     "kernel": "p2p_kernel<GAUSS,thick,VEL,compensated>",
+                     "flops_per_interaction": FLOPS_PER_PAIR,
+                     "peak_note": f"2 x {FMA_PER_CLK_PER_SM} FP32 lanes x {nsm} SMs x {sm_max:.0f} MHz (max SM clock of measured)",
+                     "frac_at_median_clock": (achieved / (fp32_peak * clocks["sm_mhz"] / sm_max)) if clocks.get("sm_mhz") else None,
+                     "main_kernel_ms": main_comp},
+        "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{args.cpu_sample} seeded targets x {N} sources"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=2048)
+    ap.add_argument("--n", type=int, default=N, help="particles (the headline workload is 1,000,000)")
+    args = ap.parse_args()
+    globals()["N"] = args.n
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

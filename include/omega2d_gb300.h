@@ -60,8 +60,10 @@ typedef struct obs_context obs_context;
 /* Context: CUDA device binding, one stream, device work buffers that grow on demand. */
 int obs_create(obs_context** ctx, int device);
 int obs_destroy(obs_context* ctx);
-/* Use an external cudaStream_t (passed as void*) for _dev calls; NULL restores the own stream. */
+/* Run subsequent work on an external cudaStream_t (passed as void*; NULL is the legacy default
+ * stream).  obs_use_own_stream switches back to the context's own non-blocking stream. */
 int obs_set_stream(obs_context* ctx, void* cuda_stream);
+int obs_use_own_stream(obs_context* ctx);
 int obs_synchronize(obs_context* ctx);
 /* Enable CUDA-event timing of the main kernel of each subsequent call (default off). */
 int obs_enable_timing(obs_context* ctx, int on);

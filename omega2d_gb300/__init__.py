@@ -105,7 +105,11 @@ class Context:
             pass
 
     def set_stream(self, stream_ptr: int | None):
-        _check(lib().obs_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)), "obs_set_stream")
+        """Use the given cudaStream_t handle (0 = legacy default stream); None = own stream."""
+        if stream_ptr is None:
+            _check(lib().obs_use_own_stream(self._h), "obs_use_own_stream")
+        else:
+            _check(lib().obs_set_stream(self._h, ctypes.c_void_p(stream_ptr)), "obs_set_stream")
 
     def synchronize(self):
         _check(lib().obs_synchronize(self._h), "obs_synchronize")

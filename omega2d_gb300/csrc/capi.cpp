@@ -173,7 +173,13 @@ int obs_destroy(obs_context* ctx) {
 
 int obs_set_stream(obs_context* ctx, void* stream) {
   if (!ctx) return OBS_ERR_ARG;
-  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return OBS_OK;
+}
+
+int obs_use_own_stream(obs_context* ctx) {
+  if (!ctx) return OBS_ERR_ARG;
+  ctx->stream = ctx->own_stream;
   return OBS_OK;
 }
 

@@ -44,6 +44,42 @@ __host__ __device__ __forceinline__ float radius_term(int core, float r) {
   return s2;
 }
 
+// ---------------------------------------------------------------- Gaussian-core series
+// g(x) = (1 - e^-x)/x = sum_{n>=0} (-x)^n/(n+1)!  and  g'(x) = sum_{m>=0} (m+1)(-1)^(m+1) x^m/(m+2)!
+// (Taylor series of the exponential).  Truncated after the x^12 term: for 0 <= x < 1 the
+// remainder is below 2e-9 relative, under FP32 rounding.
+__device__ __forceinline__ float gauss_g_series(float x) {
+  float p = 1.0f / 6227020800.0f;
+  p = fmaf(p, x, -1.0f / 479001600.0f);
+  p = fmaf(p, x, 1.0f / 39916800.0f);
+  p = fmaf(p, x, -1.0f / 3628800.0f);
+  p = fmaf(p, x, 1.0f / 362880.0f);
+  p = fmaf(p, x, -1.0f / 40320.0f);
+  p = fmaf(p, x, 1.0f / 5040.0f);
+  p = fmaf(p, x, -1.0f / 720.0f);
+  p = fmaf(p, x, 1.0f / 120.0f);
+  p = fmaf(p, x, -1.0f / 24.0f);
+  p = fmaf(p, x, 1.0f / 6.0f);
+  p = fmaf(p, x, -0.5f);
+  return fmaf(p, x, 1.0f);
+}
+
+__device__ __forceinline__ float gauss_gprime_series(float x) {
+  float p = -1.0f / 6706022400.0f;
+  p = fmaf(p, x, 1.0f / 518918400.0f);
+  p = fmaf(p, x, -1.0f / 43545600.0f);
+  p = fmaf(p, x, 1.0f / 3991680.0f);
+  p = fmaf(p, x, -1.0f / 403200.0f);
+  p = fmaf(p, x, 1.0f / 45360.0f);
+  p = fmaf(p, x, -1.0f / 5760.0f);
+  p = fmaf(p, x, 1.0f / 840.0f);
+  p = fmaf(p, x, -1.0f / 144.0f);
+  p = fmaf(p, x, 1.0f / 30.0f);
+  p = fmaf(p, x, -0.125f);
+  p = fmaf(p, x, 1.0f / 3.0f);
+  return fmaf(p, x, -0.5f);
+}
+
 // ---------------------------------------------------------------- core functions
 // K(d^2) such that one pair contributes strength*K*(-dy, dx), and (GRAD) B = 2 dK/d(d^2) as
 // the reference's "bbb".  zs/zt: radius terms; THICK selects the two-radius form.  UNIF: all
@@ -67,7 +103,20 @@ __device__ __forceinline__ void core_eval(float d2, float zs, float zt, float us
     k = (x > 16.0f) ? ood2 : k;
     k = (x < 0.001f) ? cf : k;
     K = k;
-    if constexpr (GRAD) B = (d2 == 0.0f) ? 0.0f : (2.0f * cf * e - 2.0f * k) * ood2;
+    if constexpr (GRAD) {
+      // bbb = 2 cf^2 g'(x) with g(x) = (1 - e^-x)/x.  The closed form (2 cf e - 2K)/d^2 cancels
+      // for x < 1 (g' -> -1/2 while each term ~ 1/x), so there g and g' come from their Taylor
+      // series; the x < 0.001 branch keeps the reference's cut-off value K = cf with the
+      // reference's bbb there, -2 cf^2 g(x).
+      if (x < 1.0f) {
+        const float g = gauss_g_series(x);
+        const float gp = gauss_gprime_series(x);
+        K = (x < 0.001f) ? cf : cf * g;
+        B = (x < 0.001f) ? -2.0f * cf * cf * g : 2.0f * cf * cf * gp;
+      } else {
+        B = (2.0f * cf * e - 2.0f * k) * ood2;
+      }
+    }
   } else if constexpr (CORE == CORE_V2) {
     // src/CoreFunc.h:238-274: 1/sqrt(d^4 + s^4 (+ t^4)), bbb = -2 K^3 d^2
     const float a = fmaf(d2, d2, THICK ? zs + zt : zs);

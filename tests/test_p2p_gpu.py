@@ -84,7 +84,14 @@ def test_p2p_builder_cores_match_fp64_restatement(ctx, restatement, core, restyp
         for k in range(4):
             assert rel_err(ex[k], targ.grad[k]) < 5e-5
     if restype == og.VELANDVORT:
-        assert rel_err(ex[0], targ.vort) < 5e-5
+        if core == og.CORE_SINGULAR:
+            # point vortices are irrotational away from the centres: the exact value is 0 and
+            # the engine's value is rounding noise of b d^2 + 2K; bound it by the gradient scale
+            _, _, gx = restatement.points_affect_points(core, og.VELANDGRAD, sx, sy, sr, ss, tx, ty,
+                                                        tr if thick else None, fp64=True)
+            assert np.max(np.abs(targ.vort - ex[0])) < 1e-5 * np.max(np.abs(gx[2]))
+        else:
+            assert rel_err(ex[0], targ.vort) < 5e-5
 
 
 @pytest.mark.parametrize("thick", [True, False])
@@ -205,10 +212,12 @@ def test_device_entry_point_with_torch_tensors(ctx, restatement):
     T = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
     tu = torch.zeros(n, device=dev)
     tv = torch.zeros(n, device=dev)
-    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.Stream(dev)
+    ctx.set_stream(stream.cuda_stream)
     try:
+        stream.wait_stream(torch.cuda.current_stream())
         og.points_affect_points_dev(ctx, og.CORE_RM, og.VELONLY, og.COMPENSATED, *T, T[0], T[1], T[2], tu, tv)
-        torch.cuda.synchronize()
+        stream.synchronize()
         ctx.synchronize()
     finally:
         ctx.set_stream(None)
