@@ -69,6 +69,9 @@ int obs_synchronize(obs_context* ctx);
 int obs_enable_timing(obs_context* ctx, int on);
 /* Main-kernel and whole-call device time of the most recent timed call, in milliseconds. */
 int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
+/* Device-side failure record seen by the last synchronizing call that reported one: DEV_ERR
+ * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
+int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 /* Number of engine kernel launches issued by this context since creation. */
 long long obs_launch_count(obs_context* ctx);
 const char* obs_status_string(int status);

@@ -21,6 +21,11 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
                      "-I", INCLUDE, "--expt-relaxed-constexpr"]
+# Extra flags, e.g. OBS_NVCC_EXTRA=-DOBS_DEVICE_CHECKS for a bounds-checked debug build
+# (build into a separate tree with OBS_BUILD_DIR / OBS_LIB to keep the release library).
+NVCC_FLAGS += os.environ.get("OBS_NVCC_EXTRA", "").split()
+BUILD = os.environ.get("OBS_BUILD_DIR", BUILD)
+LIB = os.environ.get("OBS_LIB", LIB)
 
 
 def nvcc() -> str:

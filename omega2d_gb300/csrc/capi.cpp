@@ -55,14 +55,15 @@ int bind(obs_context* ctx) {
 }
 
 int take_device_status(obs_context* ctx) {
-  int bits = 0;
-  cudaError_t e = cudaMemcpyAsync(&bits, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  int w[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(w, ctx->d_status, sizeof(w), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(e);
-  if (bits) {
-    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream);
+  if (w[0]) {
+    for (int k = 0; k < 4; ++k) ctx->last_failure[k] = w[k];
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(w), ctx->stream);
     cudaStreamSynchronize(ctx->stream);
-    if (bits & 1) return OBS_ERR_TIMEOUT;
+    if (w[0] & 1) return OBS_ERR_TIMEOUT;
     return OBS_ERR_CUDA;
   }
   return OBS_OK;
@@ -144,8 +145,8 @@ int obs_create(obs_context** out, int device) {
   int s = bind(ctx);
   if (!s) s = cuda_status(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
   if (!s) s = cuda_status(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
-  if (!s) s = cuda_status(cudaMalloc(&ctx->d_status, sizeof(int)));
-  if (!s) s = cuda_status(cudaMemset(ctx->d_status, 0, sizeof(int)));
+  if (!s) s = cuda_status(cudaMalloc(&ctx->d_status, 4 * sizeof(int)));
+  if (!s) s = cuda_status(cudaMemset(ctx->d_status, 0, 4 * sizeof(int)));
   for (int k = 0; k < 4 && !s; ++k) s = cuda_status(cudaEventCreate(&ctx->timing.ev[k]));
   if (s) {
     obs_destroy(ctx);
@@ -210,6 +211,15 @@ int obs_last_timing(obs_context* ctx, float* main_ms, float* call_ms) {
   if (s) return s;
   if (main_ms) *main_ms = m;
   if (call_ms) *call_ms = c;
+  return OBS_OK;
+}
+
+int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (bits) *bits = ctx->last_failure[0];
+  if (code) *code = ctx->last_failure[1];
+  if (v1) *v1 = ctx->last_failure[2];
+  if (v2) *v2 = ctx->last_failure[3];
   return OBS_OK;
 }
 

@@ -46,7 +46,8 @@ struct obs_context {
   cudaStream_t stream = nullptr;
   obs::DevBuf work;      // header | packed sources | split partials | other scratch
   obs::DevBuf io;        // staging for host-pointer calls
-  int* d_status = nullptr;   // device-side error bits (DEV_ERR_*), sticky until read
+  int* d_status = nullptr;   // device status block: DEV_ERR_* bits + first failure record
+  int last_failure[4] = {0, 0, 0, 0};   // copy of the block at the last synchronize that saw one
   obs::Timing timing;
   long long launches = 0;
 };

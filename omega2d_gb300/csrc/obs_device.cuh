@@ -15,7 +15,28 @@ enum : int { CORE_RM = 1, CORE_GAUSS = 2, CORE_V2 = 3, CORE_WL = 4, CORE_V3 = 5,
 enum : int { RES_VEL = 1, RES_GRAD = 2, RES_PSI = 3, RES_VORT = 4, RES_SHEAR = 5 };
 
 // status bits written by kernels (read back by the host)
-enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2 };
+enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2, DEV_ERR_BOUNDS = 4 };
+
+// Device status block: [0] DEV_ERR_* bits, [1] first check code, [2..3] its two values.
+constexpr int kStatusWords = 4;
+
+// First-failure record (kept even in normal builds for the bounded-wait timeout path).
+__device__ __forceinline__ void record_failure(int* status, int bit, int code, int v1, int v2) {
+  atomicOr(&status[0], bit);
+  if (atomicCAS(&status[1], 0, code) == 0) {
+    status[2] = v1;
+    status[3] = v2;
+  }
+}
+
+#ifdef OBS_DEVICE_CHECKS
+// Bounds check that records the first violation and reports false so the caller skips or
+// clamps the access (debug builds only).
+#define OBS_CHECK(status, cond, code, v1, v2) \
+  ((cond) ? true : (::obs::record_failure((status), ::obs::DEV_ERR_BOUNDS, (code), (int)(v1), (int)(v2)), false))
+#else
+#define OBS_CHECK(status, cond, code, v1, v2) true
+#endif
 
 constexpr float kLog2e = 1.4426950408889634f;
 constexpr float kLn2 = 0.6931471805599453f;

@@ -181,12 +181,15 @@ p2p_kernel(const P2PArgs a) {
     const int sp = item / a.ntb;
     const int tile0 = sp * a.tiles_per_split;
     const int ntile = min(a.tiles_per_split, a.nst - tile0);
+    (void)OBS_CHECK(a.status, sp < a.nsplit && ntile >= 1, 104, item, ntile);
 
     if (tid == 0) {
       for (int s = 0; s < NSTAGE && s < ntile; ++s) {
         const int st = (kt + s) % NSTAGE;
+        int tix = tile0 + s;
+        if (!OBS_CHECK(a.status, tix >= 0 && tix < a.nst, 101, tix, item)) tix = 0;
         mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
-        bulk_g2s(&tile[st][0], a.src + (size_t)(tile0 + s) * SRC_TILE, TILE_BYTES, &bar[st]);
+        bulk_g2s(&tile[st][0], a.src + (size_t)tix * SRC_TILE, TILE_BYTES, &bar[st]);
       }
     }
 
@@ -195,7 +198,8 @@ p2p_kernel(const P2PArgs a) {
 #pragma unroll
     for (int k = 0; k < TPT; ++k) {
       const int i = tb * TB + k * P2P_THREADS + tid;
-      const int ic = (i < a.nt) ? i : (a.nt - 1);
+      int ic = (i < a.nt) ? i : (a.nt - 1);
+      if (!OBS_CHECK(a.status, ic >= 0 && ic < a.nt, 102, ic, item)) ic = 0;
       tx[k] = a.tx[ic];
       ty[k] = a.ty[ic];
       tz[k] = THICK ? radius_term(RES == RES_PSI ? CORE_RM : CORE, a.tr[ic]) : 0.0f;
@@ -207,9 +211,9 @@ p2p_kernel(const P2PArgs a) {
       const int st = kt % NSTAGE;
       const bool ok = mbar_wait_bounded(&bar[st], (kt / NSTAGE) & 1u, WAIT_TRIES);
       if (__syncthreads_or(!ok)) {
-        // a tile never arrived: flag it, let any copy still in flight land, and stop
+        // a tile never arrived: record where, let any copy still in flight land, and stop
         if (tid == 0) {
-          atomicOr(a.status, DEV_ERR_TIMEOUT);
+          record_failure(a.status, DEV_ERR_TIMEOUT, 200 + st, (int)kt, item);
           for (int s = 0; s < NSTAGE; ++s) (void)mbar_wait_bounded(&bar[(kt + s) % NSTAGE], ((kt + s) / NSTAGE) & 1u, WAIT_TRIES);
         }
         return;
@@ -220,8 +224,10 @@ p2p_kernel(const P2PArgs a) {
         p2p_tile<CORE, THICK, RES, COMP, TPT, false>(&tile[st][0], tx, ty, tz, us2, ucf, acc, hi, lo);
       __syncthreads();   // every thread is done with this stage
       if (tid == 0 && t + NSTAGE < ntile) {
+        int tix = tile0 + t + NSTAGE;
+        if (!OBS_CHECK(a.status, tix >= 0 && tix < a.nst, 101, tix, item)) tix = 0;
         mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
-        bulk_g2s(&tile[st][0], a.src + (size_t)(tile0 + t + NSTAGE) * SRC_TILE, TILE_BYTES, &bar[st]);
+        bulk_g2s(&tile[st][0], a.src + (size_t)tix * SRC_TILE, TILE_BYTES, &bar[st]);
       }
     }
 
@@ -233,6 +239,7 @@ p2p_kernel(const P2PArgs a) {
 #pragma unroll
       for (int q = 0; q < NC; ++q)
         c[q] = COMP ? ((double)hi[k][q] + (double)lo[k][q]) : (double)acc[k][q];
+      if (!OBS_CHECK(a.status, sp < a.nsplit && i < a.nt, 103, i, sp)) continue;
       if (a.direct) {
         store_target<RES>(a, i, c);
       } else if (COMP) {
