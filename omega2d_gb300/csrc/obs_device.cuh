@@ -209,6 +209,12 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                :: "r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
 
+// Order this thread's earlier generic-proxy shared-memory accesses (made visible to it by a
+// CTA barrier) before subsequent async-proxy (TMA) writes to the same buffer.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // one-dimensional bulk copy global -> shared (TMA engine); 16-byte aligned, size % 16 == 0
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"

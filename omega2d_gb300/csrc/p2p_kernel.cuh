@@ -175,7 +175,7 @@ p2p_kernel(const P2PArgs a) {
   for (;;) {
     if (tid == 0) s_item = atomicAdd(a.counter, 1);
     __syncthreads();
-    const int item = s_item;
+    const int item = *static_cast<volatile int*>(&s_item);
     if (item >= a.nitems) break;
     const int tb = item % a.ntb;
     const int sp = item / a.ntb;
@@ -184,6 +184,7 @@ p2p_kernel(const P2PArgs a) {
     (void)OBS_CHECK(a.status, sp < a.nsplit && ntile >= 1, 104, item, ntile);
 
     if (tid == 0) {
+      fence_proxy_async_smem();   // previous item's reads of these stages precede the new copies
       for (int s = 0; s < NSTAGE && s < ntile; ++s) {
         const int st = (kt + s) % NSTAGE;
         int tix = tile0 + s;
@@ -226,6 +227,7 @@ p2p_kernel(const P2PArgs a) {
       if (tid == 0 && t + NSTAGE < ntile) {
         int tix = tile0 + t + NSTAGE;
         if (!OBS_CHECK(a.status, tix >= 0 && tix < a.nst, 101, tix, item)) tix = 0;
+        fence_proxy_async_smem();
         mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
         bulk_g2s(&tile[st][0], a.src + (size_t)tix * SRC_TILE, TILE_BYTES, &bar[st]);
       }
@@ -252,6 +254,7 @@ p2p_kernel(const P2PArgs a) {
         for (int q = 0; q < NC; ++q) p[((size_t)q * a.nsplit + sp) * a.nt + i] = acc[k][q];
       }
     }
+    __syncthreads();   // the whole CTA leaves this item before thread 0 fetches the next one
   }
 }
 
