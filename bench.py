@@ -42,7 +42,8 @@ FLOPS_PER_PAIR = 19        # flopsu_0v_0b for the exponential core (src/Kernels.
 FMA_PER_CLK_PER_SM = 128   # FP32 lanes per SM per clock
 
 
-def make_workload(seed=SEED, n=N):
+def make_workload(seed=SEED, n=None):
+    n = N if n is None else n          # N is set from --n at run time
     rng = np.random.default_rng(seed)
     x, y = rng.normal(0.0, 0.25, (2, n)).astype(np.float32)
     g = np.exp(-(x.astype(np.float64) ** 2 + y.astype(np.float64) ** 2) / 0.125)

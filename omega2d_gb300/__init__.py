@@ -267,6 +267,11 @@ def points_affect_points_dev(ctx: Context, core: int, result: int, accum: int, s
     asynchronous on the context's stream."""
     flops = ctypes.c_double()
     extra = list(extra) + [None] * (4 - len(extra))
+    ns, nt = sx.numel(), tx.numel()
+    for name, t, need in (("sy", sy, ns), ("sr", sr, ns), ("ss", ss, ns), ("ty", ty, nt), ("tr", tr, nt),
+                          ("tu", tu, nt), ("tv", tv, nt), *[(f"extra{k}", e, nt) for k, e in enumerate(extra)]):
+        if t is not None and t.numel() < need:
+            raise ValueError(f"{name} has {t.numel()} elements, the call needs {need}")
     st = lib().obs_points_affect_points_dev(
         ctx.handle, ctypes.c_int(core), ctypes.c_int(result), ctypes.c_int(accum),
         ctypes.c_int(FLAG_FINALIZE if finalize else 0), ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),

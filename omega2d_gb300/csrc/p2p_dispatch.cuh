@@ -39,6 +39,15 @@ cudaError_t p2p_dispatch(bool thick, int res, bool comp, const P2PArgs* a, int g
   return cudaErrorInvalidValue;
 }
 
+// Instances live in p2p_core_<name>.cu; other translation units only declare them.
+extern template cudaError_t p2p_dispatch<CORE_RM>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_GAUSS>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_V2>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_WL>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_V3>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_SING>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+extern template cudaError_t p2p_dispatch<CORE_CEXP>(bool, int, bool, const P2PArgs*, int, cudaStream_t, int*);
+
 // streamfunction: core-independent (kernelp), instantiated once
 cudaError_t p2p_dispatch_psi(bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st, int* occ);
 cudaError_t p2p_reduce(int res, bool comp, const P2PArgs& a, cudaStream_t st);
