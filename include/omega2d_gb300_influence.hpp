@@ -1,0 +1,66 @@
+// omega2d_gb300_influence.hpp -- header-only C++ adapters with the reference's driver shapes.
+//
+// Drop these calls into the reference's drivers (src/Influence.h) behind
+// `env.get_instrs() == gpu_cuda` (the unused enum value at src/ExecEnv.h:38).  They take any
+// element container with the reference's accessors -- get_n(), is_inert(), get_pos(),
+// get_rad(), get_str(), get_vel(), get_vort(), get_shear() (src/ElementBase.h:50-115,
+// src/Points.h:116-117) -- so the reference's Points<float> work unchanged.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+
+#include "omega2d_gb300.h"
+
+namespace omega2d_gb300 {
+
+// The core the reference was compiled with (src/CoreFunc.h:35-39), as an engine enum.
+inline int compiled_core() {
+#if defined(USE_RM_KERNEL)
+  return OBS_CORE_RM;
+#elif defined(USE_EXPONENTIAL_KERNEL)
+  return OBS_CORE_GAUSSIAN;
+#elif defined(USE_WL_KERNEL)
+  return OBS_CORE_WL;
+#elif defined(USE_V3_KERNEL)
+  return OBS_CORE_V3;
+#else
+  return OBS_CORE_V2;
+#endif
+}
+
+// One context per process and device, created on first use.
+inline obs_context* context(int device = 0) {
+  static obs_context* ctx = nullptr;
+  if (!ctx) {
+    const int s = obs_create(&ctx, device);
+    if (s != OBS_OK) throw std::runtime_error(std::string("obs_create: ") + obs_status_string(s));
+  }
+  return ctx;
+}
+
+// Mirror of points_affect_points<float,A>(src, targ, restype, env) (src/Influence.h:56-416):
+// accumulates the unscaled influence of src on targ.  result is a results_t value.
+// Returns the reference's flop count for the call.
+template <class SrcPoints, class TargPoints>
+float points_affect_points(const SrcPoints& src, TargPoints& targ, int result,
+                           int core = compiled_core(), int accum = OBS_COMPENSATED) {
+  const auto& sx = src.get_pos();
+  const auto& sr = src.get_rad();
+  const auto& ss = src.get_str();
+  const auto& tx = targ.get_pos();
+  auto& tu = targ.get_vel();
+  const float* tr = targ.is_inert() ? nullptr : targ.get_rad().data();
+  float* e0 = nullptr;
+  if (result == OBS_VELANDVORT) e0 = targ.get_vort().data();
+  if (result == OBS_VELANDSHEAR) e0 = targ.get_shear().data();
+  double flops = 0.0;
+  const int s = obs_points_affect_points(context(), core, result, accum, 0, 0.0, 0.0,
+                                         (int)src.get_n(), sx[0].data(), sx[1].data(), sr.data(), ss.data(),
+                                         (int)targ.get_n(), tx[0].data(), tx[1].data(), tr,
+                                         tu[0].data(), tu[1].data(), e0, nullptr, nullptr, nullptr, &flops);
+  if (s != OBS_OK) throw std::runtime_error(std::string("obs_points_affect_points: ") + obs_status_string(s));
+  return (float)flops;
+}
+
+}  // namespace omega2d_gb300
