@@ -31,6 +31,7 @@ extern "C" {
 #define OBS_ERR_NO_DEVICE (-5)  /* no usable CUDA device                                     */
 #define OBS_ERR_SINGULAR (-6)   /* dense solve met a zero pivot                              */
 #define OBS_ERR_UNSUPPORTED (-7)
+#define OBS_ERR_SCRATCH_LIMIT (-8)  /* size exceeds obs_points_affect_points_noalloc's scratch */
 
 /* ---- core functions (src/CoreFunc.h:35-322 selects one at compile time; here at run time) */
 #define OBS_CORE_RM 1           /* Rosenhead-Moore, src/CoreFunc.h:42-82                     */
@@ -101,6 +102,32 @@ int obs_points_affect_points_dev(obs_context* ctx, int core, int result, int acc
                                  float* tu, float* tv,
                                  float* extra0, float* extra1, float* extra2, float* extra3,
                                  double* flops);
+
+/*
+ * points_affect_points for callers that cannot allocate device memory.  No counterpart in the
+ * reference.  It is meant for code whose host framework owns every device allocation (pool
+ * allocators, memory budgets), for FFI callers that only hand over finished device buffers,
+ * and for callers that must avoid the implicit synchronization an allocation can cause.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine: its scratch is one fixed
+ * device array of 16 MiB + 256 B in the library, reserved on every GPU that loads the
+ * library until the process exits.
+ *   - Arguments and results as obs_points_affect_points_dev (device pointers, accumulate),
+ *     on the given cudaStream_t (NULL = legacy default stream); returns after that stream has
+ *     finished the call, so device-side failures are reported by this call's status.
+ *   - At most OBS_NOALLOC_MAX_SOURCES sources; more returns OBS_ERR_SCRATCH_LIMIT.  Targets are
+ *     unlimited (fewer source splits are used when the partial sums would not fit).
+ *   - The first call on each device looks up the scratch's device address (once per device,
+ *     with that device current); make that first call before any stream capture.
+ *   - Every call shares the one scratch array: calls that overlap on the GPU (other streams,
+ *     other host threads) race and corrupt each other's results.
+ */
+#define OBS_NOALLOC_MAX_SOURCES 262144
+int obs_points_affect_points_noalloc(void* cuda_stream, int core, int result, int accum, int flags,
+                                     double fsx, double fsy,
+                                     int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                     int nt, const float* tx, const float* ty, const float* tr,
+                                     float* tu, float* tv,
+                                     float* extra0, float* extra1, float* extra2, float* extra3);
 
 /*
  * Source-compatible replacements for the reference's external direct-solver hook

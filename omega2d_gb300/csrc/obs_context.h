@@ -80,4 +80,13 @@ struct P2PRequest {
 int run_p2p(obs_context* ctx, const P2PRequest& rq);
 double p2p_flops(int core, int result, bool thick, long long ns, long long nt);
 
+// Launch helpers over the same kernels for callers that supply their own scratch.
+struct P2PArgs;
+cudaError_t p2p_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss,
+                            int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st);
+cudaError_t p2p_launch_target_meta(const float* tr, int nt, unsigned* meta, cudaStream_t st);
+cudaError_t p2p_dispatch_any(int core, bool thick, int res, bool comp, const P2PArgs* a, int grid,
+                             cudaStream_t st, int* occ);
+int p2p_ncomp(int res);
+
 }  // namespace obs

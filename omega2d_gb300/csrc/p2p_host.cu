@@ -74,6 +74,28 @@ cudaError_t dispatch(int core, bool thick, int res, bool comp, const P2PArgs* a,
 
 }  // namespace
 
+// Launch helpers for callers that manage their own scratch (the no-allocation entry point).
+cudaError_t p2p_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss,
+                            int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st) {
+  const int threads = 256;
+  pack_sources_kernel<<<(ns_pad + threads - 1) / threads, threads, 0, st>>>(sx, sy, sr, ss, ns, ns_pad,
+                                                                            core, out, meta);
+  return cudaGetLastError();
+}
+
+cudaError_t p2p_launch_target_meta(const float* tr, int nt, unsigned* meta, cudaStream_t st) {
+  const int threads = 256;
+  target_meta_kernel<<<(nt + threads - 1) / threads, threads, 0, st>>>(tr, nt, meta);
+  return cudaGetLastError();
+}
+
+cudaError_t p2p_dispatch_any(int core, bool thick, int res, bool comp, const P2PArgs* a, int grid,
+                             cudaStream_t st, int* occ) {
+  return dispatch(core, thick, res, comp, a, grid, st, occ);
+}
+
+int p2p_ncomp(int res) { return ncomp_of(res); }
+
 // Reference flop counts: flopsu_0v_0b = 10 + flops_tv_nograds, flopsu_0v_0p = 10 +
 // flops_tp_nograds, flopsug_0v_0b = 25 + flops_tv_grads, flopsuw = 19 + .._grads, flopsue = 23
 // + .._grads, flopsp = 10 + .._nograds (src/Kernels.h:50-190; src/CoreFunc.h flops_*).
