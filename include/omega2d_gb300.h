@@ -104,6 +104,77 @@ int obs_points_affect_points_dev(obs_context* ctx, int core, int result, int acc
                                  double* flops);
 
 /*
+ * Panels: straight constant-strength panels given as node coordinates (nx, ny; nnodes) and
+ * node-index pairs (idx[2*k], idx[2*k+1]) for panel k, like Surfaces (src/Surfaces.h:682-724).
+ * The fluid lies to the left walking node0 -> node1.
+ *
+ * panels_affect_points -- replaces src/Influence.h:422-614: velocity at points due to panels
+ * with vortex sheet strength vs and source sheet strength ss (kernelu_1vs_0p,
+ * src/Kernels.h:362-405); ss == NULL gives the vortex-only kernelu_1v_0p (:311-354).
+ * Accumulates (unscaled) into tu, tv.
+ */
+int obs_panels_affect_points(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                             const float* vs, const float* ss,
+                             int nt, const float* tx, const float* ty, float* tu, float* tv);
+int obs_panels_affect_points_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                 const float* vs, const float* ss,
+                                 int nt, const float* tx, const float* ty, float* tu, float* tv);
+
+/* points_affect_panels -- replaces src/Influence.h:633-771: mean velocity over each panel due
+ * to point vortices of strength ss (the particle core is not used, as in the reference),
+ * accumulated into the panel-centre velocities pu, pv. */
+int obs_points_affect_panels(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int ns, const float* sx, const float* sy, const float* ss,
+                             int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                             float* pu, float* pv);
+int obs_points_affect_panels_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int ns, const float* sx, const float* sy, const float* ss,
+                                 int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                 float* pu, float* pv);
+
+/* panels_on_panels_coeff -- replaces src/Coefficients.h:155-427 (the non-augmented part):
+ * column-major (nunk*ntarg) x (nunk*nsrc) block, targets are rows, scaled by 1/(2 pi);
+ * nunk = 2 is the reference's vortex+source system (src/Surfaces.h:69), nunk = 1 vortex only;
+ * self_block != 0 when source and target are the same body (diagonal pi/(2 pi)).
+ * Either output may be NULL (FP32 as in the reference, or FP64 for the dense solve). */
+int obs_panels_on_panels_coeff(obs_context* ctx, int nunk, int self_block,
+                               int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                               int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                               float* A32, double* A64);
+int obs_panels_on_panels_coeff_dev(obs_context* ctx, int nunk, int self_block,
+                                   int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                                   int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                                   float* A32, double* A64);
+
+/* vels_to_rhs_panels -- replaces src/RHS.h:54-115: rhs = -u.t (and -u.n + bcn). */
+int obs_vels_to_rhs_panels(obs_context* ctx, int nunk, int nnodes, const float* nx, const float* ny, int npan,
+                           const unsigned* idx, const float* pu, const float* pv, const float* bcn,
+                           float* rhs32, double* rhs64);
+int obs_vels_to_rhs_panels_dev(obs_context* ctx, int nunk, int nnodes, const float* nx, const float* ny, int npan,
+                               const unsigned* idx, const float* pu, const float* pv, const float* bcn,
+                               float* rhs32, double* rhs64);
+
+/* FP64 dense solve A x = b (A column-major n x n) on the GPU by LU with partial pivoting; the
+ * reference uses Eigen GMRES in FP32 on the host (src/BEM.h:169-234).  rel_residual (optional)
+ * receives ||A x - b|| / ||b|| like the reference's check (src/BEM.h:223-233). */
+int obs_solve_dense_f64(obs_context* ctx, int n, const double* A, const double* b, double* x,
+                        double* rel_residual);
+int obs_solve_dense_f64_dev(obs_context* ctx, int n, const double* A, const double* b, double* x,
+                            double* rel_residual);
+
+/* solve_bem for one fixed reactive body -- replaces src/BEMHelper.h:43-260 without rotation
+ * augmentation: particles -> panel velocities, finalize with fs, RHS, influence matrix, FP64
+ * solve, strengths out (vs_out; ss_out when nunk == 2).  OBS_BEM_REUSE_MATRIX keeps the
+ * previous factorisation of the same order (the reference's is_A_current, src/BEM.h:49-51). */
+#define OBS_BEM_REUSE_MATRIX 2
+int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                  int ns, const float* sx, const float* sy, const float* ss,
+                  int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
+                  float* vs_out, float* ss_out, double* rel_residual);
+
+/*
  * points_affect_points for callers that cannot allocate device memory.  No counterpart in the
  * reference.  It is meant for code whose host framework owns every device allocation (pool
  * allocators, memory budgets), for FFI callers that only hand over finished device buffers,

@@ -36,7 +36,7 @@ FLAG_FINALIZE = 1
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "allocation failed", -3: "CUDA runtime error",
           -4: "device wait timed out", -5: "no usable CUDA device", -6: "singular matrix",
-          -7: "unsupported combination"}
+          -7: "unsupported combination", -8: "size exceeds the no-allocation scratch"}
 
 
 class EngineError(RuntimeError):
@@ -284,3 +284,153 @@ def points_affect_points_dev(ctx: Context, core: int, result: int, accum: int, s
 
 def flops_per_pair(core: int, result: int = VELONLY, thick: bool = True) -> int:
     return int(lib().obs_flops_per_pair(ctypes.c_int(core), ctypes.c_int(result), ctypes.c_int(1 if thick else 0)))
+
+
+# ---------------------------------------------------------------- panels (src/Surfaces.h)
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+@dataclass
+class Surfaces:
+    """1-D elements (src/Surfaces.h): straight panels between nodes (nx, ny) with node-index
+    pairs idx[2k], idx[2k+1]; the fluid is to the left walking node0 -> node1.  vs / ss are the
+    vortex / source sheet strengths, bcn the normal-velocity boundary condition, (pu, pv) the
+    panel-centre velocities."""
+    nx: np.ndarray
+    ny: np.ndarray
+    idx: np.ndarray
+    vs: np.ndarray | None = None
+    ss: np.ndarray | None = None
+    bcn: np.ndarray | None = None
+    pu: np.ndarray = field(default=None)
+    pv: np.ndarray = field(default=None)
+
+    def __post_init__(self):
+        self.nx, self.ny = _f32(self.nx), _f32(self.ny)
+        self.idx = _u32(self.idx)
+        self.vs, self.ss, self.bcn = _f32(self.vs), _f32(self.ss), _f32(self.bcn)
+        if self.pu is None:
+            self.pu = np.zeros(self.npan, np.float32)
+        if self.pv is None:
+            self.pv = np.zeros(self.npan, np.float32)
+
+    @property
+    def npan(self) -> int:
+        return self.idx.size // 2
+
+    @property
+    def nnodes(self) -> int:
+        return self.nx.size
+
+    def zero_vels(self):
+        self.pu[:] = 0
+        self.pv[:] = 0
+
+    def finalize_vels(self, fs=(0.0, 0.0)):
+        """Surfaces::finalize_vels (src/Surfaces.h:764-774) on the panel-centre velocities."""
+        f = 0.5 / np.pi
+        self.pu[:] = (fs[0] + self.pu.astype(np.float64) * f).astype(np.float32)
+        self.pv[:] = (fs[1] + self.pv.astype(np.float64) * f).astype(np.float32)
+
+    def _geo(self):
+        return (ctypes.c_int(self.nnodes), _ptr(self.nx), _ptr(self.ny), ctypes.c_int(self.npan), _ptr(self.idx))
+
+
+def circle_panels(npan: int, diameter: float = 1.0, center=(0.0, 0.0)) -> Surfaces:
+    """Closed circle of npan straight panels, nodes at theta_i = -2 pi i / npan (clockwise, so
+    the fluid is outside), as SolidCircle lays them out (src/BoundaryFeature.cpp:489-531)."""
+    th = -2.0 * np.pi * np.arange(npan) / npan
+    nx = center[0] + 0.5 * diameter * np.cos(th)
+    ny = center[1] + 0.5 * diameter * np.sin(th)
+    idx = np.stack([np.arange(npan), (np.arange(npan) + 1) % npan], 1).ravel()
+    return Surfaces(nx, ny, idx)
+
+
+def panels_affect_points(src: Surfaces, targ: Points, env: ExecEnv | None = None, vortex_only: bool = False,
+                         finalize: bool = False, fs=(0.0, 0.0)):
+    """panels_affect_points (src/Influence.h:422-614): accumulate the panels' influence on the
+    points.  The reference always uses the vortex+source kernel for active panels; vortex_only
+    selects kernelu_1v_0p."""
+    env = env or ExecEnv()
+    ss = None if (vortex_only or src.ss is None) else src.ss
+    vs = src.vs if src.vs is not None else np.zeros(src.npan, np.float32)
+    st = lib().obs_panels_affect_points(env.ctx().handle, ctypes.c_int(env.accum),
+                                        ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                        ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), *src._geo(),
+                                        _ptr(vs), _ptr(ss), ctypes.c_int(targ.n), _ptr(targ.x), _ptr(targ.y),
+                                        _ptr(targ.u), _ptr(targ.v))
+    _check(st, "obs_panels_affect_points")
+
+
+def points_affect_panels(src: Points, targ: Surfaces, env: ExecEnv | None = None,
+                         finalize: bool = False, fs=(0.0, 0.0)):
+    """points_affect_panels (src/Influence.h:633-771): mean velocity over each panel due to the
+    particles (treated as point vortices, as in the reference), accumulated into targ.pu/pv."""
+    env = env or ExecEnv()
+    st = lib().obs_points_affect_panels(env.ctx().handle, ctypes.c_int(env.accum),
+                                        ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                        ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                                        ctypes.c_int(src.n), _ptr(src.x), _ptr(src.y), _ptr(src.s),
+                                        *targ._geo(), _ptr(targ.pu), _ptr(targ.pv))
+    _check(st, "obs_points_affect_panels")
+
+
+def panels_on_panels_coeff(src: Surfaces, targ: Surfaces | None = None, nunk: int = 2, fp64: bool = False,
+                           context: Context | None = None) -> np.ndarray:
+    """panels_on_panels_coeff (src/Coefficients.h:155-427): the (nunk*ntarg, nunk*nsrc)
+    influence block (targets are rows); targ None means the self block of src."""
+    ctx = context or default_context()
+    same = targ is None
+    targ = src if same else targ
+    nel = src.npan * nunk * targ.npan * nunk
+    out = np.zeros(nel, np.float64 if fp64 else np.float32)
+    st = lib().obs_panels_on_panels_coeff(ctx.handle, ctypes.c_int(nunk), ctypes.c_int(1 if same else 0),
+                                          *src._geo(), *targ._geo(),
+                                          None if fp64 else _ptr(out), _ptr(out) if fp64 else None)
+    _check(st, "obs_panels_on_panels_coeff")
+    return out.reshape(src.npan * nunk, targ.npan * nunk).T.copy()   # column-major -> (rows, cols)
+
+
+def vels_to_rhs_panels(targ: Surfaces, nunk: int = 2, fp64: bool = False, context: Context | None = None):
+    """vels_to_rhs_panels (src/RHS.h:54-115) from targ.pu/pv and targ.bcn."""
+    ctx = context or default_context()
+    out = np.zeros(targ.npan * nunk, np.float64 if fp64 else np.float32)
+    st = lib().obs_vels_to_rhs_panels(ctx.handle, ctypes.c_int(nunk), *targ._geo(), _ptr(targ.pu), _ptr(targ.pv),
+                                      _ptr(targ.bcn), None if fp64 else _ptr(out), _ptr(out) if fp64 else None)
+    _check(st, "obs_vels_to_rhs_panels")
+    return out
+
+
+def solve_dense_f64(A: np.ndarray, b: np.ndarray, context: Context | None = None):
+    """FP64 LU solve of A x = b on the GPU; returns (x, ||A x - b|| / ||b||)."""
+    ctx = context or default_context()
+    A = np.asarray(A, np.float64)
+    n = A.shape[0]
+    Ac = np.asfortranarray(A).ravel(order="K") if A.flags.f_contiguous else np.ascontiguousarray(A.T).ravel()
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(n)
+    rel = ctypes.c_double()
+    _check(lib().obs_solve_dense_f64(ctx.handle, ctypes.c_int(n), _ptr(Ac), _ptr(b), _ptr(x), ctypes.byref(rel)),
+           "obs_solve_dense_f64")
+    return x, rel.value
+
+
+def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: ExecEnv | None = None,
+              reuse_matrix: bool = False) -> float:
+    """solve_bem for one fixed body (src/BEMHelper.h:43-260): sets bdry.vs (and bdry.ss for
+    nunk == 2) from the particles' velocity and the freestream; returns the relative residual."""
+    env = env or ExecEnv()
+    vs = np.zeros(bdry.npan, np.float32)
+    ss = np.zeros(bdry.npan, np.float32) if nunk == 2 else None
+    rel = ctypes.c_double()
+    st = lib().obs_solve_bem(env.ctx().handle, ctypes.c_int(nunk), ctypes.c_int(env.accum),
+                             ctypes.c_int(2 if reuse_matrix else 0), ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                             ctypes.c_int(vort.n), _ptr(vort.x), _ptr(vort.y), _ptr(vort.s), *bdry._geo(),
+                             _ptr(bdry.bcn), _ptr(vs), _ptr(ss), ctypes.byref(rel))
+    _check(st, "obs_solve_bem")
+    bdry.vs = vs
+    if ss is not None:
+        bdry.ss = ss
+    return rel.value

@@ -64,6 +64,8 @@ int take_device_status(obs_context* ctx) {
     cudaMemsetAsync(ctx->d_status, 0, sizeof(w), ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     if (w[0] & 1) return OBS_ERR_TIMEOUT;
+    if (w[0] & 8) return OBS_ERR_SINGULAR;
+    if (w[0] & 4) return OBS_ERR_ARG;      // a device-side index check failed (bad node index)
     return OBS_ERR_CUDA;
   }
   return OBS_OK;
@@ -164,6 +166,7 @@ int obs_destroy(obs_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->work.release();
   ctx->io.release();
+  ctx->dense.release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   for (int k = 0; k < 4; ++k)
     if (ctx->timing.ev[k]) cudaEventDestroy(ctx->timing.ev[k]);

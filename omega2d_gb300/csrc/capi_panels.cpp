@@ -1,0 +1,428 @@
+// capi_panels.cpp -- C ABI for the panel path: panels -> points, points -> panels, the
+// panel-on-panel matrix, the BEM right-hand side, the FP64 dense solve and the whole
+// single-body BEM solve (src/BEMHelper.h:43-260).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "obs_context.h"
+#include "panels.h"
+
+using obs::PanelSet;
+
+namespace {
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Host-pointer staging into ctx->io: reserve all regions first, then copy in.
+struct Stage {
+  obs_context* ctx;
+  std::vector<size_t> sizes;
+  char* base = nullptr;
+  size_t off = 0;
+  cudaError_t err = cudaSuccess;
+  explicit Stage(obs_context* c) : ctx(c) {}
+  void reserve(size_t bytes) { sizes.push_back(al(bytes)); }
+  int commit() {
+    size_t tot = 0;
+    for (size_t s : sizes) tot += s;
+    const int s = ctx->io.ensure(tot + 256, ctx->stream);
+    if (s) return s;
+    base = ctx->io.as<char>();
+    return OBS_OK;
+  }
+  template <class T> T* take(const T* host, size_t n) {
+    T* d = reinterpret_cast<T*>(base + off);
+    off += al(n * sizeof(T));
+    if (host && n && err == cudaSuccess)
+      err = cudaMemcpyAsync(d, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+    return d;
+  }
+};
+
+int check_panels(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx) {
+  if (nnodes < 0 || npan < 0) return OBS_ERR_ARG;
+  if (npan > 0 && (!nx || !ny || !idx || nnodes < 2)) return OBS_ERR_ARG;
+  return OBS_OK;
+}
+
+int check_host_idx(int nnodes, int npan, const unsigned* idx) {
+  for (size_t k = 0; k < 2 * (size_t)npan; ++k)
+    if (idx[k] >= (unsigned)nnodes) return OBS_ERR_ARG;
+  return OBS_OK;
+}
+
+int copy_back(obs_context* ctx, std::initializer_list<std::pair<void*, std::pair<const void*, size_t>>> items) {
+  // device -> temporaries -> caller, so a failure leaves the caller's arrays untouched
+  std::vector<std::vector<char>> tmp;
+  cudaError_t e = cudaSuccess;
+  for (auto& it : items) {
+    tmp.emplace_back(it.second.second);
+    if (it.second.second && e == cudaSuccess)
+      e = cudaMemcpyAsync(tmp.back().data(), it.second.first, it.second.second, cudaMemcpyDeviceToHost, ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return obs::cuda_status(e);
+  size_t k = 0;
+  for (auto& it : items) {
+    if (it.second.second) std::memcpy(it.first, tmp[k].data(), it.second.second);
+    ++k;
+  }
+  return OBS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- panels_affect_points (src/Influence.h:422-614)
+int obs_panels_affect_points_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                 const float* vs, const float* ss,
+                                 int nt, const float* tx, const float* ty, float* tu, float* tv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (nt < 0 || (npan > 0 && !vs) || (nt > 0 && (!tx || !ty || !tu || !tv))) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet ps{nnodes, nx, ny, npan, idx};
+  return obs::run_panels_affect_points(ctx, ps, vs, ss, accum, flags, fsx, fsy, nt, tx, ty, tu, tv);
+}
+
+int obs_panels_affect_points(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                             const float* vs, const float* ss,
+                             int nt, const float* tx, const float* ty, float* tu, float* tv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (nt < 0 || (npan > 0 && !vs) || (nt > 0 && (!tx || !ty || !tu || !tv))) return OBS_ERR_ARG;
+  if (npan == 0 || nt == 0) return OBS_OK;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)npan * 4);
+  for (int k = 0; k < 4; ++k) g.reserve((size_t)nt * 4);
+  if ((s = g.commit())) return s;
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  const float* dvs = g.take(vs, npan);
+  const float* dss = ss ? g.take(ss, npan) : nullptr;
+  if (!ss) g.take<float>(nullptr, npan);
+  const float* dtx = g.take(tx, nt);
+  const float* dty = g.take(ty, nt);
+  float* dtu = g.take(tu, nt);
+  float* dtv = g.take(tv, nt);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  s = obs::run_panels_affect_points(ctx, ps, dvs, dss, accum, flags, fsx, fsy, nt, dtx, dty, dtu, dtv);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  return copy_back(ctx, {{tu, {dtu, (size_t)nt * 4}}, {tv, {dtv, (size_t)nt * 4}}});
+}
+
+// ---- points_affect_panels (src/Influence.h:633-771)
+int obs_points_affect_panels_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int ns, const float* sx, const float* sy, const float* ss,
+                                 int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                                 float* pu, float* pv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (ns < 0 || (ns > 0 && (!sx || !sy || !ss)) || (npan > 0 && (!pu || !pv))) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet ps{nnodes, nx, ny, npan, idx};
+  return obs::run_points_affect_panels(ctx, ns, sx, sy, ss, ps, accum, flags, fsx, fsy, pu, pv);
+}
+
+int obs_points_affect_panels(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int ns, const float* sx, const float* sy, const float* ss,
+                             int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                             float* pu, float* pv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (ns < 0 || (ns > 0 && (!sx || !sy || !ss)) || (npan > 0 && (!pu || !pv))) return OBS_ERR_ARG;
+  if (npan == 0) return OBS_OK;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  Stage g(ctx);
+  for (int k = 0; k < 3; ++k) g.reserve((size_t)ns * 4);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)npan * 4);
+  if ((s = g.commit())) return s;
+  const float* dsx = g.take(sx, ns);
+  const float* dsy = g.take(sy, ns);
+  const float* dss = g.take(ss, ns);
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  float* dpu = g.take(pu, npan);
+  float* dpv = g.take(pv, npan);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  s = obs::run_points_affect_panels(ctx, ns, dsx, dsy, dss, ps, accum, flags, fsx, fsy, dpu, dpv);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  return copy_back(ctx, {{pu, {dpu, (size_t)npan * 4}}, {pv, {dpv, (size_t)npan * 4}}});
+}
+
+// ---- panels_on_panels_coeff (src/Coefficients.h:155-427)
+int obs_panels_on_panels_coeff_dev(obs_context* ctx, int nunk, int self_block,
+                                   int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                                   int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                                   float* A32, double* A64) {
+  if (!ctx || (nunk != 1 && nunk != 2) || (!A32 && !A64)) return OBS_ERR_ARG;
+  int s = check_panels(snn, snx, sny, snp, sidx);
+  if (!s) s = check_panels(tnn, tnx, tny, tnp, tidx);
+  if (s) return s;
+  if (self_block && snp != tnp) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet sp{snn, snx, sny, snp, sidx}, tp{tnn, tnx, tny, tnp, tidx};
+  return obs::run_panels_on_panels_coeff(ctx, sp, tp, nunk, self_block, A32, A64);
+}
+
+int obs_panels_on_panels_coeff(obs_context* ctx, int nunk, int self_block,
+                               int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                               int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                               float* A32, double* A64) {
+  if (!ctx || (nunk != 1 && nunk != 2) || (!A32 && !A64)) return OBS_ERR_ARG;
+  int s = check_panels(snn, snx, sny, snp, sidx);
+  if (!s) s = check_panels(tnn, tnx, tny, tnp, tidx);
+  if (s) return s;
+  if (self_block && snp != tnp) return OBS_ERR_ARG;
+  if (snp == 0 || tnp == 0) return OBS_OK;
+  if ((s = check_host_idx(snn, snp, sidx)) || (s = check_host_idx(tnn, tnp, tidx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  const size_t nel = (size_t)snp * nunk * tnp * nunk;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)snn * 4);
+  g.reserve((size_t)snp * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)tnn * 4);
+  g.reserve((size_t)tnp * 8);
+  g.reserve(A32 ? nel * 4 : 0);
+  g.reserve(A64 ? nel * 8 : 0);
+  if ((s = g.commit())) return s;
+  const float* dsx = g.take(snx, snn);
+  const float* dsy = g.take(sny, snn);
+  const unsigned* dsi = g.take(sidx, 2 * (size_t)snp);
+  const float* dtx = g.take(tnx, tnn);
+  const float* dty = g.take(tny, tnn);
+  const unsigned* dti = g.take(tidx, 2 * (size_t)tnp);
+  float* d32 = A32 ? g.take<float>(nullptr, nel) : nullptr;
+  double* d64 = A64 ? g.take<double>(nullptr, nel) : nullptr;
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet sp{snn, dsx, dsy, snp, dsi}, tp{tnn, dtx, dty, tnp, dti};
+  s = obs::run_panels_on_panels_coeff(ctx, sp, tp, nunk, self_block, d32, d64);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  return copy_back(ctx, {{A32, {d32, A32 ? nel * 4 : 0}}, {A64, {d64, A64 ? nel * 8 : 0}}});
+}
+
+// ---- vels_to_rhs_panels (src/RHS.h:54-115)
+int obs_vels_to_rhs_panels_dev(obs_context* ctx, int nunk, int nnodes, const float* nx, const float* ny, int npan,
+                               const unsigned* idx, const float* pu, const float* pv, const float* bcn,
+                               float* rhs32, double* rhs64) {
+  if (!ctx || (nunk != 1 && nunk != 2) || (!rhs32 && !rhs64)) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (npan > 0 && (!pu || !pv)) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet ps{nnodes, nx, ny, npan, idx};
+  return obs::run_vels_to_rhs(ctx, ps, nunk, pu, pv, bcn, rhs32, rhs64);
+}
+
+int obs_vels_to_rhs_panels(obs_context* ctx, int nunk, int nnodes, const float* nx, const float* ny, int npan,
+                           const unsigned* idx, const float* pu, const float* pv, const float* bcn,
+                           float* rhs32, double* rhs64) {
+  if (!ctx || (nunk != 1 && nunk != 2) || (!rhs32 && !rhs64)) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (npan > 0 && (!pu || !pv)) return OBS_ERR_ARG;
+  if (npan == 0) return OBS_OK;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  const size_t n = (size_t)npan * nunk;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  for (int k = 0; k < 3; ++k) g.reserve((size_t)npan * 4);
+  g.reserve(rhs32 ? n * 4 : 0);
+  g.reserve(rhs64 ? n * 8 : 0);
+  if ((s = g.commit())) return s;
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  const float* dpu = g.take(pu, npan);
+  const float* dpv = g.take(pv, npan);
+  const float* dbc = bcn ? g.take(bcn, npan) : nullptr;
+  if (!bcn) g.take<float>(nullptr, npan);
+  float* d32 = rhs32 ? g.take<float>(nullptr, n) : nullptr;
+  double* d64 = rhs64 ? g.take<double>(nullptr, n) : nullptr;
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  s = obs::run_vels_to_rhs(ctx, ps, nunk, dpu, dpv, dbc, d32, d64);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  return copy_back(ctx, {{rhs32, {d32, rhs32 ? n * 4 : 0}}, {rhs64, {d64, rhs64 ? n * 8 : 0}}});
+}
+
+// ---- FP64 dense solve of A x = b (column-major), LU with partial pivoting on the device
+int obs_solve_dense_f64_dev(obs_context* ctx, int n, const double* A, const double* b, double* x,
+                            double* rel_residual) {
+  if (!ctx || n <= 0 || !A || !b || !x) return OBS_ERR_ARG;
+  int s = obs::bind(ctx);
+  if (s) return s;
+  const size_t nn = (size_t)n * n;
+  s = ctx->dense.ensure(nn * sizeof(double) + al((size_t)n * sizeof(int)) + 256, ctx->stream);
+  if (s) return s;
+  double* lu = ctx->dense.as<double>();
+  int* piv = ctx->dense.as<int>(nn * sizeof(double));
+  cudaError_t e = cudaMemcpyAsync(lu, A, nn * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e == cudaSuccess && x != b) e = cudaMemcpyAsync(x, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) return obs::cuda_status(e);
+  ctx->bem_n = 0;
+  obs::timing_begin(ctx);
+  obs::timing_main_begin(ctx);
+  s = obs::lu_factor_f64(ctx, n, lu, piv);
+  obs::timing_main_end(ctx);
+  if (!s) s = obs::lu_solve_f64(ctx, n, lu, piv, x);
+  obs::timing_end(ctx);
+  if (!s) s = obs::take_device_status(ctx);
+  if (!s && rel_residual) s = obs::residual_f64(ctx, n, A, x, b, rel_residual);
+  return s;
+}
+
+int obs_solve_dense_f64(obs_context* ctx, int n, const double* A, const double* b, double* x,
+                        double* rel_residual) {
+  if (!ctx || n <= 0 || !A || !b || !x) return OBS_ERR_ARG;
+  int s = obs::bind(ctx);
+  if (s) return s;
+  Stage g(ctx);
+  g.reserve((size_t)n * n * 8);
+  g.reserve((size_t)n * 8);
+  g.reserve((size_t)n * 8);
+  if ((s = g.commit())) return s;
+  const double* dA = g.take(A, (size_t)n * n);
+  const double* db = g.take(b, n);
+  double* dx = g.take<double>(nullptr, n);
+  if (g.err) return obs::cuda_status(g.err);
+  s = obs_solve_dense_f64_dev(ctx, n, dA, db, dx, rel_residual);
+  if (s) return s;
+  return copy_back(ctx, {{x, {dx, (size_t)n * 8}}});
+}
+
+/*
+ * One reactive body, the whole of solve_bem (src/BEMHelper.h:43-260) for a fixed body:
+ * panel velocities from the particles (points_affect_panels), finalize with the freestream,
+ * right-hand side (vels_to_rhs_panels), the influence matrix (panels_on_panels_coeff, self
+ * block), FP64 LU solve, and the strengths written back (src/Surfaces.h:266-297).
+ * flags & OBS_BEM_REUSE_MATRIX reuses the factorisation from the previous call of the same
+ * order (the reference's is_A_current, src/BEM.h:49-51).  All arrays on the host.
+ */
+int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                  int ns, const float* sx, const float* sy, const float* ss,
+                  int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
+                  float* vs_out, float* ss_out, double* rel_residual) {
+  if (!ctx || (nunk != 1 && nunk != 2) || npan <= 0 || !vs_out || (nunk == 2 && !ss_out)) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (ns < 0 || (ns > 0 && (!sx || !sy || !ss))) return OBS_ERR_ARG;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  const int n = npan * nunk;
+  const size_t nn = (size_t)n * n;
+  const bool reuse = (flags & 2) && ctx->bem_n == n;
+  Stage g(ctx);
+  for (int k = 0; k < 3; ++k) g.reserve((size_t)ns * 4);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  for (int k = 0; k < 3; ++k) g.reserve((size_t)npan * 4);
+  g.reserve((size_t)n * 8);   // rhs
+  g.reserve((size_t)n * 8);   // x
+  g.reserve(reuse ? 0 : nn * 8);   // A (FP64)
+  if ((s = g.commit())) return s;
+  const float* dsx = g.take(sx, ns);
+  const float* dsy = g.take(sy, ns);
+  const float* dss = g.take(ss, ns);
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  float* dpu = g.take<float>(nullptr, npan);
+  float* dpv = g.take<float>(nullptr, npan);
+  const float* dbc = bcn ? g.take(bcn, npan) : nullptr;
+  if (!bcn) g.take<float>(nullptr, npan);
+  double* drhs = g.take<double>(nullptr, n);
+  double* dx = g.take<double>(nullptr, n);
+  double* dA = reuse ? nullptr : g.take<double>(nullptr, nn);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  cudaError_t e = cudaSuccess;
+  if (ns == 0) {
+    // no particles: the panel velocities are the freestream alone
+    std::vector<float> fx((size_t)npan, (float)fsx), fy((size_t)npan, (float)fsy);
+    e = cudaMemcpyAsync(dpu, fx.data(), (size_t)npan * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dpv, fy.data(), (size_t)npan * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return obs::cuda_status(e);
+  } else {
+    e = cudaMemsetAsync(dpu, 0, (size_t)npan * 4, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dpv, 0, (size_t)npan * 4, ctx->stream);
+    if (e != cudaSuccess) return obs::cuda_status(e);
+    s = obs::run_points_affect_panels(ctx, ns, dsx, dsy, dss, ps, accum, OBS_FLAG_FINALIZE, fsx, fsy, dpu, dpv);
+  }
+  if (!s) s = obs::run_vels_to_rhs(ctx, ps, nunk, dpu, dpv, dbc, nullptr, drhs);
+  if (s) return s;
+  double* lu = nullptr;
+  int* piv = nullptr;
+  if (!reuse) {
+    s = obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
+    if (s) return s;
+    s = ctx->dense.ensure(nn * sizeof(double) + al((size_t)n * sizeof(int)) + 256, ctx->stream);
+    if (s) return s;
+    lu = ctx->dense.as<double>();
+    piv = ctx->dense.as<int>(nn * sizeof(double));
+    e = cudaMemcpyAsync(lu, dA, nn * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return obs::cuda_status(e);
+    ctx->bem_n = 0;
+    s = obs::lu_factor_f64(ctx, n, lu, piv);
+    if (s) return s;
+  } else {
+    lu = ctx->dense.as<double>();
+    piv = ctx->dense.as<int>(nn * sizeof(double));
+  }
+  e = cudaMemcpyAsync(dx, drhs, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) return obs::cuda_status(e);
+  s = obs::lu_solve_f64(ctx, n, lu, piv, dx);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  ctx->bem_n = n;
+  if (rel_residual) {
+    if (reuse) *rel_residual = -1.0;   // the unfactored matrix is not kept
+    else if ((s = obs::residual_f64(ctx, n, dA, dx, drhs, rel_residual))) return s;
+  }
+  std::vector<double> hx(n);
+  e = cudaMemcpyAsync(hx.data(), dx, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return obs::cuda_status(e);
+  for (int i = 0; i < npan; ++i) {
+    if (nunk == 2) {
+      vs_out[i] = (float)hx[2 * i];
+      ss_out[i] = (float)hx[2 * i + 1];
+    } else {
+      vs_out[i] = (float)hx[i];
+    }
+  }
+  return OBS_OK;
+}
+
+}  // extern "C"

@@ -15,7 +15,7 @@ enum : int { CORE_RM = 1, CORE_GAUSS = 2, CORE_V2 = 3, CORE_WL = 4, CORE_V3 = 5,
 enum : int { RES_VEL = 1, RES_GRAD = 2, RES_PSI = 3, RES_VORT = 4, RES_SHEAR = 5 };
 
 // status bits written by kernels (read back by the host)
-enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2, DEV_ERR_BOUNDS = 4 };
+enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2, DEV_ERR_BOUNDS = 4, DEV_ERR_SINGULAR = 8 };
 
 // Device status block: [0] DEV_ERR_* bits, [1] first check code, [2..3] its two values.
 constexpr int kStatusWords = 4;

@@ -1,0 +1,486 @@
+// panels.cu -- constant-strength panel influence: panels -> points, points -> panels, the
+// panel-on-panel influence matrix and the BEM right-hand side.
+//
+// Reference: kernelu_1v_0p / kernelu_1vs_0p / kernelu_1vos_0p (src/Kernels.h:311-458),
+// panels_affect_points (src/Influence.h:422-614), points_affect_panels (:633-771),
+// panels_on_panels_coeff (src/Coefficients.h:155-427), vels_to_rhs_panels (src/RHS.h:54-115).
+//
+// Pair arithmetic is FP32 like the reference, with two accuracy changes that leave the
+// mathematics unchanged: the subtended angle is one atan2 of (cross, dot) instead of the
+// difference of two atan2 values, and 0.5*log(r0^2/r1^2) is log1p of an exactly formed
+// (r0^2 - r1^2)/r1^2.  Both remove cancellations the reference suffers at distant targets.
+#include <algorithm>
+#include <cstring>
+
+#include "obs_context.h"
+#include "obs_device.cuh"
+#include "panels.h"
+
+namespace obs {
+
+namespace {
+
+constexpr int PAN_THREADS = 128;
+constexpr int PAN_TILE = 128;           // panels (or particles) per shared-memory tile
+constexpr int PAN_COMP_BLOCK = 32;
+
+// Per panel: P = (x0, y0, x1, y1), Q = (ux, uy, vortex strength, source strength), where
+// (ux, uy) is the unit tangent node0 -> node1 formed as the reference does (px * rsqrt(panl),
+// src/Kernels.h:380-384).  Padded panels are far away with zero strength.
+__global__ void pack_panels_kernel(const float* __restrict__ nx, const float* __restrict__ ny,
+                                   const unsigned* __restrict__ idx, int nnodes,
+                                   const float* __restrict__ vs, const float* __restrict__ ss,
+                                   int np, int np_pad, float4* __restrict__ P, float4* __restrict__ Q,
+                                   float* __restrict__ len, int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np_pad) return;
+  if (i >= np) {
+    P[i] = make_float4(1.0e6f, 1.0e6f, 1.0e6f + 1.0f, 1.0e6f);
+    Q[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    if (len) len[i] = 1.0f;
+    return;
+  }
+  unsigned j0 = idx[2 * i], j1 = idx[2 * i + 1];
+  if (j0 >= (unsigned)nnodes || j1 >= (unsigned)nnodes) {
+    record_failure(status, DEV_ERR_BOUNDS, 301, i, (int)max(j0, j1));
+    P[i] = make_float4(1.0e6f, 1.0e6f, 1.0e6f + 1.0f, 1.0e6f);
+    Q[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    if (len) len[i] = 1.0f;
+    return;
+  }
+  const float x0 = nx[j0], y0 = ny[j0], x1 = nx[j1], y1 = ny[j1];
+  const float px = x1 - x0, py = y1 - y0;
+  const float panl = px * px + py * py;
+  const float m = 1.0f / sqrtf(panl);
+  P[i] = make_float4(x0, y0, x1, y1);
+  Q[i] = make_float4(px * m, py * m, vs ? vs[i] : 0.0f, ss ? ss[i] : 0.0f);
+  if (len) len[i] = sqrtf(panl);
+}
+
+// Subtended angle u* and log ratio v* of one panel seen from (tx, ty)
+// (get_ustar and my_halflog(rij2/rij12) of src/Kernels.h:256-268, 330-338).
+__device__ __forceinline__ void panel_uv_star(float4 P, float tx, float ty, float& us, float& vs) {
+  const float dx0 = tx - P.x, dy0 = ty - P.y;
+  const float dx1 = tx - P.z, dy1 = ty - P.w;
+  const float px = P.z - P.x, py = P.w - P.y;
+  us = atan2f(dy0 * dx1 - dx0 * dy1, dx0 * dx1 + dy0 * dy1);
+  const float r1 = dx1 * dx1 + dy1 * dy1;
+  const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
+  vs = 0.5f * log1pf(diff / r1);
+}
+
+// kernelu_1vs_0p (vortex + source sheet) on one target; ss = 0 gives kernelu_1v_0p.
+__device__ __forceinline__ void panel_vel(float4 P, float4 Q, float tx, float ty, float& u, float& v) {
+  float us, vs;
+  panel_uv_star(P, tx, ty, us, vs);
+  const float a = us * Q.x - vs * Q.y;   // vortex part, x
+  const float b = us * Q.y + vs * Q.x;   // vortex part, y == source part, x
+  const float c = vs * Q.y - us * Q.x;   // source part, y
+  u = Q.z * a + Q.w * b;
+  v = Q.z * b + Q.w * c;
+}
+
+struct PanArgs {
+  const float4* P;      // packed panels
+  const float4* Q;
+  const float* plen;    // panel lengths (points -> panels)
+  const float4* pts;    // packed particles (x, y, z, strength) for points -> panels
+  int nsrc;             // panels (pan->pt) or particles (pt->pan), padded count
+  int ntiles;
+  const float* tx;
+  const float* ty;
+  int nt;               // targets (points or panels)
+  int nsplit;
+  int tiles_per_split;
+  float* out_u;
+  float* out_v;
+  void* part;
+  int finalize;
+  double fsx, fsy;
+  int mode;             // 0: panels -> points, 1: points -> panels
+};
+
+__device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, double sv) {
+  const double f = a.finalize ? 0.15915494309189535 : 1.0;
+  const double fx = a.finalize ? a.fsx : 0.0, fy = a.finalize ? a.fsy : 0.0;
+  a.out_u[i] = (float)(((double)a.out_u[i] + su) * f + fx);
+  a.out_v[i] = (float)(((double)a.out_v[i] + sv) * f + fy);
+}
+
+// One thread per target, sources (panels or particles) staged through shared memory in tiles;
+// grid = (target blocks, source splits).  Compensated: FP32 partials over 32 sources folded
+// into two-sum pairs, FP64 out; plain: FP32 throughout.
+template <bool COMP>
+__global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
+  __shared__ float4 sP[PAN_TILE];
+  __shared__ float4 sQ[PAN_TILE];
+  __shared__ float sL[PAN_TILE];
+  const int i = blockIdx.x * PAN_THREADS + threadIdx.x;
+  const int sp = blockIdx.y;
+  const int ic = i < a.nt ? i : a.nt - 1;
+  // this thread's target: a point, or a panel (its geometry and inverse length)
+  float tx = 0.0f, ty = 0.0f;
+  float4 TP = make_float4(0, 0, 0, 0), TQ = make_float4(0, 0, 0, 0);
+  float tinv = 0.0f;
+  if (a.mode == 0) {
+    tx = a.tx[ic];
+    ty = a.ty[ic];
+  } else {
+    TP = a.P[ic];
+    TQ = a.Q[ic];
+    tinv = 1.0f / a.plen[ic];
+  }
+  float au = 0.0f, av = 0.0f, hu = 0.0f, lu = 0.0f, hv = 0.0f, lv = 0.0f;
+  const int t0 = sp * a.tiles_per_split;
+  const int t1 = min(t0 + a.tiles_per_split, a.ntiles);
+  for (int t = t0; t < t1; ++t) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < PAN_TILE; k += PAN_THREADS) {
+      const int j = t * PAN_TILE + k;
+      if (a.mode == 0) {
+        sP[k] = a.P[j];
+        sQ[k] = a.Q[j];
+      } else {
+        sP[k] = a.pts[j];
+      }
+    }
+    __syncthreads();
+    for (int b = 0; b < PAN_TILE; b += PAN_COMP_BLOCK) {
+#pragma unroll 4
+      for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
+        float u, v;
+        if (a.mode == 0) {
+          panel_vel(sP[b + k], sQ[b + k], tx, ty, u, v);
+        } else {
+          // the panel is the "source" of kernelu_1v_0p with the particle strength, the particle
+          // the "target"; the sum is used with a minus sign (src/Influence.h:737-759)
+          const float4 s = sP[b + k];
+          const float4 q = make_float4(TQ.x, TQ.y, s.w, 0.0f);
+          panel_vel(TP, q, s.x, s.y, u, v);
+        }
+        au += u;
+        av += v;
+      }
+      if (COMP) {
+        two_sum_acc(hu, lu, au);
+        two_sum_acc(hv, lv, av);
+        au = 0.0f;
+        av = 0.0f;
+      }
+    }
+  }
+  (void)sL;
+  if (i >= a.nt) return;
+  double su = COMP ? (double)hu + (double)lu : (double)au;
+  double sv = COMP ? (double)hv + (double)lv : (double)av;
+  if (a.mode == 1) {
+    su *= -(double)tinv;
+    sv *= -(double)tinv;
+  }
+  if (a.nsplit == 1) {
+    pan_store(a, i, su, sv);
+  } else if (COMP) {
+    double* p = static_cast<double*>(a.part);
+    p[(size_t)sp * a.nt + i] = su;
+    p[((size_t)a.nsplit + sp) * a.nt + i] = sv;
+  } else {
+    float* p = static_cast<float*>(a.part);
+    p[(size_t)sp * a.nt + i] = (float)su;
+    p[((size_t)a.nsplit + sp) * a.nt + i] = (float)sv;
+  }
+}
+
+template <bool COMP>
+__global__ void pan_reduce_kernel(const PanArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nt) return;
+  double su = 0.0, sv = 0.0;
+  if (COMP) {
+    const double* p = static_cast<const double*>(a.part);
+    for (int k = 0; k < a.nsplit; ++k) {
+      su += p[(size_t)k * a.nt + i];
+      sv += p[((size_t)a.nsplit + k) * a.nt + i];
+    }
+  } else {
+    const float* p = static_cast<const float*>(a.part);
+    float fu = 0.0f, fv = 0.0f;
+    for (int k = 0; k < a.nsplit; ++k) {
+      fu += p[(size_t)k * a.nt + i];
+      fv += p[((size_t)a.nsplit + k) * a.nt + i];
+    }
+    su = fu;
+    sv = fv;
+  }
+  pan_store(a, i, su, sv);
+}
+
+// Particles -> float4 (x, y, 0, strength), padded with zero-strength particles far away.
+__global__ void pack_points_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                   const float* __restrict__ s, int n, int n_pad, float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  out[i] = i < n ? make_float4(x[i], y[i], 0.0f, s[i]) : make_float4(1.0e6f, 1.0e6f, 0.0f, 0.0f);
+}
+
+// panels_on_panels_coeff: one thread per (target panel i, source panel j); column-major output
+// with targets as rows (src/Coefficients.h:155-427).  Unit-strength influence of source j at
+// the midpoint of target i, dotted with target i's tangent and normal, averaged with the
+// reversed evaluation weighted by len_j/len_i, the self block set to pi, all times 1/(2 pi).
+__global__ void coeff_kernel(const float4* __restrict__ SP, const float4* __restrict__ SQ,
+                             const float* __restrict__ SL, int nsrc,
+                             const float4* __restrict__ TP, const float4* __restrict__ TQ,
+                             const float* __restrict__ TL, int ntarg, int nunk, int self,
+                             float* __restrict__ A32, double* __restrict__ A64) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= ntarg || j >= nsrc) return;
+  const float4 sp = SP[j], sq = SQ[j];
+  const float4 tp = TP[i], tq = TQ[i];
+  const float ttx = tq.x, tty = tq.y;        // target tangent
+  const float tnx = -tq.y, tny = tq.x;       // target normal (left of node0 -> node1)
+  const float xi = 0.5f * (tp.z + tp.x), yi = 0.5f * (tp.w + tp.y);
+  const float xj = 0.5f * (sp.x + sp.z), yj = 0.5f * (sp.y + sp.w);
+  float us, vs;
+  panel_uv_star(sp, xi, yi, us, vs);
+  float vu = us * sq.x - vs * sq.y, vv = us * sq.y + vs * sq.x;
+  float c11 = vu * ttx + vv * tty, c12 = vu * tnx + vv * tny;
+  float c21 = 0.0f, c22 = 0.0f;
+  if (nunk == 2) {
+    const float su = us * sq.y + vs * sq.x, sv = vs * sq.y - us * sq.x;
+    c21 = su * ttx + sv * tty;
+    c22 = su * tnx + sv * tny;
+  }
+  // reversed roles: target panel as source, evaluated at the source midpoint
+  panel_uv_star(tp, xj, yj, us, vs);
+  const float fact = SL[j] / TL[i];
+  vu = us * tq.x - vs * tq.y;
+  vv = us * tq.y + vs * tq.x;
+  c11 = 0.5f * (c11 - fact * (vu * ttx + vv * tty));
+  c12 = 0.5f * (c12 - fact * (vu * tnx + vv * tny));
+  if (nunk == 2) {
+    const float su = us * tq.y + vs * tq.x, sv = vs * tq.y - us * tq.x;
+    c21 = 0.5f * (c21 - fact * (su * ttx + sv * tty));
+    c22 = 0.5f * (c22 - fact * (su * tnx + sv * tny));
+  }
+  if (self && i == j) {
+    c11 = (float)M_PI;
+    c12 = 0.0f;
+    c21 = 0.0f;
+    c22 = (float)M_PI;
+  }
+  const float fac = (float)(1.0 / (2.0 * M_PI));
+  c11 *= fac; c12 *= fac; c21 *= fac; c22 *= fac;
+  const size_t nrows = (size_t)ntarg * nunk;
+  if (nunk == 2) {
+    const size_t c0 = (size_t)(2 * j) * nrows + 2 * i, c1 = (size_t)(2 * j + 1) * nrows + 2 * i;
+    if (A32) { A32[c0] = c11; A32[c0 + 1] = c12; A32[c1] = c21; A32[c1 + 1] = c22; }
+    if (A64) { A64[c0] = c11; A64[c0 + 1] = c12; A64[c1] = c21; A64[c1 + 1] = c22; }
+  } else {
+    const size_t c0 = (size_t)j * nrows + i;
+    if (A32) A32[c0] = c11;
+    if (A64) A64[c0] = c11;
+  }
+}
+
+// vels_to_rhs_panels (src/RHS.h:54-115): rhs = -u.t (and -u.n + bc_n for two unknowns)
+template <class T>
+__global__ void rhs_kernel(const float4* __restrict__ Q, const float* __restrict__ pu,
+                           const float* __restrict__ pv, const float* __restrict__ bcn, int np, int nunk,
+                           T* __restrict__ rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const float4 q = Q[i];
+  const float t = -(pu[i] * q.x + pv[i] * q.y);
+  if (nunk == 1) {
+    rhs[i] = (T)t;
+  } else {
+    const float n = -(pu[i] * (-q.y) + pv[i] * q.x) + (bcn ? bcn[i] : 0.0f);
+    rhs[2 * i] = (T)t;
+    rhs[2 * i + 1] = (T)n;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------- host
+
+int pack_panels(obs_context* ctx, const PanelSet& ps, const float* vs, const float* ss, float4* P, float4* Q,
+                float* len, int np_pad) {
+  const int threads = 256;
+  pack_panels_kernel<<<(np_pad + threads - 1) / threads, threads, 0, ctx->stream>>>(
+      ps.nx, ps.ny, ps.idx, ps.nnodes, vs, ss, ps.npan, np_pad, P, Q, len, ctx->d_status);
+  ctx->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+namespace {
+
+int plan_splits(obs_context* ctx, int ntarg, int ntiles, int nblocks_per_split) {
+  const int want = 8 * 4 * ctx->num_sms;   // ~32 blocks per SM worth of (target, split) blocks
+  int nsplit = std::max(1, (want + nblocks_per_split - 1) / nblocks_per_split);
+  nsplit = std::min(nsplit, std::max(1, ntiles / 2));
+  (void)ntarg;
+  return nsplit;
+}
+
+int run_pan(obs_context* ctx, PanArgs& a, bool comp, size_t scratch_off) {
+  const int tblocks = (a.nt + PAN_THREADS - 1) / PAN_THREADS;
+  int nsplit = plan_splits(ctx, a.nt, a.ntiles, tblocks);
+  const int tps = (a.ntiles + nsplit - 1) / nsplit;
+  nsplit = (a.ntiles + tps - 1) / tps;
+  a.nsplit = nsplit;
+  a.tiles_per_split = tps;
+  if (nsplit > 1) {
+    const size_t bytes = (size_t)2 * nsplit * a.nt * (comp ? sizeof(double) : sizeof(float));
+    int s = ctx->work.ensure(scratch_off + bytes, ctx->stream);
+    if (s) return s;
+    a.part = ctx->work.as<char>(scratch_off);
+  }
+  // the work buffer may have moved: the caller re-derives packed pointers after ensure
+  return OBS_OK;
+}
+
+}  // namespace
+
+int launch_pan(obs_context* ctx, PanArgs& a, bool comp) {
+  const int tblocks = (a.nt + PAN_THREADS - 1) / PAN_THREADS;
+  dim3 grid(tblocks, a.nsplit);
+  timing_main_begin(ctx);
+  if (comp) pan_kernel<true><<<grid, PAN_THREADS, 0, ctx->stream>>>(a);
+  else pan_kernel<false><<<grid, PAN_THREADS, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  timing_main_end(ctx);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && a.nsplit > 1) {
+    if (comp) pan_reduce_kernel<true><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
+    else pan_reduce_kernel<false><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
+  return cuda_status(e);
+}
+
+// panels -> points (panels_affect_points)
+int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* vs, const float* ss,
+                             int accum, int flags, double fsx, double fsy,
+                             int nt, const float* tx, const float* ty, float* tu, float* tv) {
+  if (ps.npan == 0 || nt == 0) return OBS_OK;
+  const bool comp = accum == OBS_COMPENSATED;
+  const int ntiles = (ps.npan + PAN_TILE - 1) / PAN_TILE;
+  const int np_pad = ntiles * PAN_TILE;
+  const size_t hdr = 256, pbytes = (size_t)np_pad * sizeof(float4);
+  const size_t off_part = hdr + 2 * pbytes;
+  PanArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nsrc = np_pad; a.ntiles = ntiles;
+  a.tx = tx; a.ty = ty; a.nt = nt;
+  a.out_u = tu; a.out_v = tv;
+  a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
+  a.fsx = fsx; a.fsy = fsy;
+  a.mode = 0;
+  int s = ctx->work.ensure(off_part, ctx->stream);
+  if (!s) s = run_pan(ctx, a, comp, off_part);
+  if (s) return s;
+  float4* P = ctx->work.as<float4>(hdr);
+  float4* Q = ctx->work.as<float4>(hdr + pbytes);
+  a.P = P; a.Q = Q;
+  if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
+  timing_begin(ctx);
+  s = pack_panels(ctx, ps, vs, ss, P, Q, nullptr, np_pad);
+  if (!s) s = launch_pan(ctx, a, comp);
+  timing_end(ctx);
+  return s;
+}
+
+// points -> panels (points_affect_panels): mean velocity on each panel due to the particles
+int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const float* sy, const float* ss,
+                             const PanelSet& ps, int accum, int flags, double fsx, double fsy,
+                             float* pu, float* pv) {
+  if (ps.npan == 0 || ns == 0) return OBS_OK;
+  const bool comp = accum == OBS_COMPENSATED;
+  const int ntiles = (ns + PAN_TILE - 1) / PAN_TILE;
+  const int ns_pad = ntiles * PAN_TILE;
+  const int np = ps.npan;
+  const size_t hdr = 256;
+  const size_t pbytes = ((size_t)np * sizeof(float4) + 255) & ~(size_t)255;
+  const size_t lbytes = ((size_t)np * sizeof(float) + 255) & ~(size_t)255;
+  const size_t off_pts = hdr + 2 * pbytes + lbytes;
+  const size_t off_part = off_pts + (size_t)ns_pad * sizeof(float4);
+  PanArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nsrc = ns_pad; a.ntiles = ntiles;
+  a.nt = np;
+  a.out_u = pu; a.out_v = pv;
+  a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
+  a.fsx = fsx; a.fsy = fsy;
+  a.mode = 1;
+  int s = ctx->work.ensure(off_part, ctx->stream);
+  if (!s) s = run_pan(ctx, a, comp, off_part);
+  if (s) return s;
+  float4* P = ctx->work.as<float4>(hdr);
+  float4* Q = ctx->work.as<float4>(hdr + pbytes);
+  float* L = ctx->work.as<float>(hdr + 2 * pbytes);
+  float4* pts = ctx->work.as<float4>(off_pts);
+  a.P = P; a.Q = Q; a.plen = L; a.pts = pts;
+  if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
+  timing_begin(ctx);
+  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, L, np);
+  if (!s) {
+    pack_points_kernel<<<(ns_pad + 255) / 256, 256, 0, ctx->stream>>>(sx, sy, ss, ns, ns_pad, pts);
+    ctx->launches++;
+    s = cuda_status(cudaGetLastError());
+  }
+  if (!s) s = launch_pan(ctx, a, comp);
+  timing_end(ctx);
+  return s;
+}
+
+// panels_on_panels_coeff into caller buffers (either may be null)
+int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const PanelSet& targ, int nunk, int self,
+                               float* A32, double* A64) {
+  if (src.npan == 0 || targ.npan == 0) return OBS_OK;
+  if (src.npan > 65535) return OBS_ERR_UNSUPPORTED;   // one grid row per source panel
+  const size_t hdr = 256;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t sp = al((size_t)src.npan * sizeof(float4)), sl = al((size_t)src.npan * sizeof(float));
+  const size_t tp = al((size_t)targ.npan * sizeof(float4)), tl = al((size_t)targ.npan * sizeof(float));
+  int s = ctx->work.ensure(hdr + 2 * sp + sl + 2 * tp + tl, ctx->stream);
+  if (s) return s;
+  size_t off = hdr;
+  float4* SP = ctx->work.as<float4>(off); off += sp;
+  float4* SQ = ctx->work.as<float4>(off); off += sp;
+  float* SL = ctx->work.as<float>(off); off += sl;
+  float4* TP = ctx->work.as<float4>(off); off += tp;
+  float4* TQ = ctx->work.as<float4>(off); off += tp;
+  float* TL = ctx->work.as<float>(off);
+  timing_begin(ctx);
+  s = pack_panels(ctx, src, nullptr, nullptr, SP, SQ, SL, src.npan);
+  if (!s) s = pack_panels(ctx, targ, nullptr, nullptr, TP, TQ, TL, targ.npan);
+  if (s) return s;
+  dim3 grid((targ.npan + 127) / 128, src.npan);
+  timing_main_begin(ctx);
+  coeff_kernel<<<grid, 128, 0, ctx->stream>>>(SP, SQ, SL, src.npan, TP, TQ, TL, targ.npan, nunk, self, A32, A64);
+  ctx->launches++;
+  timing_main_end(ctx);
+  timing_end(ctx);
+  return cuda_status(cudaGetLastError());
+}
+
+int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,
+                    const float* bcn, float* rhs32, double* rhs64) {
+  if (ps.npan == 0) return OBS_OK;
+  const size_t hdr = 256;
+  const size_t pb = ((size_t)ps.npan * sizeof(float4) + 255) & ~(size_t)255;
+  int s = ctx->work.ensure(hdr + 2 * pb, ctx->stream);
+  if (s) return s;
+  float4* P = ctx->work.as<float4>(hdr);
+  float4* Q = ctx->work.as<float4>(hdr + pb);
+  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, nullptr, ps.npan);
+  if (s) return s;
+  const int blocks = (ps.npan + 255) / 256;
+  if (rhs32) { rhs_kernel<float><<<blocks, 256, 0, ctx->stream>>>(Q, pu, pv, bcn, ps.npan, nunk, rhs32); ctx->launches++; }
+  if (rhs64) { rhs_kernel<double><<<blocks, 256, 0, ctx->stream>>>(Q, pu, pv, bcn, ps.npan, nunk, rhs64); ctx->launches++; }
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace obs

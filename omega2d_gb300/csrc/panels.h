@@ -1,0 +1,36 @@
+// panels.h -- host-side declarations for the panel, BEM-matrix and dense-solve launchers.
+#pragma once
+
+#include "obs_context.h"
+
+namespace obs {
+
+// A set of straight panels on device: node coordinates and node-index pairs per panel
+// (src/Surfaces.h:682-724 geometry; Int = uint32_t indices, src/Omega2D.h:26).
+struct PanelSet {
+  int nnodes;
+  const float* nx;
+  const float* ny;
+  int npan;
+  const unsigned* idx;   // 2 * npan
+};
+
+int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* vs, const float* ss,
+                             int accum, int flags, double fsx, double fsy,
+                             int nt, const float* tx, const float* ty, float* tu, float* tv);
+int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const float* sy, const float* ss,
+                             const PanelSet& ps, int accum, int flags, double fsx, double fsy,
+                             float* pu, float* pv);
+int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const PanelSet& targ, int nunk, int self,
+                               float* A32, double* A64);
+int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,
+                    const float* bcn, float* rhs32, double* rhs64);
+
+// FP64 dense solve A x = b (column-major n x n) by LU with partial pivoting on the device.
+// A is factored in place in `lu` (n*n doubles, caller-owned device memory); piv receives n
+// pivot rows.  rel_residual (optional) = ||A x - b|| / ||b|| using the unfactored A.
+int lu_factor_f64(obs_context* ctx, int n, double* lu, int* piv);
+int lu_solve_f64(obs_context* ctx, int n, const double* lu, const int* piv, double* x /* in: b, out: x */);
+int residual_f64(obs_context* ctx, int n, const double* A, const double* x, const double* b, double* rel_residual);
+
+}  // namespace obs
