@@ -57,7 +57,9 @@ def test_points_affect_panels_many_sources_split(ctx, restatement):
     og.points_affect_panels(og.Points(x, y, np.full(n, 0.01, np.float32), s), surf,
                             og.ExecEnv(accum=og.COMPENSATED, context=ctx))
     u64, v64 = restatement.points_affect_panels(x, y, s, surf.nx, surf.ny, surf.idx, fp64=True)
-    assert rel_err(u64, surf.pu) < TOL64 and rel_err(v64, surf.pv) < TOL64
+    # 200k random-sign strengths: the sums cancel to ~1/sqrt(n) of the term scale, so FP32 pair
+    # rounding shows up ~sqrt(n) larger relative to the result than in the coherent cases
+    assert rel_err(u64, surf.pu) < 2e-5 and rel_err(v64, surf.pv) < 2e-5
 
 
 def test_panel_matrix_self_block(ctx, golden, restatement):
