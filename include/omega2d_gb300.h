@@ -175,6 +175,57 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
                   float* vs_out, float* ss_out, double* rel_residual);
 
 /*
+ * Reverse mode (no counterpart in the reference, which has no adjoint).  Cotangents lu, lv are
+ * on the FINALIZED velocities u = fs + (1/2 pi) sum (OBS_FLAG_FINALIZE); gradient outputs are
+ * ACCUMULATED (+=); any output pointer may be NULL.
+ *
+ * obs_points_affect_points_vjp: backward of points_affect_points for a separate target set
+ * (field points when tr == NULL, thick targets otherwise): dL/d(source x, y, strength) by a
+ * source-outer gather over the targets, and dL/d(target x, y) = (1/2 pi) (grad u)^T lam from
+ * the velocity-gradient kernel.
+ */
+int obs_points_affect_points_vjp(obs_context* ctx, int core, int accum,
+                                 int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                 int nt, const float* tx, const float* ty, const float* tr,
+                                 const float* lu, const float* lv,
+                                 float* gsx, float* gsy, float* gss, float* gtx, float* gty);
+int obs_points_affect_points_vjp_dev(obs_context* ctx, int core, int accum,
+                                     int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                     int nt, const float* tx, const float* ty, const float* tr,
+                                     const float* lu, const float* lv,
+                                     float* gsx, float* gsy, float* gss, float* gtx, float* gty);
+
+/* Backward of the self-interaction (targets are the particles, thick cores): one fused gather
+ * per particle gives dL/dx, dL/dy (both source and target roles) and dL/ds. */
+int obs_points_affect_points_vjp_self(obs_context* ctx, int core, int accum, int n, const float* x, const float* y,
+                                      const float* r, const float* s, const float* lu, const float* lv,
+                                      float* gx, float* gy, float* gs);
+int obs_points_affect_points_vjp_self_dev(obs_context* ctx, int core, int accum, int n, const float* x,
+                                          const float* y, const float* r, const float* s, const float* lu,
+                                          const float* lv, float* gx, float* gy, float* gs);
+
+/* Forward op: nsteps of first-order Euler (order 1) or Ralston RK2 (order 2) convection of the
+ * particles by their own velocity plus freestream, in place -- Convection::advect_1st /
+ * advect_2nd_ralston without bodies (src/Convection.h:274-466). */
+int obs_advect(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
+               const float* s, double fsx, double fsy, double dt, int nsteps);
+int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
+                   const float* s, double fsx, double fsy, double dt, int nsteps);
+
+/* Backward op of obs_advect from the initial positions (x0, y0): given dL/d(final x, y) in
+ * (lx, ly), accumulate dL/ds into gs and dL/d(initial x, y) into gx0, gy0.  The trajectory is
+ * recomputed per segment from checkpoints every checkpoint_every steps (0: ceil(sqrt(nsteps))).
+ * peak_bytes (optional) receives the engine's device-memory footprint (all its buffers). */
+int obs_advect_vjp(obs_context* ctx, int core, int accum, int order, int n, const float* x0, const float* y0,
+                   const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
+                   int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
+                   long long* peak_bytes);
+int obs_advect_vjp_dev(obs_context* ctx, int core, int accum, int order, int n, const float* x0, const float* y0,
+                       const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
+                       int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
+                       long long* peak_bytes);
+
+/*
  * points_affect_points for callers that cannot allocate device memory.  No counterpart in the
  * reference.  It is meant for code whose host framework owns every device allocation (pool
  * allocators, memory budgets), for FFI callers that only hand over finished device buffers,

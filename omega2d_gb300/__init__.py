@@ -434,3 +434,91 @@ def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: E
     if ss is not None:
         bdry.ss = ss
     return rel.value
+
+
+# ---------------------------------------------------------------- reverse mode and time stepping
+
+def points_affect_points_vjp(src: Points, targ: Points, lu, lv, env: ExecEnv | None = None,
+                             want_targets: bool = False):
+    """Backward of the finalized velocity at a separate target set: given cotangents (lu, lv) on
+    targ's velocities, return dL/d(src x, y, s) and, if asked, dL/d(targ x, y)."""
+    env = env or ExecEnv()
+    lu, lv = _f32(lu), _f32(lv)
+    gsx, gsy, gss = (np.zeros(src.n, np.float32) for _ in range(3))
+    gtx = np.zeros(targ.n, np.float32) if want_targets else None
+    gty = np.zeros(targ.n, np.float32) if want_targets else None
+    st = lib().obs_points_affect_points_vjp(env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(env.accum),
+                                            ctypes.c_int(src.n), _ptr(src.x), _ptr(src.y), _ptr(src.r), _ptr(src.s),
+                                            ctypes.c_int(targ.n), _ptr(targ.x), _ptr(targ.y), _ptr(targ.r),
+                                            _ptr(lu), _ptr(lv), _ptr(gsx), _ptr(gsy), _ptr(gss), _ptr(gtx), _ptr(gty))
+    _check(st, "obs_points_affect_points_vjp")
+    return (gsx, gsy, gss, gtx, gty) if want_targets else (gsx, gsy, gss)
+
+
+def points_affect_points_vjp_self(p: Points, lu, lv, env: ExecEnv | None = None):
+    """Backward of the particles' own finalized velocity: returns dL/dx, dL/dy, dL/ds."""
+    env = env or ExecEnv()
+    lu, lv = _f32(lu), _f32(lv)
+    gx, gy, gs = (np.zeros(p.n, np.float32) for _ in range(3))
+    st = lib().obs_points_affect_points_vjp_self(env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(env.accum),
+                                                 ctypes.c_int(p.n), _ptr(p.x), _ptr(p.y), _ptr(p.r), _ptr(p.s),
+                                                 _ptr(lu), _ptr(lv), _ptr(gx), _ptr(gy), _ptr(gs))
+    _check(st, "obs_points_affect_points_vjp_self")
+    return gx, gy, gs
+
+
+def advect(p: Points, fs=(0.0, 0.0), dt: float = 0.01, nsteps: int = 1, order: int = 2,
+           env: ExecEnv | None = None):
+    """Convection::advect_1st (order 1) / advect_2nd_ralston (order 2) without bodies
+    (src/Convection.h:274-466): moves p.x, p.y in place by nsteps steps."""
+    env = env or ExecEnv()
+    st = lib().obs_advect(env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(env.accum), ctypes.c_int(order),
+                          ctypes.c_int(p.n), _ptr(p.x), _ptr(p.y), _ptr(p.r), _ptr(p.s),
+                          ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(dt), ctypes.c_int(nsteps))
+    _check(st, "obs_advect")
+
+
+def advect_vjp(p0: Points, lx, ly, fs=(0.0, 0.0), dt: float = 0.01, nsteps: int = 1, order: int = 2,
+               checkpoint_every: int = 0, env: ExecEnv | None = None):
+    """Backward of advect from the initial state p0: given dL/d(final x, y), returns
+    (dL/ds, dL/dx0, dL/dy0, engine device bytes)."""
+    env = env or ExecEnv()
+    lx, ly = _f32(lx), _f32(ly)
+    gs, gx, gy = (np.zeros(p0.n, np.float32) for _ in range(3))
+    peak = ctypes.c_longlong()
+    st = lib().obs_advect_vjp(env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(env.accum), ctypes.c_int(order),
+                              ctypes.c_int(p0.n), _ptr(p0.x), _ptr(p0.y), _ptr(p0.r), _ptr(p0.s),
+                              ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(dt),
+                              ctypes.c_int(nsteps), ctypes.c_int(checkpoint_every), _ptr(lx), _ptr(ly),
+                              _ptr(gs), _ptr(gx), _ptr(gy), ctypes.byref(peak))
+    _check(st, "obs_advect_vjp")
+    return gs, gx, gy, peak.value
+
+
+def points_affect_points_vjp_dev(ctx: Context, core: int, accum: int, sx, sy, sr, ss, tx, ty, tr, lu, lv,
+                                 gsx=None, gsy=None, gss=None, gtx=None, gty=None):
+    """Device-resident backward (CUDA tensors), asynchronous on the context's stream."""
+    st = lib().obs_points_affect_points_vjp_dev(ctx.handle, ctypes.c_int(core), ctypes.c_int(accum),
+                                                ctypes.c_int(sx.numel()), _ptr(sx), _ptr(sy), _ptr(sr), _ptr(ss),
+                                                ctypes.c_int(tx.numel()), _ptr(tx), _ptr(ty), _ptr(tr), _ptr(lu),
+                                                _ptr(lv), _ptr(gsx), _ptr(gsy), _ptr(gss), _ptr(gtx), _ptr(gty))
+    _check(st, "obs_points_affect_points_vjp_dev")
+
+
+def advect_dev(ctx: Context, core: int, accum: int, order: int, x, y, r, s, fs, dt, nsteps):
+    st = lib().obs_advect_dev(ctx.handle, ctypes.c_int(core), ctypes.c_int(accum), ctypes.c_int(order),
+                              ctypes.c_int(x.numel()), _ptr(x), _ptr(y), _ptr(r), _ptr(s), ctypes.c_double(fs[0]),
+                              ctypes.c_double(fs[1]), ctypes.c_double(dt), ctypes.c_int(nsteps))
+    _check(st, "obs_advect_dev")
+
+
+def advect_vjp_dev(ctx: Context, core: int, accum: int, order: int, x0, y0, r, s, fs, dt, nsteps,
+                   checkpoint_every, lx, ly, gs=None, gx0=None, gy0=None) -> int:
+    peak = ctypes.c_longlong()
+    st = lib().obs_advect_vjp_dev(ctx.handle, ctypes.c_int(core), ctypes.c_int(accum), ctypes.c_int(order),
+                                  ctypes.c_int(x0.numel()), _ptr(x0), _ptr(y0), _ptr(r), _ptr(s),
+                                  ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(dt),
+                                  ctypes.c_int(nsteps), ctypes.c_int(checkpoint_every), _ptr(lx), _ptr(ly),
+                                  _ptr(gs), _ptr(gx0), _ptr(gy0), ctypes.byref(peak))
+    _check(st, "obs_advect_vjp_dev")
+    return peak.value

@@ -47,6 +47,7 @@ struct obs_context {
   obs::DevBuf work;      // header | packed sources | split partials | other scratch
   obs::DevBuf io;        // staging for host-pointer calls
   obs::DevBuf dense;     // BEM matrix (FP64) and its LU factors + pivots
+  obs::DevBuf state;     // time stepping: stage velocities, checkpoints, adjoint vectors
   int bem_n = 0;         // order of the factored BEM matrix held in `dense` (0: none)
   int* d_status = nullptr;   // device status block: DEV_ERR_* bits + first failure record
   int last_failure[4] = {0, 0, 0, 0};   // copy of the block at the last synchronize that saw one
