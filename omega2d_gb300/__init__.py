@@ -74,6 +74,14 @@ def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
 
 
+def _own32(a):
+    """A float32 copy owned by the container (the reference's containers copy their inputs,
+    src/Points.h:75-104), so in-place updates never write through to the caller's arrays."""
+    if a is None:
+        return None
+    return np.array(a, dtype=np.float32, copy=True, order="C")
+
+
 def _ptr(a):
     if a is None:
         return None
@@ -188,8 +196,8 @@ class Points:
     grad: list | None = None   # [du/dx, dv/dx, du/dy, dv/dy]
 
     def __post_init__(self):
-        self.x, self.y = _f32(self.x), _f32(self.y)
-        self.r, self.s = _f32(self.r), _f32(self.s)
+        self.x, self.y = _own32(self.x), _own32(self.y)
+        self.r, self.s = _own32(self.r), _own32(self.s)
         n = self.x.size
         if self.u is None:
             self.u = np.zeros(n, np.float32)
@@ -308,9 +316,9 @@ class Surfaces:
     pv: np.ndarray = field(default=None)
 
     def __post_init__(self):
-        self.nx, self.ny = _f32(self.nx), _f32(self.ny)
-        self.idx = _u32(self.idx)
-        self.vs, self.ss, self.bcn = _f32(self.vs), _f32(self.ss), _f32(self.bcn)
+        self.nx, self.ny = _own32(self.nx), _own32(self.ny)
+        self.idx = np.array(self.idx, dtype=np.uint32, copy=True)
+        self.vs, self.ss, self.bcn = _own32(self.vs), _own32(self.ss), _own32(self.bcn)
         if self.pu is None:
             self.pu = np.zeros(self.npan, np.float32)
         if self.pv is None:
