@@ -73,6 +73,15 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
 /* Device-side failure record seen by the last synchronizing call that reported one: DEV_ERR
  * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
+/* Kernel variant for particle-on-particle velocity sums.  AUTO uses the packed-FP32 kernels
+ * (two targets per f32x2 register pair) where they exist (velocity only, Gaussian and RM
+ * cores) and the generic kernels elsewhere; GENERIC forces the generic kernels; PACKED2 /
+ * PACKED4 pick 2 or 4 target pairs per thread for the packed kernels. */
+#define OBS_VARIANT_AUTO 0
+#define OBS_VARIANT_GENERIC 1
+#define OBS_VARIANT_PACKED2 2
+#define OBS_VARIANT_PACKED4 4
+int obs_set_kernel_variant(obs_context* ctx, int variant);
 /* Number of engine kernel launches issued by this context since creation. */
 long long obs_launch_count(obs_context* ctx);
 const char* obs_status_string(int status);

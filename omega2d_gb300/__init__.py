@@ -33,6 +33,7 @@ CORE_RM, CORE_GAUSSIAN, CORE_V2, CORE_WL, CORE_V3, CORE_SINGULAR, CORE_COMPACT_E
 VELONLY, VELANDGRAD, PSIONLY, VELANDVORT, VELANDSHEAR = 1, 2, 3, 4, 5
 PLAIN_F32, COMPENSATED = 0, 1
 FLAG_FINALIZE = 1
+VARIANT_AUTO, VARIANT_GENERIC, VARIANT_PACKED2, VARIANT_PACKED4 = 0, 1, 2, 4
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "allocation failed", -3: "CUDA runtime error",
           -4: "device wait timed out", -5: "no usable CUDA device", -6: "singular matrix",
@@ -129,6 +130,10 @@ class Context:
         m, c = ctypes.c_float(), ctypes.c_float()
         _check(lib().obs_last_timing(self._h, ctypes.byref(m), ctypes.byref(c)), "obs_last_timing")
         return m.value, c.value
+
+    def set_kernel_variant(self, variant: int):
+        """VARIANT_AUTO (packed FP32 kernels where available), VARIANT_GENERIC, PACKED2/PACKED4."""
+        _check(lib().obs_set_kernel_variant(self._h, ctypes.c_int(variant)), "obs_set_kernel_variant")
 
     @property
     def launches(self) -> int:

@@ -53,6 +53,7 @@ struct obs_context {
   int last_failure[4] = {0, 0, 0, 0};   // copy of the block at the last synchronize that saw one
   obs::Timing timing;
   long long launches = 0;
+  int kernel_variant = 0;   // OBS_VARIANT_*
 };
 
 namespace obs {
@@ -91,5 +92,12 @@ cudaError_t p2p_launch_target_meta(const float* tr, int nt, unsigned* meta, cuda
 cudaError_t p2p_dispatch_any(int core, bool thick, int res, bool comp, const P2PArgs* a, int grid,
                              cudaStream_t st, int* occ);
 int p2p_ncomp(int res);
+
+// packed-FP32 velocity kernels (p2p_packed.cu)
+bool packed_supported(int core, int res);
+cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
+                            int* occ);
+cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, int ns, int ns_pad,
+                               int core, float4* out, unsigned* meta, cudaStream_t st);
 
 }  // namespace obs

@@ -4,6 +4,7 @@
 
 #include "obs_context.h"
 #include "p2p_dispatch.cuh"
+#include "p2p_packed.cuh"
 
 namespace obs {
 
@@ -128,13 +129,22 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int kcore = (res == RES_PSI) ? CORE_RM : rq.core;
   cudaStream_t st = ctx->stream;
 
+  // ---- kernel choice: the packed-FP32 kernels serve velocity-only Gaussian / RM sums
+  const int variant = ctx->kernel_variant;
+  const bool packed = variant != OBS_VARIANT_GENERIC && packed_supported(rq.core, res);
+  const int np = (variant == OBS_VARIANT_PACKED4) ? 4 : 2;
+  auto launch = [&](const P2PArgs* args, int g, int* occ_out) -> cudaError_t {
+    return packed ? packed_dispatch(rq.core, np, thick, comp, args, g, st, occ_out)
+                  : dispatch(rq.core, thick, res, comp, args, g, st, occ_out);
+  };
+
   // ---- plan the split
   int occ = 0;
-  cudaError_t e = dispatch(rq.core, thick, res, comp, nullptr, 0, st, &occ);
+  cudaError_t e = launch(nullptr, 0, &occ);
   if (e != cudaSuccess) return cuda_status(e);
   occ = std::max(occ, 1);
   const int slots = occ * ctx->num_sms;
-  const int tb = P2P_THREADS * p2p_tpt(res);
+  const int tb = P2P_THREADS * (packed ? 2 * np : p2p_tpt(res));
   const int ntb = (rq.nt + tb - 1) / tb;
   const int nst = (rq.ns + SRC_TILE - 1) / SRC_TILE;
   const int want_items = 24 * slots;
@@ -148,7 +158,7 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
 
   // ---- work buffer: header | packed sources | partials
   const size_t hdr = 256;
-  const size_t src_bytes = (size_t)nst * SRC_TILE * sizeof(float4);
+  const size_t src_bytes = (size_t)nst * SRC_TILE * sizeof(float4) * (packed ? PK_ELEM : 1);
   const size_t part_bytes = nsplit > 1 ? (size_t)nc * nsplit * rq.nt * (comp ? sizeof(double) : sizeof(float)) : 0;
   int s = ctx->work.ensure(hdr + src_bytes + part_bytes, st);
   if (s) return s;
@@ -162,8 +172,13 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   {
     const int threads = 256;
     const int ns_pad = nst * SRC_TILE;
-    pack_sources_kernel<<<(ns_pad + threads - 1) / threads, threads, 0, st>>>(
-        rq.sx, rq.sy, rq.sr, rq.ss, rq.ns, ns_pad, kcore, src, h->meta);
+    if (packed) {
+      e = packed_launch_pack(rq.sx, rq.sy, rq.sr, rq.ss, rq.ns, ns_pad, kcore, src, h->meta, st);
+      if (e != cudaSuccess) return cuda_status(e);
+    } else {
+      pack_sources_kernel<<<(ns_pad + threads - 1) / threads, threads, 0, st>>>(
+          rq.sx, rq.sy, rq.sr, rq.ss, rq.ns, ns_pad, kcore, src, h->meta);
+    }
     ctx->launches++;
     if (thick) {
       target_meta_kernel<<<(rq.nt + threads - 1) / threads, threads, 0, st>>>(rq.tr, rq.nt, h->meta);
@@ -191,7 +206,7 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   a.fsx = rq.fsx; a.fsy = rq.fsy;
 
   timing_main_begin(ctx);
-  e = dispatch(rq.core, thick, res, comp, &a, grid, st, nullptr);
+  e = launch(&a, grid, nullptr);
   ctx->launches++;
   timing_main_end(ctx);
   if (e != cudaSuccess) return cuda_status(e);

@@ -1,0 +1,78 @@
+// p2p_packed.cu -- instances and launch helpers of the packed-FP32 velocity kernels.
+#include "obs_context.h"
+#include "p2p_packed.cuh"
+
+namespace obs {
+
+namespace {
+
+// Sources staged for the packed kernels: (x, x, y, y), (G, G, -G, -G), (z, z, 0, 0); padded
+// with zero-strength sources at the origin and radius term 1 (finite for both cores).
+__global__ void pack_sources_dup_kernel(const float* __restrict__ sx, const float* __restrict__ sy,
+                                        const float* __restrict__ sr, const float* __restrict__ ss,
+                                        int ns, int ns_pad, int core, float4* __restrict__ out,
+                                        unsigned* __restrict__ meta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const float r = (i < ns && sr) ? sr[i] : 0.0f;
+  if (i < ns) {
+    const float x = sx[i], y = sy[i], g = ss[i], z = radius_term(core, r);
+    out[PK_ELEM * i] = make_float4(x, x, y, y);
+    out[PK_ELEM * i + 1] = make_float4(g, g, -g, -g);
+    out[PK_ELEM * i + 2] = make_float4(z, z, 0.0f, 0.0f);
+  } else if (i < ns_pad) {
+    out[PK_ELEM * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    out[PK_ELEM * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    out[PK_ELEM * i + 2] = make_float4(1.0f, 1.0f, 0.0f, 0.0f);
+  }
+  // radius extrema, as pack_sources_kernel does
+  unsigned rmin = (i < ns) ? __float_as_uint(r) : ~0u;
+  unsigned rmax = (i < ns) ? __float_as_uint(r) : 0u;
+  int any = (i < ns) ? 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) {
+    rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+    rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    any |= __shfl_xor_sync(0xffffffffu, any, o);
+  }
+  if ((threadIdx.x & 31) == 0 && any) {
+    atomicMax(&meta[0], ~rmin);
+    atomicMax(&meta[1], rmax);
+  }
+}
+
+template <int CORE, int NP>
+cudaError_t packed_dispatch_np(bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st, int* occ) {
+  auto run = [&](auto kern) -> cudaError_t {
+    if (!a) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, P2P_THREADS, 0);
+    kern<<<grid, P2P_THREADS, 0, st>>>(*a);
+    return cudaGetLastError();
+  };
+  if (thick) return comp ? run(p2p_packed_kernel<CORE, true, true, NP>) : run(p2p_packed_kernel<CORE, true, false, NP>);
+  return comp ? run(p2p_packed_kernel<CORE, false, true, NP>) : run(p2p_packed_kernel<CORE, false, false, NP>);
+}
+
+}  // namespace
+
+bool packed_supported(int core, int res) {
+  return res == RES_VEL && (core == CORE_GAUSS || core == CORE_RM);
+}
+
+cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
+                            int* occ) {
+  if (core == CORE_GAUSS) {
+    return np == 4 ? packed_dispatch_np<CORE_GAUSS, 4>(thick, comp, a, grid, st, occ)
+                   : packed_dispatch_np<CORE_GAUSS, 2>(thick, comp, a, grid, st, occ);
+  }
+  if (core == CORE_RM) {
+    return np == 4 ? packed_dispatch_np<CORE_RM, 4>(thick, comp, a, grid, st, occ)
+                   : packed_dispatch_np<CORE_RM, 2>(thick, comp, a, grid, st, occ);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, int ns, int ns_pad,
+                               int core, float4* out, unsigned* meta, cudaStream_t st) {
+  pack_sources_dup_kernel<<<(ns_pad + 255) / 256, 256, 0, st>>>(sx, sy, sr, ss, ns, ns_pad, core, out, meta);
+  return cudaGetLastError();
+}
+
+}  // namespace obs

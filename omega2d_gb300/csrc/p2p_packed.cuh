@@ -1,0 +1,230 @@
+// p2p_packed.cuh -- velocity-only particle kernels with packed FP32 (f32x2) arithmetic.
+//
+// Same work decomposition, TMA pipeline, bounded waits and compensated accumulation as
+// p2p_kernel.cuh; what changes is the inner loop.  Each thread holds NP pairs of targets in
+// 64-bit register pairs and every FP32 operation of the pair arithmetic is issued as one
+// packed FADD2/FMUL2/FFMA2 for two targets.  Sources are staged pre-duplicated
+// (x, x, y, y | G, G, -G, -G | z, z, -, -) so the packed operands need no broadcast moves.
+//
+// Gaussian core (src/CoreFunc.h:111-153), all radii equal (the hoisted path):
+//   t = d^2 * (-cf log2 e);  e = 2^t;  G K = (1/d^2) * (G - G e)   [FFMA2(e, -G, G), FMUL2]
+//   d^2/s^2 < 0.001 -> G K = G cf (the reference's cut-off, also covers the coincident pair);
+//   d^2/s^2 > 16 uses the same expression: it differs from the reference's 1/d^2 by
+//   e^{-d^2/s^2} < 1.2e-7 relative, below FP32 resolution.
+// Rosenhead-Moore core (src/CoreFunc.h:47-59): G K = G / (d^2 + s^2).
+// With varying radii the kernel evaluates the reference forms per target (scalar).
+#pragma once
+
+#include "p2p_kernel.cuh"
+
+namespace obs {
+
+constexpr int PK_ELEM = 3;   // float4 per staged source
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// packed two-sum: hi + lo accumulates b
+__device__ __forceinline__ void two_sum2(float2& hi, float2& lo, float2 b) {
+  const float2 m1 = f2(-1.0f, -1.0f);
+  const float2 s = __fadd2_rn(hi, b);
+  const float2 bp = __ffma2_rn(hi, m1, s);        // s - hi
+  const float2 ap = __ffma2_rn(bp, m1, s);        // s - bp
+  const float2 da = __ffma2_rn(ap, m1, hi);       // hi - ap
+  const float2 db = __ffma2_rn(bp, m1, b);        // b - bp
+  lo = __fadd2_rn(lo, __fadd2_rn(da, db));
+  hi = s;
+}
+
+template <int CORE, bool THICK, bool COMP, int NP, bool UNIF>
+__device__ __forceinline__ void packed_tile(const float4* __restrict__ tile, const float2 (&ntx)[NP],
+                                            const float2 (&nty)[NP], const float2 (&tz)[NP], float us2, float ucf,
+                                            float2 (&u)[NP], float2 (&vn)[NP], float2 (&hu)[NP], float2 (&lu)[NP],
+                                            float2 (&hv)[NP], float2 (&lv)[NP]) {
+  constexpr int NB = COMP ? SRC_TILE / COMP_BLOCK : 1;
+  constexpr int BLK = COMP ? COMP_BLOCK : SRC_TILE;
+  const float cfl = -ucf * kLog2e;
+  const float thr = -0.001f * kLog2e;            // d^2/s^2 < 0.001  <=>  t > thr
+  const float2 cfl2 = f2(cfl, cfl);
+  const float2 s22 = f2(us2, us2);
+  for (int b = 0; b < NB; ++b) {
+#pragma unroll 2
+    for (int jj = 0; jj < BLK; ++jj) {
+      const float4* e4 = tile + PK_ELEM * (b * BLK + jj);
+      const float4 A = e4[0];
+      const float4 B = e4[1];
+      const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+      const float2 g2 = f2(B.x, B.y), ng2 = f2(B.z, B.w);
+      if constexpr (UNIF) {
+        if constexpr (CORE == CORE_GAUSS) {
+          const float gcf = B.x * ucf;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+            const float2 ndy = __fadd2_rn(sy2, nty[p]);
+            float2 d2 = __fmul2_rn(ndy, ndy);
+            d2 = __ffma2_rn(ndx, ndx, d2);
+            const float2 t = __fmul2_rn(d2, cfl2);
+            const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
+            const float2 e = f2(ex2_a(t.x), ex2_a(t.y));
+            const float2 omeg = __ffma2_rn(e, ng2, g2);
+            float2 r2 = __fmul2_rn(ood2, omeg);
+            r2.x = (t.x > thr) ? gcf : r2.x;
+            r2.y = (t.y > thr) ? gcf : r2.y;
+            u[p] = __ffma2_rn(r2, ndy, u[p]);
+            vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+          }
+        } else {  // CORE_RM
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+            const float2 ndy = __fadd2_rn(sy2, nty[p]);
+            float2 q = __ffma2_rn(ndy, ndy, s22);
+            q = __ffma2_rn(ndx, ndx, q);
+            const float2 k = f2(rcp_a(q.x), rcp_a(q.y));
+            const float2 r2 = __fmul2_rn(g2, k);
+            u[p] = __ffma2_rn(r2, ndy, u[p]);
+            vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+          }
+        }
+      } else {
+        // varying radii: the reference forms per target (scalar)
+        const float4 C = e4[2];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+          const float2 ndy = __fadd2_rn(sy2, nty[p]);
+          float2 d2 = __fmul2_rn(ndy, ndy);
+          d2 = __ffma2_rn(ndx, ndx, d2);
+          float K0, K1, Bd;
+          core_eval<CORE, THICK, false, false>(d2.x, C.x, tz[p].x, 0.0f, 0.0f, K0, Bd);
+          core_eval<CORE, THICK, false, false>(d2.y, C.x, tz[p].y, 0.0f, 0.0f, K1, Bd);
+          const float2 r2 = __fmul2_rn(g2, f2(K0, K1));
+          u[p] = __ffma2_rn(r2, ndy, u[p]);
+          vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+        }
+      }
+    }
+    if constexpr (COMP) {
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        two_sum2(hu[p], lu[p], u[p]);
+        two_sum2(hv[p], lv[p], vn[p]);
+        u[p] = f2(0.0f, 0.0f);
+        vn[p] = f2(0.0f, 0.0f);
+      }
+    }
+  }
+}
+
+template <int CORE, bool THICK, bool COMP, int NP>
+__global__ void __launch_bounds__(P2P_THREADS)
+p2p_packed_kernel(const P2PArgs a) {
+  constexpr int TPT = 2 * NP;
+  constexpr int TB = P2P_THREADS * TPT;
+  constexpr uint32_t TILE_BYTES = SRC_TILE * PK_ELEM * sizeof(float4);
+  __shared__ __align__(128) float4 tile[NSTAGE][SRC_TILE * PK_ELEM];
+  __shared__ __align__(8) uint64_t bar[NSTAGE];
+  __shared__ int s_item;
+
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool unif = (~a.meta[0] == a.meta[1]) && (!THICK || ~a.meta[2] == a.meta[3]);
+  float us2 = 0.0f, ucf = 0.0f;
+  if (unif) {
+    us2 = radius_term(CORE, __uint_as_float(a.meta[1])) + (THICK ? radius_term(CORE, __uint_as_float(a.meta[3])) : 0.0f);
+    ucf = __frcp_rn(us2);
+  }
+
+  uint32_t kt = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int item = *static_cast<volatile int*>(&s_item);
+    if (item >= a.nitems) break;
+    const int tb = item % a.ntb;
+    const int sp = item / a.ntb;
+    const int tile0 = sp * a.tiles_per_split;
+    const int ntile = min(a.tiles_per_split, a.nst - tile0);
+    if (tid == 0) {
+      fence_proxy_async_smem();
+      for (int s = 0; s < NSTAGE && s < ntile; ++s) {
+        const int st = (kt + s) % NSTAGE;
+        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+        bulk_g2s(&tile[st][0], a.src + (size_t)(tile0 + s) * SRC_TILE * PK_ELEM, TILE_BYTES, &bar[st]);
+      }
+    }
+    // targets k = 2p, 2p+1 of this thread sit at tb*TB + k*P2P_THREADS + tid
+    float2 ntx[NP], nty[NP], tz[NP], u[NP], vn[NP], hu[NP], lu[NP], hv[NP], lv[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      float xs[2], ys[2], zs[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = tb * TB + (2 * p + h) * P2P_THREADS + tid;
+        const int ic = (i < a.nt) ? i : (a.nt - 1);
+        xs[h] = -a.tx[ic];
+        ys[h] = -a.ty[ic];
+        zs[h] = THICK ? radius_term(CORE, a.tr[ic]) : 0.0f;
+      }
+      ntx[p] = f2(xs[0], xs[1]);
+      nty[p] = f2(ys[0], ys[1]);
+      tz[p] = f2(zs[0], zs[1]);
+      u[p] = vn[p] = hu[p] = lu[p] = hv[p] = lv[p] = f2(0.0f, 0.0f);
+    }
+    for (int t = 0; t < ntile; ++t, ++kt) {
+      const int st = kt % NSTAGE;
+      const bool ok = mbar_wait_bounded(&bar[st], (kt / NSTAGE) & 1u, WAIT_TRIES);
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) {
+          record_failure(a.status, DEV_ERR_TIMEOUT, 210 + st, (int)kt, item);
+          for (int s = 0; s < NSTAGE; ++s) (void)mbar_wait_bounded(&bar[(kt + s) % NSTAGE], ((kt + s) / NSTAGE) & 1u, WAIT_TRIES);
+        }
+        return;
+      }
+      if (unif)
+        packed_tile<CORE, THICK, COMP, NP, true>(&tile[st][0], ntx, nty, tz, us2, ucf, u, vn, hu, lu, hv, lv);
+      else
+        packed_tile<CORE, THICK, COMP, NP, false>(&tile[st][0], ntx, nty, tz, us2, ucf, u, vn, hu, lu, hv, lv);
+      __syncthreads();
+      if (tid == 0 && t + NSTAGE < ntile) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar[st], TILE_BYTES);
+        bulk_g2s(&tile[st][0], a.src + (size_t)(tile0 + t + NSTAGE) * SRC_TILE * PK_ELEM, TILE_BYTES, &bar[st]);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = tb * TB + (2 * p + h) * P2P_THREADS + tid;
+        if (i >= a.nt) continue;
+        double c[2];
+        if (COMP) {
+          c[0] = (double)(h ? hu[p].y : hu[p].x) + (double)(h ? lu[p].y : lu[p].x);
+          c[1] = -((double)(h ? hv[p].y : hv[p].x) + (double)(h ? lv[p].y : lv[p].x));
+        } else {
+          c[0] = (double)(h ? u[p].y : u[p].x);
+          c[1] = -(double)(h ? vn[p].y : vn[p].x);
+        }
+        if (a.direct) {
+          store_target<RES_VEL>(a, i, c);
+        } else if (COMP) {
+          double* q = static_cast<double*>(a.part);
+          q[((size_t)0 * a.nsplit + sp) * a.nt + i] = c[0];
+          q[((size_t)1 * a.nsplit + sp) * a.nt + i] = c[1];
+        } else {
+          float* q = static_cast<float*>(a.part);
+          q[((size_t)0 * a.nsplit + sp) * a.nt + i] = (float)c[0];
+          q[((size_t)1 * a.nsplit + sp) * a.nt + i] = (float)c[1];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace obs
