@@ -5,7 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 
-#include "../../include/omega2d_gb300.h"
+#include "omega2d_gb300.h"
 
 namespace obs {
 

@@ -116,8 +116,10 @@ __device__ __forceinline__ void packed_tile(const float4* __restrict__ tile, con
   }
 }
 
+// NP = 2 fits 64 registers without spills: 8 CTAs (32 warps) per SM to hide the MUFU and
+// packed-FMA latencies; NP = 4 keeps its 128 registers (4 CTAs per SM).
 template <int CORE, bool THICK, bool COMP, int NP>
-__global__ void __launch_bounds__(P2P_THREADS)
+__global__ void __launch_bounds__(P2P_THREADS, NP == 2 ? 8 : 4)
 p2p_packed_kernel(const P2PArgs a) {
   constexpr int TPT = 2 * NP;
   constexpr int TB = P2P_THREADS * TPT;
