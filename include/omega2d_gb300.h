@@ -82,6 +82,22 @@ int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 #define OBS_VARIANT_PACKED2 2
 #define OBS_VARIANT_PACKED4 4
 int obs_set_kernel_variant(obs_context* ctx, int variant);
+/* Processing order inside a packed Gaussian velocity sum.  Binning sorts points into a
+ * 256 x 256 Morton-ordered grid over their bounding box (a stable sort), so that each warp's
+ * targets and each block of 32 sources lie close together; (warp, block) pairs farther apart
+ * than 4 core radii then take the reference's far-field form G/d^2 (d^2/s^2 > 16) without the
+ * exponential.  Results are always written in the caller's order.
+ *   INPUT          : caller's order for targets and sources;
+ *   BINNED_TARGETS : binned targets; results are bit-identical to INPUT;
+ *   BINNED         : binned targets and sources; sources are summed in the binned order, so
+ *                    results differ from INPUT by rounding only (and are reproducible);
+ *   AUTO           : BINNED when the sum has at least 2e9 pairs and 4096 targets and sources,
+ *                    else INPUT. */
+#define OBS_ORDER_AUTO 0
+#define OBS_ORDER_INPUT 1
+#define OBS_ORDER_BINNED 2
+#define OBS_ORDER_BINNED_TARGETS 3
+int obs_set_target_order(obs_context* ctx, int order);
 /* Number of engine kernel launches issued by this context since creation. */
 long long obs_launch_count(obs_context* ctx);
 const char* obs_status_string(int status);

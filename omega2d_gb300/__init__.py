@@ -34,6 +34,7 @@ VELONLY, VELANDGRAD, PSIONLY, VELANDVORT, VELANDSHEAR = 1, 2, 3, 4, 5
 PLAIN_F32, COMPENSATED = 0, 1
 FLAG_FINALIZE = 1
 VARIANT_AUTO, VARIANT_GENERIC, VARIANT_PACKED2, VARIANT_PACKED4 = 0, 1, 2, 4
+ORDER_AUTO, ORDER_INPUT, ORDER_BINNED, ORDER_BINNED_TARGETS = 0, 1, 2, 3
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "allocation failed", -3: "CUDA runtime error",
           -4: "device wait timed out", -5: "no usable CUDA device", -6: "singular matrix",
@@ -134,6 +135,11 @@ class Context:
     def set_kernel_variant(self, variant: int):
         """VARIANT_AUTO (packed FP32 kernels where available), VARIANT_GENERIC, PACKED2/PACKED4."""
         _check(lib().obs_set_kernel_variant(self._h, ctypes.c_int(variant)), "obs_set_kernel_variant")
+
+    def set_target_order(self, order: int):
+        """ORDER_AUTO, ORDER_INPUT, ORDER_BINNED (targets and sources) or ORDER_BINNED_TARGETS: the
+        processing order of packed Gaussian velocity sums (results stay in the caller's order)."""
+        _check(lib().obs_set_target_order(self._h, ctypes.c_int(order)), "obs_set_target_order")
 
     @property
     def launches(self) -> int:

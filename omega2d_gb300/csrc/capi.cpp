@@ -237,6 +237,15 @@ int obs_set_kernel_variant(obs_context* ctx, int variant) {
   return OBS_OK;
 }
 
+int obs_set_target_order(obs_context* ctx, int order) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (order != OBS_ORDER_AUTO && order != OBS_ORDER_INPUT && order != OBS_ORDER_BINNED &&
+      order != OBS_ORDER_BINNED_TARGETS)
+    return OBS_ERR_ARG;
+  ctx->target_order = order;
+  return OBS_OK;
+}
+
 long long obs_launch_count(obs_context* ctx) {
   return ctx ? ctx->launches : -1;
 }

@@ -54,6 +54,7 @@ struct obs_context {
   obs::Timing timing;
   long long launches = 0;
   int kernel_variant = 0;   // OBS_VARIANT_*
+  int target_order = 0;     // OBS_ORDER_*
 };
 
 namespace obs {
@@ -97,7 +98,15 @@ int p2p_ncomp(int res);
 bool packed_supported(int core, int res);
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
                             int* occ);
-cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, int ns, int ns_pad,
-                               int core, float4* out, unsigned* meta, cudaStream_t st);
+cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, const int* perm,
+                               int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st);
+// Spatial (Morton) order of n points (bin_order.cu).  `scratch` holds bin_scratch_bytes(n)
+// bytes, 256-aligned.  On return perm[k] is the caller's index of the k-th point in the order;
+// the order is stable, so it depends on the input alone.  bin_gather writes x, y (and r when
+// given) in that order.
+size_t bin_scratch_bytes(int n);
+cudaError_t bin_order(const float* x, const float* y, int n, void* scratch, int* perm, cudaStream_t st, int* launches);
+cudaError_t bin_gather(const int* perm, const float* x, const float* y, const float* r, int n, float* bx, float* by,
+                       float* br, cudaStream_t st, int* launches);
 
 }  // namespace obs

@@ -155,25 +155,65 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int nitems = ntb * nsplit;
   const int grid = std::min(nitems, slots);
   const int nc = ncomp_of(res);
+  // spatial (Morton) order lets the packed Gaussian kernel skip the exponential for far (warp, block) pairs
+  const int order = ctx->target_order;
+  const bool gauss_packed = packed && rq.core == CORE_GAUSS;
+  const bool big = (double)rq.ns * rq.nt >= 2e9 && rq.nt >= 4096 && rq.ns >= 4096;
+  const bool bin_t = gauss_packed && (order == OBS_ORDER_BINNED || order == OBS_ORDER_BINNED_TARGETS ||
+                                      (order == OBS_ORDER_AUTO && big));
+  const bool bin_s = gauss_packed && (order == OBS_ORDER_BINNED || (order == OBS_ORDER_AUTO && big));
+  const bool same_pts = bin_t && bin_s && rq.sx == rq.tx && rq.sy == rq.ty && rq.ns == rq.nt;
 
-  // ---- work buffer: header | packed sources | partials
+  // ---- work buffer: header | packed sources | partials | target order (perm, x, y, r) |
+  //      source order (perm) | sort scratch
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t hdr = 256;
   const size_t src_bytes = (size_t)nst * SRC_TILE * sizeof(float4) * (packed ? PK_ELEM : 1);
-  const size_t part_bytes = nsplit > 1 ? (size_t)nc * nsplit * rq.nt * (comp ? sizeof(double) : sizeof(float)) : 0;
-  int s = ctx->work.ensure(hdr + src_bytes + part_bytes, st);
+  const size_t part_bytes = nsplit > 1 ? al((size_t)nc * nsplit * rq.nt * (comp ? sizeof(double) : sizeof(float))) : 0;
+  const size_t tvec = al((size_t)rq.nt * sizeof(float));
+  const size_t svec = (bin_s && !same_pts) ? al((size_t)rq.ns * sizeof(int)) : 0;
+  const size_t sort_bytes = (bin_t || bin_s) ? bin_scratch_bytes(std::max(bin_t ? rq.nt : 0, bin_s ? rq.ns : 0)) : 0;
+  const size_t bin_bytes = (bin_t ? 4 * tvec : 0) + svec + sort_bytes;
+  int s = ctx->work.ensure(hdr + src_bytes + part_bytes + bin_bytes, st);
   if (s) return s;
   WorkHeader* h = ctx->work.as<WorkHeader>(0);
   float4* src = ctx->work.as<float4>(hdr);
   void* part = part_bytes ? ctx->work.as<char>(hdr + src_bytes) : nullptr;
+  size_t off = hdr + src_bytes + part_bytes;
+  int* tperm = nullptr;
+  float *bx = nullptr, *by = nullptr, *br = nullptr;
+  if (bin_t) {
+    tperm = ctx->work.as<int>(off);
+    bx = ctx->work.as<float>(off + tvec);
+    by = ctx->work.as<float>(off + 2 * tvec);
+    if (thick) br = ctx->work.as<float>(off + 3 * tvec);
+    off += 4 * tvec;
+  }
+  int* sperm = nullptr;
+  if (bin_s) {
+    sperm = same_pts ? tperm : ctx->work.as<int>(off);
+    off += svec;
+  }
+  void* sort_scratch = sort_bytes ? ctx->work.as<char>(off) : nullptr;
 
   timing_begin(ctx);
   e = cudaMemsetAsync(h, 0, sizeof(WorkHeader), st);
   if (e != cudaSuccess) return cuda_status(e);
   {
+    int nl = 0;
+    if (bin_t) {
+      e = bin_order(rq.tx, rq.ty, rq.nt, sort_scratch, tperm, st, &nl);
+      if (e == cudaSuccess) e = bin_gather(tperm, rq.tx, rq.ty, rq.tr, rq.nt, bx, by, br, st, &nl);
+    }
+    if (e == cudaSuccess && bin_s && !same_pts) e = bin_order(rq.sx, rq.sy, rq.ns, sort_scratch, sperm, st, &nl);
+    ctx->launches += nl;
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  {
     const int threads = 256;
     const int ns_pad = nst * SRC_TILE;
     if (packed) {
-      e = packed_launch_pack(rq.sx, rq.sy, rq.sr, rq.ss, rq.ns, ns_pad, kcore, src, h->meta, st);
+      e = packed_launch_pack(rq.sx, rq.sy, rq.sr, rq.ss, sperm, rq.ns, ns_pad, kcore, src, h->meta, st);
       if (e != cudaSuccess) return cuda_status(e);
     } else {
       pack_sources_kernel<<<(ns_pad + threads - 1) / threads, threads, 0, st>>>(
@@ -193,6 +233,10 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   a.src = src;
   a.nst = nst;
   a.tx = rq.tx; a.ty = rq.ty; a.tr = rq.tr;
+  if (bin_t) {
+    a.tx = bx; a.ty = by; a.tr = br;
+    a.perm = tperm;
+  }
   a.nt = rq.nt; a.ntb = ntb;
   a.nsplit = nsplit; a.tiles_per_split = tps; a.nitems = nitems;
   a.counter = &h->counter;

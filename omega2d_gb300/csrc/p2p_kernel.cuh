@@ -42,6 +42,7 @@ struct P2PArgs {
   int* status;           // DEV_ERR_* bits
   float* out[6];         // u, v, then extras (grad: ux vx uy vy; vort: w; shear: e; psi: p)
   void* part;            // split partials [ncomp][nsplit][nt] (double if compensated, else float)
+  const int* perm;       // targets processed in binned order: output index of binned target i
   int direct;            // nsplit == 1: write outputs from the main kernel
   int finalize;          // apply fs + (1/2pi) in the epilogue
   double fsx, fsy;
@@ -62,8 +63,10 @@ constexpr double kInv2Pi = 0.15915494309189535;   // 0.5/pi, src/ElementBase.h:2
 // GRAD components: S1 = sum G*b*dx*dy, S2 = sum G*(b dx^2 + K), S3 = -sum G*(b dy^2 + K);
 // then du/dx = -S1, dv/dy = S1, dv/dx = S2, du/dy = S3 (kernelug_0v_0b, src/Kernels.h:112-133).
 template <int RES>
-__device__ __forceinline__ void store_target(const P2PArgs& a, int i, const double* c) {
+__device__ __forceinline__ void store_target(const P2PArgs& a, int ib, const double* c) {
   const double f = a.finalize ? kInv2Pi : 1.0;
+  const int i = a.perm ? a.perm[ib] : ib;
+  if ((unsigned)i >= (unsigned)a.nt) return;      // never taken: perm is a permutation of 0..nt-1
   auto put = [&](int k, double add, double fs) {
     float* p = a.out[k];
     const double v = ((double)p[i] + add) * f + fs;

@@ -7,15 +7,18 @@ namespace obs {
 namespace {
 
 // Sources staged for the packed kernels: (x, x, y, y), (G, G, -G, -G), (z, z, 0, 0); padded
-// with zero-strength sources at the origin and radius term 1 (finite for both cores).
+// with zero-strength sources at the origin and radius term 1 (finite for both cores).  With a
+// permutation, staged source i is the caller's source perm[i].
 __global__ void pack_sources_dup_kernel(const float* __restrict__ sx, const float* __restrict__ sy,
                                         const float* __restrict__ sr, const float* __restrict__ ss,
-                                        int ns, int ns_pad, int core, float4* __restrict__ out,
-                                        unsigned* __restrict__ meta) {
+                                        const int* __restrict__ perm, int ns, int ns_pad, int core,
+                                        float4* __restrict__ out, unsigned* __restrict__ meta) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const float r = (i < ns && sr) ? sr[i] : 0.0f;
+  int j = (i < ns && perm) ? perm[i] : i;
+  if ((unsigned)j >= (unsigned)ns) j = i;         // never taken for i < ns: perm is a permutation
+  const float r = (i < ns && sr) ? sr[j] : 0.0f;
   if (i < ns) {
-    const float x = sx[i], y = sy[i], g = ss[i], z = radius_term(core, r);
+    const float x = sx[j], y = sy[j], g = ss[j], z = radius_term(core, r);
     out[PK_ELEM * i] = make_float4(x, x, y, y);
     out[PK_ELEM * i + 1] = make_float4(g, g, -g, -g);
     out[PK_ELEM * i + 2] = make_float4(z, z, 0.0f, 0.0f);
@@ -69,9 +72,9 @@ cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PAr
   return cudaErrorInvalidValue;
 }
 
-cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, int ns, int ns_pad,
-                               int core, float4* out, unsigned* meta, cudaStream_t st) {
-  pack_sources_dup_kernel<<<(ns_pad + 255) / 256, 256, 0, st>>>(sx, sy, sr, ss, ns, ns_pad, core, out, meta);
+cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, const int* perm,
+                               int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st) {
+  pack_sources_dup_kernel<<<(ns_pad + 255) / 256, 256, 0, st>>>(sx, sy, sr, ss, perm, ns, ns_pad, core, out, meta);
   return cudaGetLastError();
 }
 

@@ -5,12 +5,18 @@
 // 64-bit register pairs and every FP32 operation of the pair arithmetic is issued as one
 // packed FADD2/FMUL2/FFMA2 for two targets.  Sources are staged pre-duplicated
 // (x, x, y, y | G, G, -G, -G | z, z, -, -) so the packed operands need no broadcast moves.
+// A warp owns 32*2*NP consecutive targets (consecutive in the binned order when the host
+// bins targets spatially, see p2p_packed.cu).
 //
-// Gaussian core (src/CoreFunc.h:111-153), all radii equal (the hoisted path):
-//   t = d^2 * (-cf log2 e);  e = 2^t;  G K = (1/d^2) * (G - G e)   [FFMA2(e, -G, G), FMUL2]
-//   d^2/s^2 < 0.001 -> G K = G cf (the reference's cut-off, also covers the coincident pair);
-//   d^2/s^2 > 16 uses the same expression: it differs from the reference's 1/d^2 by
-//   e^{-d^2/s^2} < 1.2e-7 relative, below FP32 resolution.
+// Gaussian core (src/CoreFunc.h:111-153), all radii equal (the hoisted path), per pair with
+// x = d^2/s^2, exactly the reference's three branches:
+//   x > 16     : G K = G * (1/d^2)                                   (fast form)
+//   x < 0.001  : G K = G * (1/s^2)
+//   otherwise  : G K = (1/d^2) * (G - G e),  e = 2^(d^2 * (-log2 e / s^2))
+// Per tile each warp marks the 32-source blocks that have a source within 4.02 s of the
+// warp's target bounding box (a conservative test); unmarked blocks only need the fast form
+// and skip the exponential.  Marked blocks evaluate all three branches, so a pair gets the same
+// value whichever path its warp takes.
 // Rosenhead-Moore core (src/CoreFunc.h:47-59): G K = G / (d^2 + s^2).
 // With varying radii the kernel evaluates the reference forms per target (scalar).
 #pragma once
@@ -20,6 +26,8 @@
 namespace obs {
 
 constexpr int PK_ELEM = 3;   // float4 per staged source
+constexpr int PK_BLK = 32;   // sources per near-mask bit word / compensated block
+constexpr int PK_NB = SRC_TILE / PK_BLK;
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
@@ -35,111 +43,146 @@ __device__ __forceinline__ void two_sum2(float2& hi, float2& lo, float2 b) {
   hi = s;
 }
 
-template <int CORE, bool THICK, bool COMP, int NP, bool UNIF>
-__device__ __forceinline__ void packed_tile(const float4* __restrict__ tile, const float2 (&ntx)[NP],
-                                            const float2 (&nty)[NP], const float2 (&tz)[NP], float us2, float ucf,
-                                            float2 (&u)[NP], float2 (&vn)[NP], float2 (&hu)[NP], float2 (&lu)[NP],
-                                            float2 (&hv)[NP], float2 (&lv)[NP]) {
-  constexpr int NB = COMP ? SRC_TILE / COMP_BLOCK : 1;
-  constexpr int BLK = COMP ? COMP_BLOCK : SRC_TILE;
-  const float cfl = -ucf * kLog2e;
-  const float thr = -0.001f * kLog2e;            // d^2/s^2 < 0.001  <=>  t > thr
-  const float2 cfl2 = f2(cfl, cfl);
-  const float2 s22 = f2(us2, us2);
-  for (int b = 0; b < NB; ++b) {
+struct PackedUni {
+  float us2, ucf, cfl, thr_small, thr_far;
+  float2 cfl2, s22;
+};
+
+// Gaussian, uniform radii: one 32-source block; FULL evaluates all three branches
+template <bool FULL, int NP>
+__device__ __forceinline__ void gauss_block(const float4* __restrict__ blk, const PackedUni& q,
+                                            const float2 (&ntx)[NP], const float2 (&nty)[NP],
+                                            float2 (&u)[NP], float2 (&vn)[NP]) {
 #pragma unroll 2
-    for (int jj = 0; jj < BLK; ++jj) {
-      const float4* e4 = tile + PK_ELEM * (b * BLK + jj);
-      const float4 A = e4[0];
-      const float4 B = e4[1];
-      const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
-      const float2 g2 = f2(B.x, B.y), ng2 = f2(B.z, B.w);
-      if constexpr (UNIF) {
-        if constexpr (CORE == CORE_GAUSS) {
-          const float gcf = B.x * ucf;
-#pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float2 ndx = __fadd2_rn(sx2, ntx[p]);
-            const float2 ndy = __fadd2_rn(sy2, nty[p]);
-            float2 d2 = __fmul2_rn(ndy, ndy);
-            d2 = __ffma2_rn(ndx, ndx, d2);
-            const float2 t = __fmul2_rn(d2, cfl2);
-            const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
-            const float2 e = f2(ex2_a(t.x), ex2_a(t.y));
-            const float2 omeg = __ffma2_rn(e, ng2, g2);
-            float2 r2 = __fmul2_rn(ood2, omeg);
-            r2.x = (t.x > thr) ? gcf : r2.x;
-            r2.y = (t.y > thr) ? gcf : r2.y;
-            u[p] = __ffma2_rn(r2, ndy, u[p]);
-            vn[p] = __ffma2_rn(r2, ndx, vn[p]);
-          }
-        } else {  // CORE_RM
-#pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float2 ndx = __fadd2_rn(sx2, ntx[p]);
-            const float2 ndy = __fadd2_rn(sy2, nty[p]);
-            float2 q = __ffma2_rn(ndy, ndy, s22);
-            q = __ffma2_rn(ndx, ndx, q);
-            const float2 k = f2(rcp_a(q.x), rcp_a(q.y));
-            const float2 r2 = __fmul2_rn(g2, k);
-            u[p] = __ffma2_rn(r2, ndy, u[p]);
-            vn[p] = __ffma2_rn(r2, ndx, vn[p]);
-          }
-        }
-      } else {
-        // varying radii: the reference forms per target (scalar)
-        const float4 C = e4[2];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          const float2 ndx = __fadd2_rn(sx2, ntx[p]);
-          const float2 ndy = __fadd2_rn(sy2, nty[p]);
-          float2 d2 = __fmul2_rn(ndy, ndy);
-          d2 = __ffma2_rn(ndx, ndx, d2);
-          float K0, K1, Bd;
-          core_eval<CORE, THICK, false, false>(d2.x, C.x, tz[p].x, 0.0f, 0.0f, K0, Bd);
-          core_eval<CORE, THICK, false, false>(d2.y, C.x, tz[p].y, 0.0f, 0.0f, K1, Bd);
-          const float2 r2 = __fmul2_rn(g2, f2(K0, K1));
-          u[p] = __ffma2_rn(r2, ndy, u[p]);
-          vn[p] = __ffma2_rn(r2, ndx, vn[p]);
-        }
-      }
-    }
-    if constexpr (COMP) {
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+    if constexpr (!FULL) {
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        two_sum2(hu[p], lu[p], u[p]);
-        two_sum2(hv[p], lv[p], vn[p]);
-        u[p] = f2(0.0f, 0.0f);
-        vn[p] = f2(0.0f, 0.0f);
+        const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+        const float2 ndy = __fadd2_rn(sy2, nty[p]);
+        float2 d2 = __fmul2_rn(ndy, ndy);
+        d2 = __ffma2_rn(ndx, ndx, d2);
+        const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
+        const float2 r2 = __fmul2_rn(g2, ood2);
+        u[p] = __ffma2_rn(r2, ndy, u[p]);
+        vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+      }
+    } else {
+      const float2 ng2 = f2(B.z, B.w);
+      const float gcf = B.x * q.ucf;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+        const float2 ndy = __fadd2_rn(sy2, nty[p]);
+        float2 d2 = __fmul2_rn(ndy, ndy);
+        d2 = __ffma2_rn(ndx, ndx, d2);
+        const float2 t = __fmul2_rn(d2, q.cfl2);
+        const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
+        const float2 e = f2(ex2_a(t.x), ex2_a(t.y));
+        const float2 omeg = __ffma2_rn(e, ng2, g2);
+        const float2 rm = __fmul2_rn(ood2, omeg);
+        const float2 rf = __fmul2_rn(g2, ood2);
+        float2 r2;
+        r2.x = (t.x < q.thr_far) ? rf.x : ((t.x > q.thr_small) ? gcf : rm.x);
+        r2.y = (t.y < q.thr_far) ? rf.y : ((t.y > q.thr_small) ? gcf : rm.y);
+        u[p] = __ffma2_rn(r2, ndy, u[p]);
+        vn[p] = __ffma2_rn(r2, ndx, vn[p]);
       }
     }
   }
 }
 
-// NP = 2 fits 64 registers without spills: 8 CTAs (32 warps) per SM to hide the MUFU and
-// packed-FMA latencies; NP = 4 keeps its 128 registers (4 CTAs per SM).
+// RM, uniform radii, one 32-source block
+template <int NP>
+__device__ __forceinline__ void rm_block(const float4* __restrict__ blk, const PackedUni& q, const float2 (&ntx)[NP],
+                                         const float2 (&nty)[NP], float2 (&u)[NP], float2 (&vn)[NP]) {
+#pragma unroll 2
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+      const float2 ndy = __fadd2_rn(sy2, nty[p]);
+      float2 w = __ffma2_rn(ndy, ndy, q.s22);
+      w = __ffma2_rn(ndx, ndx, w);
+      const float2 k = f2(rcp_a(w.x), rcp_a(w.y));
+      const float2 r2 = __fmul2_rn(g2, k);
+      u[p] = __ffma2_rn(r2, ndy, u[p]);
+      vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+    }
+  }
+}
+
+// varying radii: the reference forms per target, one 32-source block
+template <int CORE, bool THICK, int NP>
+__device__ __forceinline__ void general_block(const float4* __restrict__ blk, const float2 (&ntx)[NP],
+                                              const float2 (&nty)[NP], const float2 (&tz)[NP], float2 (&u)[NP],
+                                              float2 (&vn)[NP]) {
+#pragma unroll 2
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float4 C = blk[PK_ELEM * jj + 2];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+      const float2 ndy = __fadd2_rn(sy2, nty[p]);
+      float2 d2 = __fmul2_rn(ndy, ndy);
+      d2 = __ffma2_rn(ndx, ndx, d2);
+      float K0, K1, Bd;
+      core_eval<CORE, THICK, false, false>(d2.x, C.x, tz[p].x, 0.0f, 0.0f, K0, Bd);
+      core_eval<CORE, THICK, false, false>(d2.y, C.x, tz[p].y, 0.0f, 0.0f, K1, Bd);
+      const float2 r2 = __fmul2_rn(g2, f2(K0, K1));
+      u[p] = __ffma2_rn(r2, ndy, u[p]);
+      vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+    }
+  }
+}
+
+// NP = 2 fits 64 registers without spills: 8 CTAs (32 warps) per SM; NP = 4 keeps its 128
+// registers (4 CTAs per SM).
 template <int CORE, bool THICK, bool COMP, int NP>
 __global__ void __launch_bounds__(P2P_THREADS, NP == 2 ? 8 : 4)
 p2p_packed_kernel(const P2PArgs a) {
   constexpr int TPT = 2 * NP;
   constexpr int TB = P2P_THREADS * TPT;
+  constexpr int WT = 32 * TPT;                      // targets per warp
   constexpr uint32_t TILE_BYTES = SRC_TILE * PK_ELEM * sizeof(float4);
   __shared__ __align__(128) float4 tile[NSTAGE][SRC_TILE * PK_ELEM];
   __shared__ __align__(8) uint64_t bar[NSTAGE];
+  __shared__ unsigned smask[P2P_THREADS / 32][PK_NB];
   __shared__ int s_item;
 
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
     fence_mbar_init();
   }
   __syncthreads();
   const bool unif = (~a.meta[0] == a.meta[1]) && (!THICK || ~a.meta[2] == a.meta[3]);
-  float us2 = 0.0f, ucf = 0.0f;
+  PackedUni q;
+  q.us2 = 0.0f;
+  q.ucf = 0.0f;
   if (unif) {
-    us2 = radius_term(CORE, __uint_as_float(a.meta[1])) + (THICK ? radius_term(CORE, __uint_as_float(a.meta[3])) : 0.0f);
-    ucf = __frcp_rn(us2);
+    q.us2 = radius_term(CORE, __uint_as_float(a.meta[1])) + (THICK ? radius_term(CORE, __uint_as_float(a.meta[3])) : 0.0f);
+    q.ucf = __frcp_rn(q.us2);
   }
+  q.cfl = -q.ucf * kLog2e;
+  q.thr_small = -0.001f * kLog2e;                  // x < 0.001  <=>  t > thr_small
+  q.thr_far = -16.0f * kLog2e;                     // x > 16     <=>  t < thr_far
+  q.cfl2 = f2(q.cfl, q.cfl);
+  q.s22 = f2(q.us2, q.us2);
+  const float lim = 16.16f * q.us2;               // near test with a 1 % margin (d < 4.02 s)
 
   uint32_t kt = 0;
   for (;;) {
@@ -159,23 +202,33 @@ p2p_packed_kernel(const P2PArgs a) {
         bulk_g2s(&tile[st][0], a.src + (size_t)(tile0 + s) * SRC_TILE * PK_ELEM, TILE_BYTES, &bar[st]);
       }
     }
-    // targets k = 2p, 2p+1 of this thread sit at tb*TB + k*P2P_THREADS + tid
+    // this warp's targets: WT consecutive ones; (pair p, half h, lane) -> (2p + h) * 32 + lane
     float2 ntx[NP], nty[NP], tz[NP], u[NP], vn[NP], hu[NP], lu[NP], hv[NP], lv[NP];
+    float bx0 = 3.0e38f, bx1 = -3.0e38f, by0 = 3.0e38f, by1 = -3.0e38f;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       float xs[2], ys[2], zs[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int i = tb * TB + (2 * p + h) * P2P_THREADS + tid;
+        const int i = tb * TB + warp * WT + (2 * p + h) * 32 + lane;
         const int ic = (i < a.nt) ? i : (a.nt - 1);
-        xs[h] = -a.tx[ic];
-        ys[h] = -a.ty[ic];
+        const float x = a.tx[ic], y = a.ty[ic];
+        bx0 = fminf(bx0, x); bx1 = fmaxf(bx1, x);
+        by0 = fminf(by0, y); by1 = fmaxf(by1, y);
+        xs[h] = -x;
+        ys[h] = -y;
         zs[h] = THICK ? radius_term(CORE, a.tr[ic]) : 0.0f;
       }
       ntx[p] = f2(xs[0], xs[1]);
       nty[p] = f2(ys[0], ys[1]);
       tz[p] = f2(zs[0], zs[1]);
       u[p] = vn[p] = hu[p] = lu[p] = hv[p] = lv[p] = f2(0.0f, 0.0f);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+      bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+      by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+      by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
     }
     for (int t = 0; t < ntile; ++t, ++kt) {
       const int st = kt % NSTAGE;
@@ -187,10 +240,42 @@ p2p_packed_kernel(const P2PArgs a) {
         }
         return;
       }
-      if (unif)
-        packed_tile<CORE, THICK, COMP, NP, true>(&tile[st][0], ntx, nty, tz, us2, ucf, u, vn, hu, lu, hv, lv);
-      else
-        packed_tile<CORE, THICK, COMP, NP, false>(&tile[st][0], ntx, nty, tz, us2, ucf, u, vn, hu, lu, hv, lv);
+      const float4* tl = &tile[st][0];
+      if (CORE == CORE_GAUSS && unif) {
+        // near-mask of this warp: bit j of word b set when source b*32+j may be within 4 s
+#pragma unroll
+        for (int b = 0; b < PK_NB; ++b) {
+          const float4 A = tl[PK_ELEM * (b * PK_BLK + lane)];
+          const float dx = fmaxf(0.0f, fmaxf(bx0 - A.x, A.x - bx1));
+          const float dy = fmaxf(0.0f, fmaxf(by0 - A.z, A.z - by1));
+          const unsigned m = __ballot_sync(0xffffffffu, fmaf(dx, dx, dy * dy) <= lim);
+          if (lane == 0) smask[warp][b] = m;
+        }
+        __syncwarp();
+      }
+      for (int b = 0; b < PK_NB; ++b) {
+        const float4* blk = tl + PK_ELEM * b * PK_BLK;
+        if constexpr (CORE == CORE_GAUSS) {
+          if (unif) {
+            if (smask[warp][b] == 0u) gauss_block<false, NP>(blk, q, ntx, nty, u, vn);
+            else gauss_block<true, NP>(blk, q, ntx, nty, u, vn);
+          } else {
+            general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+          }
+        } else {
+          if (unif) rm_block<NP>(blk, q, ntx, nty, u, vn);
+          else general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+        }
+        if constexpr (COMP) {
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            two_sum2(hu[p], lu[p], u[p]);
+            two_sum2(hv[p], lv[p], vn[p]);
+            u[p] = f2(0.0f, 0.0f);
+            vn[p] = f2(0.0f, 0.0f);
+          }
+        }
+      }
       __syncthreads();
       if (tid == 0 && t + NSTAGE < ntile) {
         fence_proxy_async_smem();
@@ -202,7 +287,7 @@ p2p_packed_kernel(const P2PArgs a) {
     for (int p = 0; p < NP; ++p) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int i = tb * TB + (2 * p + h) * P2P_THREADS + tid;
+        const int i = tb * TB + warp * WT + (2 * p + h) * 32 + lane;
         if (i >= a.nt) continue;
         double c[2];
         if (COMP) {
@@ -215,13 +300,13 @@ p2p_packed_kernel(const P2PArgs a) {
         if (a.direct) {
           store_target<RES_VEL>(a, i, c);
         } else if (COMP) {
-          double* q = static_cast<double*>(a.part);
-          q[((size_t)0 * a.nsplit + sp) * a.nt + i] = c[0];
-          q[((size_t)1 * a.nsplit + sp) * a.nt + i] = c[1];
+          double* qp = static_cast<double*>(a.part);
+          qp[((size_t)0 * a.nsplit + sp) * a.nt + i] = c[0];
+          qp[((size_t)1 * a.nsplit + sp) * a.nt + i] = c[1];
         } else {
-          float* q = static_cast<float*>(a.part);
-          q[((size_t)0 * a.nsplit + sp) * a.nt + i] = (float)c[0];
-          q[((size_t)1 * a.nsplit + sp) * a.nt + i] = (float)c[1];
+          float* qp = static_cast<float*>(a.part);
+          qp[((size_t)0 * a.nsplit + sp) * a.nt + i] = (float)c[0];
+          qp[((size_t)1 * a.nsplit + sp) * a.nt + i] = (float)c[1];
         }
       }
     }

@@ -55,3 +55,112 @@ def test_packed_edge_sizes(ctx, restatement, ns, nt):
     og.points_affect_points(og.Points(sx, sy, sr, ss), t, og.VELONLY, og.ExecEnv(og.CORE_GAUSSIAN, og.COMPENSATED, ctx))
     u, v, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, tx, ty, tr, fp64=True)
     assert rel_err(u, t.u) < 2e-6 and rel_err(v, t.v) < 2e-6
+
+
+def _vel(ctx, src, tx, ty, tr, core, accum, order, variant):
+    try:
+        ctx.set_kernel_variant(variant)
+        ctx.set_target_order(order)
+        t = og.Points(tx, ty, tr, None, u=np.full(tx.size, 0.5, np.float32))
+        og.points_affect_points(src, t, og.VELONLY, og.ExecEnv(core, accum, ctx), finalize=True, fs=(1.0, -0.25))
+    finally:
+        ctx.set_kernel_variant(og.VARIANT_AUTO)
+        ctx.set_target_order(og.ORDER_AUTO)
+    return t.u, t.v
+
+
+@pytest.mark.parametrize("sigma", [1e-4, 2e-3, 0.05])
+@pytest.mark.parametrize("thick", [True, False])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED4])
+def test_binned_order_identities(ctx, sigma, thick, accum, variant):
+    """Binned target order gives the same bits as the caller's order: the far-block fast form and
+    the full form agree pair by pair, and each target's sum runs over the sources in one order."""
+    rng = np.random.default_rng(int(sigma * 1e5) + 7 * thick + accum + variant)
+    ns, nt = 9000, 7001
+    sx, sy = rng.normal(0, 0.3, (2, ns)).astype(np.float32)
+    ss = rng.normal(0, 1e-3, ns).astype(np.float32)
+    sr = np.full(ns, sigma, np.float32)
+    tx, ty = rng.normal(0, 0.3, (2, nt)).astype(np.float32)
+    tx[:300], ty[:300] = sx[:300], sy[:300]                        # coincident pairs: x < 0.001
+    tx[300:600] = sx[300:600] + 3 * sigma                          # the exponential branch
+    ty[300:600] = sy[300:600]
+    tr = np.full(nt, sigma, np.float32) if thick else None
+    src = og.Points(sx, sy, sr, ss)
+    a = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_INPUT, variant)
+    b = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED_TARGETS, variant)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    # binned sources change the summation order only: reproducible, and equal up to rounding
+    c = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED, variant)
+    d = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED, variant)
+    assert np.array_equal(c[0], d[0]) and np.array_equal(c[1], d[1])
+    tol = 1e-6 if accum == og.COMPENSATED else 2e-5
+    assert rel_err(a[0], c[0]) < tol and rel_err(a[1], c[1]) < tol
+
+
+@pytest.mark.parametrize("sigma", [1e-4, 2e-3])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+def test_binned_targets_vs_fp64(ctx, restatement, sigma, accum):
+    rng = np.random.default_rng(11 + accum)
+    ns, nt = 6000, 5003
+    sx, sy = rng.normal(0, 0.3, (2, ns)).astype(np.float32)
+    ss = rng.normal(0, 1e-3, ns).astype(np.float32)
+    sr = np.full(ns, sigma, np.float32)
+    tx, ty = rng.normal(0, 0.3, (2, nt)).astype(np.float32)
+    tx[:200], ty[:200] = sx[:200], sy[:200]
+    tx[200:400], ty[200:400] = sx[200:400] + 2.5 * sigma, sy[200:400]
+    tr = np.full(nt, sigma, np.float32)
+    u, v = _vel(ctx, og.Points(sx, sy, sr, ss), tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED,
+                og.VARIANT_AUTO)
+    u64, v64, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, tx, ty, tr, fp64=True,
+                                                   tu=np.full(nt, 0.5), tv=np.zeros(nt))
+    u64, v64 = 1.0 + u64 / (2 * np.pi), -0.25 + v64 / (2 * np.pi)
+    tol = 2e-6 if accum == og.COMPENSATED else 2e-5
+    assert rel_err(u64, u) < tol and rel_err(v64, v) < tol
+
+
+@pytest.mark.parametrize("nt", [1, 31, 4097])
+def test_binned_targets_degenerate(ctx, restatement, nt):
+    """All targets on one point, or on one line: the bounding box has zero width."""
+    rng = np.random.default_rng(nt)
+    ns = 3000
+    sx, sy = rng.uniform(-1, 1, (2, ns)).astype(np.float32)
+    ss = rng.normal(0, 1e-2, ns).astype(np.float32)
+    sr = np.full(ns, 0.01, np.float32)
+    for tx, ty in ((np.full(nt, 0.25, np.float32), np.full(nt, -0.5, np.float32)),
+                   (np.linspace(-1, 1, nt).astype(np.float32), np.zeros(nt, np.float32))):
+        tr = np.full(nt, 0.01, np.float32)
+        u, v = _vel(ctx, og.Points(sx, sy, sr, ss), tx, ty, tr, og.CORE_GAUSSIAN, og.COMPENSATED,
+                    og.ORDER_BINNED, og.VARIANT_AUTO)
+        u64, v64, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, tx, ty, tr, fp64=True,
+                                                       tu=np.full(nt, 0.5), tv=np.zeros(nt))
+        u64, v64 = 1.0 + u64 / (2 * np.pi), -0.25 + v64 / (2 * np.pi)
+        assert rel_err(u64, u) < 2e-6 and rel_err(v64, v) < 2e-6
+
+
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+def test_binned_self_interaction_shared_order(ctx, accum):
+    """Self-interaction on one set of device arrays reuses the target order for the sources;
+    the result equals that of separate copies, whose orders are computed independently."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5 + accum)
+    n = 20000
+    x, y = rng.normal(0, 0.25, (2, n)).astype(np.float32)
+    g = rng.normal(0, 1e-4, n).astype(np.float32)
+    r = np.full(n, 0.003, np.float32)
+    dev = torch.device("cuda", 0)
+    X, Y, R, G = [torch.from_numpy(a).to(dev) for a in (x, y, r, g)]
+    outs = []
+    try:
+        ctx.set_target_order(og.ORDER_BINNED)
+        for same in (True, False):
+            TU = torch.zeros(n, device=dev)
+            TV = torch.zeros(n, device=dev)
+            tx, ty, tr = (X, Y, R) if same else (X.clone(), Y.clone(), R.clone())
+            og.points_affect_points_dev(ctx, og.CORE_GAUSSIAN, og.VELONLY, accum, X, Y, R, G, tx, ty, tr, TU, TV)
+            ctx.synchronize()
+            outs.append((TU.cpu().numpy(), TV.cpu().numpy()))
+    finally:
+        ctx.set_target_order(og.ORDER_AUTO)
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert np.isfinite(outs[0][0]).all()
