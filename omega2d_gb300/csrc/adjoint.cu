@@ -311,6 +311,8 @@ int run_adjoint(obs_context* ctx, int core, int accum, int mode,
                 const float* elu, const float* elv,
                 float* gx, float* gy, float* gg, size_t off) {
   if (no == 0 || ne == 0) return OBS_OK;
+  if (ctx->kernel_variant != OBS_VARIANT_GENERIC && adjoint_packed_supported(core))
+    return run_adjoint_packed(ctx, accum, mode, no, ox, oy, orad, og, ne, ex, ey, er, eg, elu, elv, gx, gy, gg, off);
   const bool comp = accum == OBS_COMPENSATED;
   const bool thick = (mode == ADJ_SELF) || er != nullptr;
   cudaStream_t st = ctx->stream;

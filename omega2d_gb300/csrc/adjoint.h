@@ -13,6 +13,14 @@ int run_adjoint(obs_context* ctx, int core, int accum, int mode,
                 const float* elu, const float* elv,
                 float* gx, float* gy, float* gg, size_t off);
 
+// Packed-FP32 variant for the Gaussian core (adjoint_packed.cu), same arguments and results;
+// run_adjoint dispatches to it unless the generic kernels are forced.
+bool adjoint_packed_supported(int core);
+int run_adjoint_packed(obs_context* ctx, int accum, int mode, int no, const float* ox, const float* oy,
+                       const float* orad, const float* og, int ne, const float* ex, const float* ey, const float* er,
+                       const float* eg, const float* elu, const float* elv, float* gx, float* gy, float* gg,
+                       size_t off);
+
 // Euler (order 1) or Ralston RK2 (order 2) steps of the self-induced velocity, in place on
 // device positions (Convection::advect_1st / advect_2nd_ralston, src/Convection.h:274-466).
 int run_advect(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y,

@@ -10,7 +10,7 @@
 //      exclusive scan over the [digit][tile] table, and a stable scatter whose in-tile ranks
 //      come from warp match + per-warp digit counts, so the order is a function of the input
 //      alone (points of one cell keep the caller's relative order);
-//   4. optional gather of x, y, r into the sorted order.
+//   4. optional gather of x, y, r, g into the sorted order.
 // Everything runs on the caller's stream; nothing is synchronized.
 #include "obs_context.h"
 #include "obs_device.cuh"
@@ -171,8 +171,9 @@ __global__ void __launch_bounds__(RS_THREADS) rs_scatter_kernel(const unsigned* 
 }
 
 __global__ void bin_gather_kernel(const int* __restrict__ perm, const float* __restrict__ x,
-                                  const float* __restrict__ y, const float* __restrict__ r, int n,
-                                  float* __restrict__ bx, float* __restrict__ by, float* __restrict__ br) {
+                                  const float* __restrict__ y, const float* __restrict__ r,
+                                  const float* __restrict__ g, int n, float* __restrict__ bx,
+                                  float* __restrict__ by, float* __restrict__ br, float* __restrict__ bg) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   int i = perm[k];
@@ -180,6 +181,7 @@ __global__ void bin_gather_kernel(const int* __restrict__ perm, const float* __r
   bx[k] = x[i];
   by[k] = y[i];
   if (r) br[k] = r[i];
+  if (g) bg[k] = g[i];
 }
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -221,10 +223,10 @@ cudaError_t bin_order(const float* x, const float* y, int n, void* scratch, int*
   return cudaGetLastError();
 }
 
-cudaError_t bin_gather(const int* perm, const float* x, const float* y, const float* r, int n, float* bx, float* by,
-                       float* br, cudaStream_t st, int* launches) {
+cudaError_t bin_gather(const int* perm, const float* x, const float* y, const float* r, const float* g, int n,
+                       float* bx, float* by, float* br, float* bg, cudaStream_t st, int* launches) {
   if (n <= 0) return cudaSuccess;
-  bin_gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(perm, x, y, r, n, bx, by, br);
+  bin_gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(perm, x, y, r, g, n, bx, by, br, bg);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

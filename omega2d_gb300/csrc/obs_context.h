@@ -102,11 +102,11 @@ cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr
                                int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st);
 // Spatial (Morton) order of n points (bin_order.cu).  `scratch` holds bin_scratch_bytes(n)
 // bytes, 256-aligned.  On return perm[k] is the caller's index of the k-th point in the order;
-// the order is stable, so it depends on the input alone.  bin_gather writes x, y (and r when
+// the order is stable, so it depends on the input alone.  bin_gather writes x, y (and r, g when
 // given) in that order.
 size_t bin_scratch_bytes(int n);
 cudaError_t bin_order(const float* x, const float* y, int n, void* scratch, int* perm, cudaStream_t st, int* launches);
-cudaError_t bin_gather(const int* perm, const float* x, const float* y, const float* r, int n, float* bx, float* by,
-                       float* br, cudaStream_t st, int* launches);
+cudaError_t bin_gather(const int* perm, const float* x, const float* y, const float* r, const float* g, int n,
+                       float* bx, float* by, float* br, float* bg, cudaStream_t st, int* launches);
 
 }  // namespace obs

@@ -203,7 +203,7 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
     int nl = 0;
     if (bin_t) {
       e = bin_order(rq.tx, rq.ty, rq.nt, sort_scratch, tperm, st, &nl);
-      if (e == cudaSuccess) e = bin_gather(tperm, rq.tx, rq.ty, rq.tr, rq.nt, bx, by, br, st, &nl);
+      if (e == cudaSuccess) e = bin_gather(tperm, rq.tx, rq.ty, rq.tr, nullptr, rq.nt, bx, by, br, nullptr, st, &nl);
     }
     if (e == cudaSuccess && bin_s && !same_pts) e = bin_order(rq.sx, rq.sy, rq.ns, sort_scratch, sperm, st, &nl);
     ctx->launches += nl;
