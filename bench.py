@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 N = 1_000_000
 SIGMA = 0.005
 SEED = 2
-METRIC = "Ginteractions/s @N=1M, Gaussian core, compensated FP32 (err<=1e-6 vs FP64)"
+METRIC = "Ginteractions/s @N=1M, compensated vs plain fp32 @err\u22641e-6 vs fp64; adjoint/fwd"
 UNIT = "Ginteractions/s"
 FLOPS_PER_PAIR = 19        # flopsu_0v_0b for the exponential core (src/Kernels.h:79 + src/CoreFunc.h:145)
 FMA_PER_CLK_PER_SM = 128   # FP32 lanes per SM per clock
@@ -50,6 +50,76 @@ def make_workload(seed=SEED, n=None):
     s = (g / g.sum()).astype(np.float32)
     r = np.full(n, SIGMA, np.float32)
     return x, y, r, s
+
+
+ADJ_NS = 500_000          # differentiation workload: sources uniform in [-1,1]^2, core 0.01, Gaussian
+ADJ_GRID = 100            # probes on a 100 x 100 grid over [-0.5,0.5]^2; loss = sum |u_probe|^2
+
+
+def make_adjoint_workload(seed=4):
+    rng = np.random.default_rng(seed)
+    sx, sy = rng.uniform(-1.0, 1.0, (2, ADJ_NS)).astype(np.float32)
+    ss = rng.normal(0.0, 1.0 / np.sqrt(ADJ_NS), ADJ_NS).astype(np.float32)
+    sr = np.full(ADJ_NS, 0.01, np.float32)
+    g = np.linspace(-0.5, 0.5, ADJ_GRID, dtype=np.float32)
+    px, py = [a.ravel().astype(np.float32) for a in np.meshgrid(g, g)]
+    return sx, sy, sr, ss, px, py
+
+
+def time_adjoint(og, torch, ctx, stream, dev, flush, steps, warmup):
+    """Forward (finalized probe velocities) and hand-written backward (dL/d source x, y, G of
+    L = sum u^2 + v^2 over the probes), both compensated, device-resident inputs, CUDA events on
+    the launching stream, L2 flushed before each timed call.  Returns timings, the backward's
+    launch count and, for the precision check, the host arrays and the device results."""
+    sx, sy, sr, ss, px, py = make_adjoint_workload()
+    SX, SY, SR, SS, PX, PY = [torch.from_numpy(a).to(dev) for a in (sx, sy, sr, ss, px, py)]
+    npb = px.size
+    PU = torch.zeros(npb, device=dev)
+    PV = torch.zeros(npb, device=dev)
+    GX, GY, GS = [torch.zeros(ADJ_NS, device=dev) for _ in range(3)]
+
+    def fwd():
+        PU.zero_()
+        PV.zero_()
+        og.points_affect_points_dev(ctx, og.CORE_GAUSSIAN, og.VELONLY, og.COMPENSATED, SX, SY, SR, SS, PX, PY, None,
+                                    PU, PV, finalize=True)
+
+    def bwd():
+        GX.zero_()
+        GY.zero_()
+        GS.zero_()
+        og.points_affect_points_vjp_dev(ctx, og.CORE_GAUSSIAN, og.COMPENSATED, SX, SY, SR, SS, PX, PY, None,
+                                        2.0 * PU, 2.0 * PV, GX, GY, GS)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        l0 = ctx.launches
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        ctx.synchronize()
+        return tot / steps, ctx.launches - l0
+
+    f_ms, f_l = timed(fwd)
+    fwd()
+    b_ms, b_l = timed(bwd)
+    pairs = float(ADJ_NS) * npb
+    res = {"workload": f"{ADJ_NS} sources U[-1,1]^2, core 0.01, Gaussian; {npb} probes on a "
+                       f"{ADJ_GRID}x{ADJ_GRID} grid over [-0.5,0.5]^2; loss sum |u|^2 (no freestream)",
+           "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+           "forward_ginter_s": pairs / (f_ms * 1e-3) / 1e9, "backward_ginter_s": pairs / (b_ms * 1e-3) / 1e9}
+    host = (sx, sy, sr, ss, px, py, PU.cpu().numpy(), PV.cpu().numpy(), GX.cpu().numpy(), GY.cpu().numpy(),
+            GS.cpu().numpy())
+    return res, f_l + b_l, host
 
 
 def dist_env():
@@ -236,6 +306,7 @@ def run_engine(args):
     with ClockSampler(local) as clk:
         ms_comp, main_comp, launches = timed(og.COMPENSATED, args.steps, args.warmup)
         ms_plain, main_plain, _ = timed(og.PLAIN_F32, max(1, args.steps // 2), 1)
+        adjoint, adj_launches, adj_host = time_adjoint(og, torch, ctx, stream, dev, flush, args.steps, args.warmup)
     clocks = clk.summary()
 
     # end to end through the host-pointer C ABI call (copies in the timed region)
@@ -274,6 +345,15 @@ def run_engine(args):
         got = np.concatenate([TU.cpu().numpy()[sub], TV.cpu().numpy()[sub]])
         mx, rms = rel_errs(ref64, got)
         prec[name] = {"max_rel": mx, "rms_rel": rms}
+    # backward precision: the FP64 reference adjoint for 1024 seeded sources, with the same
+    # cotangents (twice the engine's probe velocities)
+    asx, asy, asr, ass, apx, apy, apu, apv, agx, agy, ags = adj_host
+    asub = np.random.default_rng(4321).choice(ADJ_NS, 1024, replace=False)
+    rx, ry, rs = orc.probe_vjp(po.GAUSS, asx[asub], asy[asub], asr[asub], ass[asub], apx, apy, 2.0 * apu, 2.0 * apv)
+    adjoint["precision"] = {"subset_sources": 1024}
+    for nm, ref, got in (("dL/dx", rx, agx[asub]), ("dL/dy", ry, agy[asub]), ("dL/dG", rs, ags[asub])):
+        mx, rms = rel_errs(ref, got)
+        adjoint["precision"][nm] = {"max_rel": mx, "rms_rel": rms}
 
     # CPU baseline: the reference's CPU path on a bounded sample, all host cores
     threads = os.cpu_count() or 1
@@ -299,13 +379,16 @@ def run_engine(args):
                 "ms_per_step": float(np.mean(e2e_ms))},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "kernel": "p2p_kernel<GAUSS,thick,VEL,compensated>",
+                     "kernel": "p2p_packed_kernel<GAUSS,thick,compensated,2> (Morton-ordered targets and sources)",
                      "flops_per_interaction": FLOPS_PER_PAIR,
+                     "flops_note": "the reference's count for the Gaussian thick-target velocity kernel; far "
+                                   "(warp, block) pairs execute 7 FP32 lane-ops + 1 MUFU.RCP per interaction",
                      "peak_note": f"2 x {FMA_PER_CLK_PER_SM} FP32 lanes x {nsm} SMs x {sm_max:.0f} MHz (max SM clock of measured)",
                      "frac_at_median_clock": (achieved / (fp32_peak * clocks["sm_mhz"] / sm_max)) if clocks.get("sm_mhz") else None,
                      "main_kernel_ms": main_comp},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": f"{args.cpu_sample} seeded targets x {N} sources"},
+        "adjoint": adjoint,
         "gpu_launches": launches,
         "clocks": clocks,
     }

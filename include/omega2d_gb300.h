@@ -98,6 +98,11 @@ int obs_set_kernel_variant(obs_context* ctx, int variant);
 #define OBS_ORDER_BINNED 2
 #define OBS_ORDER_BINNED_TARGETS 3
 int obs_set_target_order(obs_context* ctx, int order);
+/* The spatial order used above, as a utility on device arrays: perm[k] (device, n ints) is the
+ * index of the k-th point after a stable sort by the Morton key of its cell in a 256 x 256 grid
+ * over the points' bounding box (cell = min(255, floor((v - min) * (256 / (max - min))))).
+ * Asynchronous on the context's stream. */
+int obs_morton_order_dev(obs_context* ctx, int n, const float* x, const float* y, int* perm);
 /* Number of engine kernel launches issued by this context since creation. */
 long long obs_launch_count(obs_context* ctx);
 const char* obs_status_string(int status);

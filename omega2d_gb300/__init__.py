@@ -301,6 +301,15 @@ def points_affect_points_dev(ctx: Context, core: int, result: int, accum: int, s
     return flops.value
 
 
+def morton_order_dev(ctx: Context, x, y, perm):
+    """Stable Morton-cell order of n points (CUDA tensors x, y; int32 tensor perm receives it)."""
+    n = x.numel()
+    if y.numel() < n or perm.numel() < n:
+        raise ValueError("y and perm need at least x.numel() elements")
+    _check(lib().obs_morton_order_dev(ctx.handle, ctypes.c_int(n), _ptr(x), _ptr(y), _ptr(perm)),
+           "obs_morton_order_dev")
+
+
 def flops_per_pair(core: int, result: int = VELONLY, thick: bool = True) -> int:
     return int(lib().obs_flops_per_pair(ctypes.c_int(core), ctypes.c_int(result), ctypes.c_int(1 if thick else 0)))
 

@@ -385,6 +385,7 @@ __global__ void pa_reduce_kernel(const PAArgs a) {
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     double s = 0.0;
+#pragma unroll 8
     for (int k = 0; k < a.nsplit; ++k) s += a.part[((size_t)q * a.nsplit + k) * a.no + i];
     c[q] = s;
   }

@@ -6,8 +6,9 @@
 // exponential.  This file produces that order:
 //   1. bounding box of the points (order-preserving float keys, atomic max);
 //   2. 16-bit Morton key of each point's cell in a 256 x 256 grid over the box;
-//   3. stable LSD radix sort of (key, index) in two 8-bit passes: per-tile digit counts, one
-//      exclusive scan over the [digit][tile] table, and a stable scatter whose in-tile ranks
+//   3. stable LSD radix sort of (key, index) in two 8-bit passes: per-tile digit counts (and
+//      digit totals), per-digit offsets over the tiles (one warp per digit), and a stable
+//      scatter whose in-tile ranks
 //      come from warp match + per-warp digit counts, so the order is a function of the input
 //      alone (points of one cell keep the caller's relative order);
 //   4. optional gather of x, y, r, g into the sorted order.
@@ -21,9 +22,10 @@ namespace {
 
 constexpr int BIN_BITS = 8;                       // cells per axis: 256
 constexpr int RS_THREADS = 256;                   // = number of digits per pass
-constexpr int RS_CHUNKS = 16;
+constexpr int RS_CHUNKS = 4;
 constexpr int RS_TILE = RS_THREADS * RS_CHUNKS;   // points per radix tile
 constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int HDR_BYTES = 4096;                   // bb | digit totals of pass 1 | of pass 2
 
 // order-preserving map of a float to an unsigned key (and back)
 __device__ __forceinline__ unsigned ord_key(float f) {
@@ -34,24 +36,28 @@ __device__ __forceinline__ float ord_val(unsigned k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// bb[0] = ~min key x, bb[1] = max key x, bb[2] = ~min key y, bb[3] = max key y (zeroed first)
-__global__ void bin_bbox_kernel(const float* __restrict__ x, const float* __restrict__ y, int n,
-                                unsigned* __restrict__ bb) {
-  unsigned nx0 = 0, x1 = 0, ny0 = 0, y1 = 0;
+// bb[0] = ~min key x, bb[1] = max key x, bb[2] = ~min key y, bb[3] = max key y (zeroed first);
+// one set of atomics per block
+__global__ void __launch_bounds__(256) bin_bbox_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                                       int n, unsigned* __restrict__ bb) {
+  __shared__ unsigned red[4][8];
+  unsigned v[4] = {0u, 0u, 0u, 0u};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const unsigned kx = ord_key(x[i]), ky = ord_key(y[i]);
-    nx0 = max(nx0, ~kx); x1 = max(x1, kx);
-    ny0 = max(ny0, ~ky); y1 = max(y1, ky);
+    v[0] = max(v[0], ~kx); v[1] = max(v[1], kx);
+    v[2] = max(v[2], ~ky); v[3] = max(v[3], ky);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    nx0 = max(nx0, __shfl_xor_sync(0xffffffffu, nx0, o));
-    x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-    ny0 = max(ny0, __shfl_xor_sync(0xffffffffu, ny0, o));
-    y1 = max(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    for (int o = 16; o > 0; o >>= 1) v[c] = max(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
+    if (lane == 0) red[c][w] = v[c];
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&bb[0], nx0); atomicMax(&bb[1], x1);
-    atomicMax(&bb[2], ny0); atomicMax(&bb[3], y1);
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    unsigned m = 0u;
+    for (int q = 0; q < 8; ++q) m = max(m, red[threadIdx.x][q]);
+    atomicMax(&bb[threadIdx.x], m);
   }
 }
 
@@ -79,51 +85,46 @@ __global__ void bin_key_kernel(const float* __restrict__ x, const float* __restr
   keys[i] = spread8(cell_of(x[i], x0, sx)) | (spread8(cell_of(y[i], y0, sy)) << 1);
 }
 
-// digit counts of one tile: table[digit * ntiles + tile]
+// digit counts of one tile: table[digit * ntiles + tile]; digit totals into tot[256] (zeroed)
 __global__ void __launch_bounds__(RS_THREADS) rs_count_kernel(const unsigned* __restrict__ keys, int n, int shift,
-                                                             unsigned* __restrict__ table, int ntiles) {
+                                                             unsigned* __restrict__ table, int ntiles,
+                                                             unsigned* __restrict__ tot) {
   __shared__ unsigned cnt[RS_THREADS];
   cnt[threadIdx.x] = 0;
   __syncthreads();
   const int base = blockIdx.x * RS_TILE;
+#pragma unroll
   for (int k = 0; k < RS_CHUNKS; ++k) {
     const int i = base + k * RS_THREADS + threadIdx.x;
     if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
   }
   __syncthreads();
-  table[(size_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+  const unsigned c = cnt[threadIdx.x];
+  table[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
+  if (c) atomicAdd(&tot[threadIdx.x], c);
 }
 
-// exclusive prefix sum of m counts, in place; one block of 1024 threads, each a contiguous run
-__global__ void __launch_bounds__(1024) rs_scan_kernel(unsigned* __restrict__ v, int m) {
-  __shared__ unsigned wsum[32];
-  const int t = threadIdx.x;
-  const int per = (m + 1023) / 1024;
-  const int lo = min(m, t * per), hi = min(m, lo + per);
-  unsigned s = 0;
-  for (int k = lo; k < hi; ++k) s += v[k];
-  unsigned incl = s;
-  const int lane = t & 31, w = t >> 5;
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned q = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += q;
-  }
-  if (lane == 31) wsum[w] = incl;
-  __syncthreads();
-  if (w == 0) {
-    unsigned x = wsum[lane];
+// exclusive offsets in place: table[d][t] <- sum of all counts of digits < d + counts of digit d
+// in tiles < t.  One warp per digit; the row is scanned 32 tiles at a time (coalesced).
+__global__ void __launch_bounds__(256) rs_offsets_kernel(unsigned* __restrict__ table, int ntiles,
+                                                         const unsigned* __restrict__ tot) {
+  const int lane = threadIdx.x & 31;
+  const int d = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (d >= RS_THREADS) return;
+  unsigned base = 0;
+  for (int q = lane; q < d; q += 32) base += tot[q];
+  for (int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(0xffffffffu, base, o);
+  unsigned* row = table + (size_t)d * ntiles;
+  for (int t0 = 0; t0 < ntiles; t0 += 32) {
+    const int t = t0 + lane;
+    const unsigned c = (t < ntiles) ? row[t] : 0u;
+    unsigned incl = c;
     for (int o = 1; o < 32; o <<= 1) {
-      const unsigned q = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += q;
+      const unsigned q = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += q;
     }
-    wsum[lane] = x;
-  }
-  __syncthreads();
-  unsigned run = incl - s + (w ? wsum[w - 1] : 0u);
-  for (int k = lo; k < hi; ++k) {
-    const unsigned c = v[k];
-    v[k] = run;
-    run += c;
+    if (t < ntiles) row[t] = base + incl - c;
+    base += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 
@@ -188,10 +189,10 @@ size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
 
-// scratch: bb (256 bytes) | table[256][ntiles] | keys A | keys B | payload B
+// scratch: header (bb, digit totals) | table[256][ntiles] | keys A | keys B | payload B
 size_t bin_scratch_bytes(int n) {
   const size_t ntiles = ((size_t)n + RS_TILE - 1) / RS_TILE;
-  return 256 + al256(RS_THREADS * ntiles * sizeof(unsigned)) + 3 * al256((size_t)n * sizeof(unsigned));
+  return HDR_BYTES + al256(RS_THREADS * ntiles * sizeof(unsigned)) + 3 * al256((size_t)n * sizeof(unsigned));
 }
 
 cudaError_t bin_order(const float* x, const float* y, int n, void* scratch, int* perm, cudaStream_t st,
@@ -200,24 +201,25 @@ cudaError_t bin_order(const float* x, const float* y, int n, void* scratch, int*
   const int ntiles = (n + RS_TILE - 1) / RS_TILE;
   char* p = static_cast<char*>(scratch);
   unsigned* bb = reinterpret_cast<unsigned*>(p);
-  unsigned* table = reinterpret_cast<unsigned*>(p + 256);
-  unsigned* ka = reinterpret_cast<unsigned*>(p + 256 + al256(RS_THREADS * (size_t)ntiles * sizeof(unsigned)));
+  unsigned* tot0 = reinterpret_cast<unsigned*>(p + 256);
+  unsigned* tot1 = tot0 + RS_THREADS;
+  unsigned* table = reinterpret_cast<unsigned*>(p + HDR_BYTES);
+  unsigned* ka = reinterpret_cast<unsigned*>(p + HDR_BYTES + al256(RS_THREADS * (size_t)ntiles * sizeof(unsigned)));
   unsigned* kb = ka + al256((size_t)n * sizeof(unsigned)) / sizeof(unsigned);
   int* vb = reinterpret_cast<int*>(kb + al256((size_t)n * sizeof(unsigned)) / sizeof(unsigned));
-  cudaError_t e = cudaMemsetAsync(bb, 0, 4 * sizeof(unsigned), st);
+  cudaError_t e = cudaMemsetAsync(p, 0, HDR_BYTES, st);
   if (e != cudaSuccess) return e;
   const int threads = 256;
   const int blocks = (n + threads - 1) / threads;
-  bin_bbox_kernel<<<blocks < 1024 ? blocks : 1024, threads, 0, st>>>(x, y, n, bb);
+  bin_bbox_kernel<<<blocks < 512 ? blocks : 512, threads, 0, st>>>(x, y, n, bb);
   bin_key_kernel<<<blocks, threads, 0, st>>>(x, y, n, bb, ka);
-  const int m = RS_THREADS * ntiles;
   // pass 1: low digit, identity payload, (ka) -> (kb, vb)
-  rs_count_kernel<<<ntiles, RS_THREADS, 0, st>>>(ka, n, 0, table, ntiles);
-  rs_scan_kernel<<<1, 1024, 0, st>>>(table, m);
+  rs_count_kernel<<<ntiles, RS_THREADS, 0, st>>>(ka, n, 0, table, ntiles, tot0);
+  rs_offsets_kernel<<<RS_THREADS / 8, 256, 0, st>>>(table, ntiles, tot0);
   rs_scatter_kernel<<<ntiles, RS_THREADS, 0, st>>>(ka, nullptr, n, 0, table, ntiles, kb, vb);
   // pass 2: high digit, (kb, vb) -> (ka, perm)
-  rs_count_kernel<<<ntiles, RS_THREADS, 0, st>>>(kb, n, BIN_BITS, table, ntiles);
-  rs_scan_kernel<<<1, 1024, 0, st>>>(table, m);
+  rs_count_kernel<<<ntiles, RS_THREADS, 0, st>>>(kb, n, BIN_BITS, table, ntiles, tot1);
+  rs_offsets_kernel<<<RS_THREADS / 8, 256, 0, st>>>(table, ntiles, tot1);
   rs_scatter_kernel<<<ntiles, RS_THREADS, 0, st>>>(kb, vb, n, BIN_BITS, table, ntiles, ka, perm);
   if (launches) *launches += 8;
   return cudaGetLastError();

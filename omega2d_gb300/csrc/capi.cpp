@@ -246,6 +246,19 @@ int obs_set_target_order(obs_context* ctx, int order) {
   return OBS_OK;
 }
 
+int obs_morton_order_dev(obs_context* ctx, int n, const float* x, const float* y, int* perm) {
+  if (!ctx || n < 0 || (n > 0 && (!x || !y || !perm))) return OBS_ERR_ARG;
+  if (n == 0) return OBS_OK;
+  int s = bind(ctx);
+  if (s) return s;
+  s = ctx->work.ensure(obs::bin_scratch_bytes(n), ctx->stream);
+  if (s) return s;
+  int nl = 0;
+  s = cuda_status(obs::bin_order(x, y, n, ctx->work.p, perm, ctx->stream, &nl));
+  ctx->launches += nl;
+  return s;
+}
+
 long long obs_launch_count(obs_context* ctx) {
   return ctx ? ctx->launches : -1;
 }

@@ -274,11 +274,13 @@ __global__ void p2p_reduce_kernel(const P2PArgs a) {
     if (COMP) {
       const double* p = static_cast<const double*>(a.part) + (size_t)q * a.nsplit * a.nt + i;
       double s = 0.0;
+#pragma unroll 8
       for (int k = 0; k < a.nsplit; ++k) s += p[(size_t)k * a.nt];
       c[q] = s;
     } else {
       const float* p = static_cast<const float*>(a.part) + (size_t)q * a.nsplit * a.nt + i;
       float s = 0.0f;
+#pragma unroll 8
       for (int k = 0; k < a.nsplit; ++k) s += p[(size_t)k * a.nt];
       c[q] = (double)s;
     }

@@ -164,3 +164,45 @@ def test_binned_self_interaction_shared_order(ctx, accum):
         ctx.set_target_order(og.ORDER_AUTO)
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
     assert np.isfinite(outs[0][0]).all()
+
+
+def _morton_ref(x, y):
+    """Host restatement of the engine's order: float32 cell arithmetic, stable sort."""
+    x = np.asarray(x, np.float32)
+    y = np.asarray(y, np.float32)
+
+    def cells(v):
+        lo, hi = v.min(), v.max()
+        w = np.float32(hi - lo)
+        sc = np.float32(256.0) / w if w > 0 else np.float32(0.0)
+        c = np.minimum(np.maximum((v - lo) * sc, np.float32(0.0)), np.float32(255.0))
+        return c.astype(np.uint32)
+
+    def spread(v):
+        v = (v | (v << 4)) & 0x0F0F
+        v = (v | (v << 2)) & 0x3333
+        return (v | (v << 1)) & 0x5555
+
+    key = spread(cells(x)) | (spread(cells(y)) << 1)
+    return np.argsort(key, kind="stable")
+
+
+@pytest.mark.parametrize("n,dist", [(1, "u"), (1000, "u"), (300_001, "n"), (65536, "line"), (5000, "dup")])
+def test_morton_order_matches_host_stable_sort(ctx, n, dist):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(n)
+    if dist == "u":
+        x, y = rng.uniform(-1, 1, (2, n)).astype(np.float32)
+    elif dist == "n":
+        x, y = rng.normal(0, 0.25, (2, n)).astype(np.float32)
+    elif dist == "line":
+        x = np.linspace(-3, 5, n).astype(np.float32)
+        y = np.full(n, 0.5, np.float32)
+    else:
+        x, y = rng.integers(0, 4, (2, n)).astype(np.float32)       # many equal keys: stability
+    dev = torch.device("cuda", 0)
+    X, Y = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+    P = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    og.morton_order_dev(ctx, X, Y, P)
+    ctx.synchronize()
+    assert np.array_equal(P.cpu().numpy(), _morton_ref(x, y))
