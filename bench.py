@@ -397,6 +397,263 @@ def run_engine(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------- the other configurations
+# `--workload` runs one of them instead of the headline line; each prints one JSON line with
+# its own metric, CUDA-event timings on the launching stream (L2 flushed between timed
+# calls), a precision check against the FP64 oracle where one fits in seconds, and the CPU
+# restatement timed on the host cores.
+
+def _engine_setup():
+    import torch
+    import omega2d_gb300 as og
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ctx = og.Context(0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    return torch, og, dev, ctx, stream, flush
+
+
+def _event_time(torch, stream, flush, fn, steps, warmup, prep=None):
+    """Mean milliseconds of fn() over `steps` timed calls after `warmup` untimed ones; prep()
+    (untimed) runs before every call."""
+    for _ in range(warmup):
+        if prep:
+            prep()
+        fn()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        if prep:
+            prep()
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        tot += e0.elapsed_time(e1)
+    return tot / steps
+
+
+def run_euler20k(args):
+    """20,000 vortex blobs U[-1,1]^2, G ~ N(0, 1/N), core 0.01, Rosenhead-Moore, freestream
+    (1, 0): one velocity evaluation, then 10 first-order Euler steps with dt = 0.01."""
+    torch, og, dev, ctx, stream, flush = _engine_setup()
+    n, K, dt, fs = 20_000, 10, 0.01, (1.0, 0.0)
+    rng = np.random.default_rng(1)
+    x, y = rng.uniform(-1.0, 1.0, (2, n)).astype(np.float32)
+    s = rng.normal(0.0, 1.0 / np.sqrt(n), n).astype(np.float32)
+    r = np.full(n, 0.01, np.float32)
+    X0, Y0, R, S = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
+    X, Y = X0.clone(), Y0.clone()
+    U, V = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    out = {"workload": "euler20k", "metric": "Ginteractions/s, RM core, 20k particles, 10 Euler steps",
+           "unit": UNIT, "data": "synthetic (seed 1)", "n": n, "steps_per_run": K}
+    with ClockSampler(0) as clk:
+        for name, accum in (("compensated", og.COMPENSATED), ("plain", og.PLAIN_F32)):
+            def vel():
+                U.zero_()
+                V.zero_()
+                og.points_affect_points_dev(ctx, og.CORE_RM, og.VELONLY, accum, X0, Y0, R, S, X0, Y0, R, U, V,
+                                            finalize=True, fs=fs)
+
+            def reset():
+                X.copy_(X0)
+                Y.copy_(Y0)
+
+            def euler():
+                og.advect_dev(ctx, og.CORE_RM, accum, 1, X, Y, R, S, fs, dt, K)
+            tv = _event_time(torch, stream, flush, vel, args.steps, args.warmup)
+            te = _event_time(torch, stream, flush, euler, args.steps, args.warmup, prep=reset)
+            ctx.synchronize()
+            out[name] = {"velocity_ms": tv, "velocity_ginter_s": n * n / (tv * 1e-3) / 1e9,
+                         "euler10_ms": te, "value": K * n * n / (te * 1e-3) / 1e9,
+                         "final_x": X.cpu().numpy().astype(np.float64), "final_y": Y.cpu().numpy().astype(np.float64)}
+    out["clocks"] = clk.summary()
+    out["value"] = out["compensated"]["value"]
+    # FP64 oracle trajectories and the CPU restatement (float pairs, double sums, all cores)
+    from oracle import pyoracle as po
+    orc = po.Restatement()
+    x64, y64 = orc.advect(1, po.RM, x, y, r, s, fs, dt, K, fp64=True)
+    disp = float(np.max(np.hypot(x64 - x, y64 - y)))
+    for name in ("compensated", "plain"):
+        ex = np.hypot(out[name].pop("final_x") - x64, out[name].pop("final_y") - y64)
+        out[name]["position_error_max_over_displacement"] = float(ex.max() / disp)
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    orc.advect(1, po.RM, x, y, r, s, fs, dt, K)
+    tc = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": K * n * n / tc / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": "the full workload (10 Euler steps of 20k particles)"}
+    print(json.dumps(out), flush=True)
+
+
+def run_bem2048(args):
+    """Unit-diameter circle of 2048 panels and 200,000 particles uniform in the annulus
+    0.55 < r < 3 (G ~ N(0, 1e-4)): particles-on-panels (RHS), the 4096 x 4096 panels-on-panels
+    matrix in FP64, its FP64 LU solve, and panels-on-particles velocity, all on the device."""
+    torch, og, dev, ctx, stream, flush = _engine_setup()
+    npan, npart = 2048, 200_000
+    rng = np.random.default_rng(3)
+    rad = np.sqrt(rng.uniform(0.55 ** 2, 3.0 ** 2, npart))
+    th = rng.uniform(0.0, 2.0 * np.pi, npart)
+    px, py = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    ps = rng.normal(0.0, 1e-2, npart).astype(np.float32)
+    bd = og.circle_panels(npan)
+    NX, NY = torch.from_numpy(bd.nx).to(dev), torch.from_numpy(bd.ny).to(dev)
+    IDX = torch.from_numpy(bd.idx.astype(np.int32)).to(dev)
+    PX, PY, PS = [torch.from_numpy(a).to(dev) for a in (px, py, ps)]
+    nunk, m = 2, 2 * npan
+    PU, PV = torch.zeros(npan, device=dev), torch.zeros(npan, device=dev)
+    RHS = torch.zeros(m, dtype=torch.float64, device=dev)
+    A = torch.zeros(m * m, dtype=torch.float64, device=dev)
+    SOL = torch.zeros(m, dtype=torch.float64, device=dev)
+    TU, TV = torch.zeros(npart, device=dev), torch.zeros(npart, device=dev)
+    acc = og.COMPENSATED
+    box = {}
+
+    def d3():
+        PU.zero_()
+        PV.zero_()
+        og.points_affect_panels_dev(ctx, acc, PX, PY, PS, NX, NY, IDX, PU, PV, finalize=True)
+
+    def b2():
+        og.vels_to_rhs_panels_dev(ctx, nunk, NX, NY, IDX, PU, PV, None, None, RHS)
+
+    def b1():
+        og.panels_on_panels_coeff_dev(ctx, nunk, NX, NY, IDX, None, A)
+
+    def solve():
+        box["rel"] = og.solve_dense_f64_dev(ctx, A, RHS, SOL)
+
+    def d2():
+        TU.zero_()
+        TV.zero_()
+        vs = SOL[0::2].float()
+        ss = SOL[1::2].float()
+        og.panels_affect_points_dev(ctx, acc, NX, NY, IDX, vs, ss, PX, PY, TU, TV)
+
+    def pipeline():
+        d3(); b2(); b1(); solve(); d2()
+    out = {"workload": "bem2048", "metric": "ms per BEM coupling step (2048 panels, 200k particles)",
+           "unit": "ms", "higher_is_better": False, "data": "synthetic (seed 3)", "unknowns": m}
+    with ClockSampler(0) as clk:
+        times = {k: _event_time(torch, stream, flush, f, args.steps, args.warmup)
+                 for k, f in (("points_affect_panels", d3), ("vels_to_rhs", b2), ("panels_on_panels_coeff_f64", b1),
+                              ("lu_solve_f64", solve), ("panels_affect_points", d2), ("pipeline", pipeline))}
+    ctx.synchronize()
+    out["clocks"] = clk.summary()
+    out["ms"] = times
+    out["value"] = times["pipeline"]
+    out["ginter_s"] = {"points_affect_panels": npart * npan / (times["points_affect_panels"] * 1e-3) / 1e9,
+                       "panels_affect_points": npart * npan / (times["panels_affect_points"] * 1e-3) / 1e9,
+                       "lu_tflops_f64": (2.0 / 3.0) * m ** 3 / (times["lu_solve_f64"] * 1e-3) / 1e12}
+    out["relative_residual"] = box.get("rel")
+    sol = SOL.cpu().numpy()
+    tu, tv = TU.cpu().numpy(), TV.cpu().numpy()
+    # FP64 oracle: the same five steps in FP64 (D2 on a 4096-particle subset)
+    from oracle import pyoracle as po
+    orc = po.Restatement()
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    pu, pv = orc.points_affect_panels(px, py, ps, bd.nx, bd.ny, bd.idx, fp64=True)
+    t_d3 = time.perf_counter() - t0
+    pu, pv = pu / (2 * np.pi), pv / (2 * np.pi)
+    rhs = orc.vels_to_rhs_panels(nunk, bd.nx, bd.ny, bd.idx, pu, pv, fp64=True)
+    t0 = time.perf_counter()
+    A64 = orc.panels_on_panels_coeff(nunk, bd.nx, bd.ny, bd.idx, fp64=True)
+    t_b1 = time.perf_counter() - t0
+    x64 = np.linalg.solve(A64, rhs)
+    sub = np.random.default_rng(33).choice(npart, 4096, replace=False)
+    u64, v64 = orc.panels_affect_points(bd.nx, bd.ny, bd.idx, x64[0::2], x64[1::2], px[sub], py[sub], fp64=True)
+    vel = np.concatenate([u64, v64])
+    out["precision"] = {"strengths_max_rel": float(np.max(np.abs(sol - x64)) / np.max(np.abs(x64))),
+                        "panels_affect_points_subset_max_rel":
+                            float(np.max(np.abs(np.concatenate([tu[sub], tv[sub]]) - vel)) / np.max(np.abs(vel)))}
+    out["cpu_baseline"] = {"kind": "port", "cores": threads,
+                           "points_affect_panels_ginter_s": npart * npan / t_d3 / 1e9,
+                           "panels_on_panels_coeff_ms": 1e3 * t_b1,
+                           "sample": "FP64 restatement of the full particles-on-panels sum and matrix"}
+    print(json.dumps(out), flush=True)
+
+
+def run_rk2adjoint2M(args):
+    """Two co-rotating Gaussian patches of 1M particles each (sigma 0.1, centres (+-0.3, 0),
+    total circulation 1 each), core 0.004, Gaussian; `--rk-steps` Ralston RK2 steps with
+    dt = 0.005; loss L = |X_A - X_B|^2 with X_P = sum_P G^2 x / sum_P G^2; gradient of L with
+    respect to the initial strengths through the trajectory, checkpoints every 8 steps."""
+    torch, og, dev, ctx, stream, flush = _engine_setup()
+    n, K, dt, every = 2_000_000, args.rk_steps, 0.005, 8
+    rng = np.random.default_rng(5)
+    lab = (np.arange(n) % 2).astype(np.int64)
+    cx = np.where(lab == 0, -0.3, 0.3)
+    x = cx + rng.normal(0.0, 0.1, n)
+    y = rng.normal(0.0, 0.1, n)
+    w = np.exp(-((x - cx) ** 2 + y ** 2) / (2 * 0.1 ** 2))
+    s = np.where(lab == 0, w / w[lab == 0].sum(), w / w[lab == 1].sum())
+    x, y, s = x.astype(np.float32), y.astype(np.float32), s.astype(np.float32)
+    r = np.full(n, 0.004, np.float32)
+    X0, Y0, R, S = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
+    X, Y = X0.clone(), Y0.clone()
+    GS, GX, GY = [torch.zeros(n, device=dev) for _ in range(3)]
+    acc = og.COMPENSATED
+    torch.cuda.reset_peak_memory_stats(dev)
+    with ClockSampler(0) as clk:
+        og.advect_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, 1)    # warm-up
+        X.copy_(X0)
+        Y.copy_(Y0)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        og.advect_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, K)
+        e[1].record(stream)
+        e[1].synchronize()
+        # loss and its seed on the host in FP64 (the loss is not part of the engine)
+        xT, yT, s64 = X.cpu().numpy().astype(np.float64), Y.cpu().numpy().astype(np.float64), s.astype(np.float64)
+        gxT, gyT, gs_direct = np.zeros(n), np.zeros(n), np.zeros(n)
+        cen = []
+        for P in (0, 1):
+            m = lab == P
+            w2 = s64[m] ** 2
+            cen.append((np.sum(w2 * xT[m]) / w2.sum(), np.sum(w2 * yT[m]) / w2.sum(), w2.sum()))
+        dX, dY = cen[0][0] - cen[1][0], cen[0][1] - cen[1][1]
+        L = dX * dX + dY * dY
+        for P, sg in ((0, 1.0), (1, -1.0)):
+            m = lab == P
+            W = cen[P][2]
+            gxT[m] = sg * 2 * dX * s64[m] ** 2 / W
+            gyT[m] = sg * 2 * dY * s64[m] ** 2 / W
+            gs_direct[m] = sg * 2 * (dX * (xT[m] - cen[P][0]) + dY * (yT[m] - cen[P][1])) * 2 * s64[m] / W
+        LX = torch.from_numpy(gxT.astype(np.float32)).to(dev)
+        LY = torch.from_numpy(gyT.astype(np.float32)).to(dev)
+        torch.cuda.synchronize()
+        e[2].record(stream)
+        peak = og.advect_vjp_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X0, Y0, R, S, (0.0, 0.0), dt, K, every, LX, LY,
+                                 GS, GX, GY)
+        e[3].record(stream)
+        e[3].synchronize()
+    ctx.synchronize()
+    f_ms, b_ms = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    evals = 2.0 * K * float(n) * float(n)
+    gs = GS.cpu().numpy().astype(np.float64) + gs_direct
+    out = {"workload": "rk2adjoint2M", "metric": "Ginteractions/s forward and adjoint, 2M particles, RK2",
+           "unit": UNIT, "data": "synthetic (seed 5)", "n": n, "rk2_steps": K, "dt": dt, "checkpoint_every": every,
+           "forward_ms": f_ms, "forward_ginter_s": evals / (f_ms * 1e-3) / 1e9,
+           "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+           "adjoint_note": "recomputes the trajectory from checkpoints (2K velocity sums) and runs 2K self VJP gathers",
+           "value": evals / (f_ms * 1e-3) / 1e9, "loss": L, "grad_strength_norm": float(np.linalg.norm(gs)),
+           "grad_strength_finite": bool(np.isfinite(gs).all()),
+           "peak_hbm_bytes": {"engine": int(peak), "caller_tensors": int(torch.cuda.max_memory_allocated(dev))},
+           "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,10 +662,19 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--n", type=int, default=N, help="particles (the headline workload is 1,000,000)")
+    ap.add_argument("--workload", default="patch1M", choices=["patch1M", "euler20k", "bem2048", "rk2adjoint2M"],
+                    help="patch1M is the headline line; the others measure the remaining configurations")
+    ap.add_argument("--rk-steps", type=int, default=64, help="RK2 steps of rk2adjoint2M")
     args = ap.parse_args()
     globals()["N"] = args.n
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "euler20k":
+        run_euler20k(args)
+    elif args.workload == "bem2048":
+        run_bem2048(args)
+    elif args.workload == "rk2adjoint2M":
+        run_rk2adjoint2M(args)
     else:
         run_engine(args)
 

@@ -464,6 +464,53 @@ def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: E
     return rel.value
 
 
+# ---------------------------------------------------------------- device-resident panel calls
+# All arrays are CUDA tensors (node coordinates float32, idx int32/uint32 pairs); asynchronous
+# on the context's stream, same semantics as the host calls above.
+
+def points_affect_panels_dev(ctx: Context, accum: int, sx, sy, ss, nx, ny, idx, pu, pv, finalize=False,
+                             fs=(0.0, 0.0)):
+    _check(lib().obs_points_affect_panels_dev(ctx.handle, ctypes.c_int(accum),
+                                              ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                              ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                                              ctypes.c_int(sx.numel()), _ptr(sx), _ptr(sy), _ptr(ss),
+                                              ctypes.c_int(nx.numel()), _ptr(nx), _ptr(ny),
+                                              ctypes.c_int(idx.numel() // 2), _ptr(idx), _ptr(pu), _ptr(pv)),
+           "obs_points_affect_panels_dev")
+
+
+def panels_affect_points_dev(ctx: Context, accum: int, nx, ny, idx, vs, ss, tx, ty, tu, tv, finalize=False,
+                             fs=(0.0, 0.0)):
+    _check(lib().obs_panels_affect_points_dev(ctx.handle, ctypes.c_int(accum),
+                                              ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                              ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                                              ctypes.c_int(nx.numel()), _ptr(nx), _ptr(ny),
+                                              ctypes.c_int(idx.numel() // 2), _ptr(idx), _ptr(vs), _ptr(ss),
+                                              ctypes.c_int(tx.numel()), _ptr(tx), _ptr(ty), _ptr(tu), _ptr(tv)),
+           "obs_panels_affect_points_dev")
+
+
+def panels_on_panels_coeff_dev(ctx: Context, nunk: int, nx, ny, idx, A32=None, A64=None):
+    """Self block of one body into device buffers (column-major, (nunk*npan)^2 elements)."""
+    geo = (ctypes.c_int(nx.numel()), _ptr(nx), _ptr(ny), ctypes.c_int(idx.numel() // 2), _ptr(idx))
+    _check(lib().obs_panels_on_panels_coeff_dev(ctx.handle, ctypes.c_int(nunk), ctypes.c_int(1), *geo, *geo,
+                                                _ptr(A32), _ptr(A64)), "obs_panels_on_panels_coeff_dev")
+
+
+def vels_to_rhs_panels_dev(ctx: Context, nunk: int, nx, ny, idx, pu, pv, bcn=None, rhs32=None, rhs64=None):
+    _check(lib().obs_vels_to_rhs_panels_dev(ctx.handle, ctypes.c_int(nunk), ctypes.c_int(nx.numel()), _ptr(nx),
+                                            _ptr(ny), ctypes.c_int(idx.numel() // 2), _ptr(idx), _ptr(pu), _ptr(pv),
+                                            _ptr(bcn), _ptr(rhs32), _ptr(rhs64)), "obs_vels_to_rhs_panels_dev")
+
+
+def solve_dense_f64_dev(ctx: Context, A, b, x) -> float:
+    """FP64 LU solve on device arrays (A column-major n x n); returns ||A x - b|| / ||b||."""
+    rel = ctypes.c_double()
+    _check(lib().obs_solve_dense_f64_dev(ctx.handle, ctypes.c_int(b.numel()), _ptr(A), _ptr(b), _ptr(x),
+                                         ctypes.byref(rel)), "obs_solve_dense_f64_dev")
+    return rel.value
+
+
 # ---------------------------------------------------------------- reverse mode and time stepping
 
 def points_affect_points_vjp(src: Points, targ: Points, lu, lv, env: ExecEnv | None = None,
