@@ -122,6 +122,22 @@ def time_adjoint(og, torch, ctx, stream, dev, flush, steps, warmup):
     return res, f_l + b_l, host
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest of one float over all ranks (the identity on one process)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, world_size: int, max_ms: float) -> float:
+    """Whole-job throughput in G-units/s: every rank's units over the slowest rank's time."""
+    return world_size * units_per_rank / (max_ms * 1e-3) / 1e9
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -297,10 +313,8 @@ def run_engine(args):
         ctx.synchronize()
         launches = ctx.launches - launches0
         if ws > 1:
-            t = torch.tensor([tot], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot = max_over_ranks(tot, dev)
             torch.distributed.barrier()
-            tot = float(t.item())
         return tot / steps, main / steps, launches
 
     with ClockSampler(local) as clk:
@@ -323,9 +337,9 @@ def run_engine(args):
     h2d = 4 * N * 4 + 3 * N * 4 + 2 * N * 4
     d2h = 2 * N * 4
 
-    value = ws * pairs / (ms_comp * 1e-3) / 1e9
-    plain_value = ws * pairs / (ms_plain * 1e-3) / 1e9
-    e2e_value = ws * pairs / (np.mean(e2e_ms) * 1e-3) / 1e9
+    value = aggregate_rate(pairs, ws, ms_comp)
+    plain_value = aggregate_rate(pairs, ws, ms_plain)
+    e2e_value = aggregate_rate(pairs, ws, max_over_ranks(float(np.mean(e2e_ms)), dev))
 
     if rank != 0:
         if ws > 1:
