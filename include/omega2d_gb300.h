@@ -133,6 +133,17 @@ int obs_points_affect_points_dev(obs_context* ctx, int core, int result, int acc
                                  float* extra0, float* extra1, float* extra2, float* extra3,
                                  double* flops);
 
+/* points_affect_points_vorticity -- replaces src/InfluenceVort.h:47-126 (the non-Vc branch):
+ * Gaussian-blob vorticity at field points, tw += sum 2 G exp(-d^2/s^2) / s^2 with s the source
+ * core radius (no cut-off, as in that branch).  OBS_FLAG_FINALIZE scales tw by 1/(2 pi) like
+ * finalize_vels does (src/ElementBase.h:215-234). */
+int obs_points_affect_points_vorticity(obs_context* ctx, int accum, int flags,
+                                       int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                       int nt, const float* tx, const float* ty, float* tw);
+int obs_points_affect_points_vorticity_dev(obs_context* ctx, int accum, int flags,
+                                           int ns, const float* sx, const float* sy, const float* sr,
+                                           const float* ss, int nt, const float* tx, const float* ty, float* tw);
+
 /*
  * Panels: straight constant-strength panels given as node coordinates (nx, ny; nnodes) and
  * node-index pairs (idx[2*k], idx[2*k+1]) for panel k, like Surfaces (src/Surfaces.h:682-724).
@@ -151,6 +162,23 @@ int obs_panels_affect_points_dev(obs_context* ctx, int accum, int flags, double 
                                  int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
                                  const float* vs, const float* ss,
                                  int nt, const float* tx, const float* ty, float* tu, float* tv);
+
+/* panels_affect_panels -- replaces src/Influence.h:774-795: velocities at the target panels'
+ * centres due to the source panels, through the reference's collocation points
+ * (Surfaces::represent_as_particles(1e-4, -1), src/Surfaces.h:830-876: 1 + (int)(len_i /
+ * (1.2 len_0)) points per panel, 1e-4 off the panel into the fluid; the first tnp point
+ * velocities are added to the tnp panels, index by index, as the reference does).
+ * Accumulates (unscaled) into pu, pv. */
+int obs_panels_affect_panels(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                             const float* vs, const float* ss,
+                             int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                             float* pu, float* pv);
+int obs_panels_affect_panels_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                                 const float* vs, const float* ss,
+                                 int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                                 float* pu, float* pv);
 
 /* points_affect_panels -- replaces src/Influence.h:633-771: mean velocity over each panel due
  * to point vortices of strength ss (the particle core is not used, as in the reference),
@@ -234,9 +262,14 @@ int obs_points_affect_points_vjp_self_dev(obs_context* ctx, int core, int accum,
                                           const float* y, const float* r, const float* s, const float* lu,
                                           const float* lv, float* gx, float* gy, float* gs);
 
-/* Forward op: nsteps of first-order Euler (order 1) or Ralston RK2 (order 2) convection of the
- * particles by their own velocity plus freestream, in place -- Convection::advect_1st /
- * advect_2nd_ralston without bodies (src/Convection.h:274-466). */
+/* Forward op: nsteps of convection of the particles by their own velocity plus freestream, in
+ * place, without bodies -- Convection::advect_1st (order 1), advect_2nd_ralston (order 2, the
+ * reference's second order), advect_3rd (order 3) and advect_2nd_heun (order 4)
+ * (src/Convection.h:274-598). */
+#define OBS_ADVECT_EULER 1
+#define OBS_ADVECT_RK2_RALSTON 2
+#define OBS_ADVECT_RK3 3
+#define OBS_ADVECT_RK2_HEUN 4
 int obs_advect(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
                const float* s, double fsx, double fsy, double dt, int nsteps);
 int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
@@ -246,6 +279,18 @@ int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, floa
  * (lx, ly), accumulate dL/ds into gs and dL/d(initial x, y) into gx0, gy0.  The trajectory is
  * recomputed per segment from checkpoints every checkpoint_every steps (0: ceil(sqrt(nsteps))).
  * peak_bytes (optional) receives the engine's device-memory footprint (all its buffers). */
+/* Forward op that also records the checkpoints (every checkpoint_every steps; 0: ceil(sqrt
+ * (nsteps))) and copies of r and s in the context, so that obs_advect_vjp_tape_dev can run the
+ * backward without repeating the forward sweep.  One recording per context; the next
+ * recording (or obs_advect_vjp) replaces it. */
+int obs_advect_record_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y,
+                          const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
+                          int checkpoint_every);
+/* Backward op of the recorded forward: dL/d(final x, y) in (lx, ly); accumulates dL/ds into gs
+ * and dL/d(initial x, y) into gx0, gy0 (device arrays; any output may be NULL).  Returns
+ * OBS_ERR_ARG when nothing is recorded. */
+int obs_advect_vjp_tape_dev(obs_context* ctx, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
+                            long long* peak_bytes);
 int obs_advect_vjp(obs_context* ctx, int core, int accum, int order, int n, const float* x0, const float* y0,
                    const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
                    int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,

@@ -279,6 +279,28 @@ def points_affect_points(src: Points, targ: Points, restype: ResultsType | int =
     return flops.value
 
 
+def points_affect_points_vorticity(src: Points, targ: Points, env: ExecEnv | None = None,
+                                   finalize: bool = False) -> None:
+    """points_affect_points_vorticity (src/InfluenceVort.h:47-126): accumulate the Gaussian-blob
+    vorticity of the source particles at the targets (field points) into ``targ.vort``.  The
+    core is always the Gaussian blob; env supplies the context and accumulation mode."""
+    env = env or ExecEnv()
+    if targ.vort is None:
+        targ.vort = np.zeros(targ.n, np.float32)
+    st = lib().obs_points_affect_points_vorticity(
+        env.ctx().handle, ctypes.c_int(env.accum), ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+        ctypes.c_int(src.n), _ptr(src.x), _ptr(src.y), _ptr(src.r), _ptr(src.s),
+        ctypes.c_int(targ.n), _ptr(targ.x), _ptr(targ.y), _ptr(targ.vort))
+    _check(st, "obs_points_affect_points_vorticity")
+
+
+def points_affect_points_vorticity_dev(ctx: Context, accum: int, sx, sy, sr, ss, tx, ty, tw, finalize=False):
+    _check(lib().obs_points_affect_points_vorticity_dev(
+        ctx.handle, ctypes.c_int(accum), ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+        ctypes.c_int(sx.numel()), _ptr(sx), _ptr(sy), _ptr(sr), _ptr(ss),
+        ctypes.c_int(tx.numel()), _ptr(tx), _ptr(ty), _ptr(tw)), "obs_points_affect_points_vorticity_dev")
+
+
 def points_affect_points_dev(ctx: Context, core: int, result: int, accum: int, sx, sy, sr, ss,
                              tx, ty, tr, tu, tv, extra=(None, None, None, None), finalize=False,
                              fs=(0.0, 0.0)) -> float:
@@ -403,6 +425,20 @@ def points_affect_panels(src: Points, targ: Surfaces, env: ExecEnv | None = None
                                         ctypes.c_int(src.n), _ptr(src.x), _ptr(src.y), _ptr(src.s),
                                         *targ._geo(), _ptr(targ.pu), _ptr(targ.pv))
     _check(st, "obs_points_affect_panels")
+
+
+def panels_affect_panels(src: Surfaces, targ: Surfaces, env: ExecEnv | None = None, finalize: bool = False,
+                         fs=(0.0, 0.0)):
+    """panels_affect_panels (src/Influence.h:774-795): accumulate the source panels' influence
+    on the target panels' centre velocities (targ.pu, targ.pv) through the reference's
+    collocation points 1e-4 off the target panels."""
+    env = env or ExecEnv()
+    vs = src.vs if src.vs is not None else np.zeros(src.npan, np.float32)
+    st = lib().obs_panels_affect_panels(env.ctx().handle, ctypes.c_int(env.accum),
+                                        ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                        ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), *src._geo(),
+                                        _ptr(vs), _ptr(src.ss), *targ._geo(), _ptr(targ.pu), _ptr(targ.pv))
+    _check(st, "obs_panels_affect_panels")
 
 
 def panels_on_panels_coeff(src: Surfaces, targ: Surfaces | None = None, nunk: int = 2, fp64: bool = False,
@@ -544,8 +580,8 @@ def points_affect_points_vjp_self(p: Points, lu, lv, env: ExecEnv | None = None)
 
 def advect(p: Points, fs=(0.0, 0.0), dt: float = 0.01, nsteps: int = 1, order: int = 2,
            env: ExecEnv | None = None):
-    """Convection::advect_1st (order 1) / advect_2nd_ralston (order 2) without bodies
-    (src/Convection.h:274-466): moves p.x, p.y in place by nsteps steps."""
+    """Convection::advect_1st (order 1), advect_2nd_ralston (2), advect_3rd (3) or
+    advect_2nd_heun (4) without bodies (src/Convection.h:274-598): moves p.x, p.y in place."""
     env = env or ExecEnv()
     st = lib().obs_advect(env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(env.accum), ctypes.c_int(order),
                           ctypes.c_int(p.n), _ptr(p.x), _ptr(p.y), _ptr(p.r), _ptr(p.s),
@@ -585,6 +621,26 @@ def advect_dev(ctx: Context, core: int, accum: int, order: int, x, y, r, s, fs, 
                               ctypes.c_int(x.numel()), _ptr(x), _ptr(y), _ptr(r), _ptr(s), ctypes.c_double(fs[0]),
                               ctypes.c_double(fs[1]), ctypes.c_double(dt), ctypes.c_int(nsteps))
     _check(st, "obs_advect_dev")
+
+
+ADVECT_EULER, ADVECT_RK2_RALSTON, ADVECT_RK3, ADVECT_RK2_HEUN = 1, 2, 3, 4
+
+
+def advect_record_dev(ctx: Context, core: int, accum: int, order: int, x, y, r, s, fs, dt, nsteps,
+                      checkpoint_every: int = 0):
+    """advect_dev that keeps checkpoints in the context for advect_vjp_tape_dev."""
+    _check(lib().obs_advect_record_dev(ctx.handle, ctypes.c_int(core), ctypes.c_int(accum), ctypes.c_int(order),
+                                       ctypes.c_int(x.numel()), _ptr(x), _ptr(y), _ptr(r), _ptr(s),
+                                       ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(dt),
+                                       ctypes.c_int(nsteps), ctypes.c_int(checkpoint_every)), "obs_advect_record_dev")
+
+
+def advect_vjp_tape_dev(ctx: Context, lx, ly, gs=None, gx0=None, gy0=None) -> int:
+    """Backward of the last advect_record_dev on this context; returns the engine's device bytes."""
+    peak = ctypes.c_longlong()
+    _check(lib().obs_advect_vjp_tape_dev(ctx.handle, _ptr(lx), _ptr(ly), _ptr(gs), _ptr(gx0), _ptr(gy0),
+                                         ctypes.byref(peak)), "obs_advect_vjp_tape_dev")
+    return peak.value
 
 
 def advect_vjp_dev(ctx: Context, core: int, accum: int, order: int, x0, y0, r, s, fs, dt, nsteps,

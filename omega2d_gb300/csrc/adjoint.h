@@ -26,6 +26,17 @@ int run_adjoint_packed(obs_context* ctx, int accum, int mode, int no, const floa
 int run_advect(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y,
                const float* r, const float* s, double fsx, double fsy, double dt, int nsteps);
 
+// Schemes: 1 Euler, 2 Ralston RK2, 3 RK3, 4 Heun RK2 (src/Convection.h:274-598).
+bool advect_order_ok(int order);
+// run_advect that also records checkpoints every `every` steps into ctx->tape for
+// run_advect_vjp_tape (0: ceil(sqrt(nsteps))).
+int run_advect_record(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
+                      const float* s, double fsx, double fsy, double dt, int nsteps, int every);
+// Backward of the recorded run: dL/d(final positions) in (lx, ly); accumulates dL/ds and
+// dL/d(initial positions).  The tape stays valid for further cotangents.
+int run_advect_vjp_tape(obs_context* ctx, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
+                        long long* peak_bytes);
+
 // Reverse of run_advect from the initial positions: given dL/d(final positions), accumulate
 // dL/ds and dL/d(initial positions); the trajectory is recomputed from checkpoints every
 // `every` steps.  peak_bytes (optional) receives the engine's device memory high-water mark.

@@ -168,6 +168,7 @@ int obs_destroy(obs_context* ctx) {
   ctx->io.release();
   ctx->dense.release();
   ctx->state.release();
+  ctx->tape.release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   for (int k = 0; k < 4; ++k)
     if (ctx->timing.ev[k]) cudaEventDestroy(ctx->timing.ev[k]);

@@ -173,7 +173,7 @@ int obs_points_affect_points_vjp_self(obs_context* ctx, int core, int accum, int
 
 int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
                    const float* s, double fsx, double fsy, double dt, int nsteps) {
-  if (!ctx || bad_core_accum(core, accum) || (order != 1 && order != 2) || n < 0 || nsteps < 0) return OBS_ERR_ARG;
+  if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0) return OBS_ERR_ARG;
   if (n > 0 && (!x || !y || !r || !s)) return OBS_ERR_ARG;
   int st = obs::bind(ctx);
   if (st) return st;
@@ -182,7 +182,7 @@ int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, floa
 
 int obs_advect(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y, const float* r,
                const float* s, double fsx, double fsy, double dt, int nsteps) {
-  if (!ctx || bad_core_accum(core, accum) || (order != 1 && order != 2) || n < 0 || nsteps < 0) return OBS_ERR_ARG;
+  if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0) return OBS_ERR_ARG;
   if (n > 0 && (!x || !y || !r || !s)) return OBS_ERR_ARG;
   if (n == 0 || nsteps == 0) return OBS_OK;
   int st = obs::bind(ctx);
@@ -198,11 +198,32 @@ int obs_advect(obs_context* ctx, int core, int accum, int order, int n, float* x
   return fetch(ctx, {{x, dx}, {y, dy}}, n);
 }
 
+int obs_advect_record_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y,
+                          const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
+                          int checkpoint_every) {
+  if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
+      checkpoint_every < 0)
+    return OBS_ERR_ARG;
+  if (n > 0 && (!x || !y || !r || !s)) return OBS_ERR_ARG;
+  int st = obs::bind(ctx);
+  if (st) return st;
+  return obs::run_advect_record(ctx, core, accum, order, n, x, y, r, s, fsx, fsy, dt, nsteps, checkpoint_every);
+}
+
+int obs_advect_vjp_tape_dev(obs_context* ctx, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
+                            long long* peak_bytes) {
+  if (!ctx || !lx || !ly) return OBS_ERR_ARG;
+  if (!ctx->tape_info.valid) return OBS_ERR_ARG;
+  int st = obs::bind(ctx);
+  if (st) return st;
+  return obs::run_advect_vjp_tape(ctx, lx, ly, gs, gx0, gy0, peak_bytes);
+}
+
 int obs_advect_vjp_dev(obs_context* ctx, int core, int accum, int order, int n, const float* x0, const float* y0,
                        const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
                        int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
                        long long* peak_bytes) {
-  if (!ctx || bad_core_accum(core, accum) || (order != 1 && order != 2) || n < 0 || nsteps < 0 ||
+  if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
       checkpoint_every < 0)
     return OBS_ERR_ARG;
   if (n > 0 && (!x0 || !y0 || !r || !s || !lx || !ly)) return OBS_ERR_ARG;
@@ -216,7 +237,7 @@ int obs_advect_vjp(obs_context* ctx, int core, int accum, int order, int n, cons
                    const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
                    int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
                    long long* peak_bytes) {
-  if (!ctx || bad_core_accum(core, accum) || (order != 1 && order != 2) || n < 0 || nsteps < 0 ||
+  if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
       checkpoint_every < 0)
     return OBS_ERR_ARG;
   if (n > 0 && (!x0 || !y0 || !r || !s || !lx || !ly)) return OBS_ERR_ARG;

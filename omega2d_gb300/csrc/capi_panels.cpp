@@ -126,6 +126,64 @@ int obs_panels_affect_points(obs_context* ctx, int accum, int flags, double fsx,
   return copy_back(ctx, {{tu, {dtu, (size_t)nt * 4}}, {tv, {dtv, (size_t)nt * 4}}});
 }
 
+// ---- panels_affect_panels (src/Influence.h:774-795)
+int obs_panels_affect_panels_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                                 int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                                 const float* vs, const float* ss,
+                                 int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                                 float* pu, float* pv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(snn, snx, sny, snp, sidx);
+  if (!s) s = check_panels(tnn, tnx, tny, tnp, tidx);
+  if (s) return s;
+  if ((snp > 0 && !vs) || (tnp > 0 && (!pu || !pv))) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet src{snn, snx, sny, snp, sidx}, targ{tnn, tnx, tny, tnp, tidx};
+  return obs::run_panels_affect_panels(ctx, src, vs, ss, accum, flags, fsx, fsy, targ, pu, pv);
+}
+
+int obs_panels_affect_panels(obs_context* ctx, int accum, int flags, double fsx, double fsy,
+                             int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                             const float* vs, const float* ss,
+                             int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                             float* pu, float* pv) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(snn, snx, sny, snp, sidx);
+  if (!s) s = check_panels(tnn, tnx, tny, tnp, tidx);
+  if (s) return s;
+  if ((snp > 0 && !vs) || (tnp > 0 && (!pu || !pv))) return OBS_ERR_ARG;
+  if (snp == 0 || tnp == 0) return OBS_OK;
+  if ((s = check_host_idx(snn, snp, sidx)) || (s = check_host_idx(tnn, tnp, tidx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)snn * 4);
+  g.reserve((size_t)snp * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)snp * 4);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)tnn * 4);
+  g.reserve((size_t)tnp * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)tnp * 4);
+  if ((s = g.commit())) return s;
+  const float* dsnx = g.take(snx, snn);
+  const float* dsny = g.take(sny, snn);
+  const unsigned* dsidx = g.take(sidx, 2 * (size_t)snp);
+  const float* dvs = g.take(vs, snp);
+  const float* dss = ss ? g.take(ss, snp) : nullptr;
+  if (!ss) g.take<float>(nullptr, snp);
+  const float* dtnx = g.take(tnx, tnn);
+  const float* dtny = g.take(tny, tnn);
+  const unsigned* dtidx = g.take(tidx, 2 * (size_t)tnp);
+  float* dpu = g.take(pu, tnp);
+  float* dpv = g.take(pv, tnp);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet src{snn, dsnx, dsny, snp, dsidx}, targ{tnn, dtnx, dtny, tnp, dtidx};
+  s = obs::run_panels_affect_panels(ctx, src, dvs, dss, accum, flags, fsx, fsy, targ, dpu, dpv);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  return copy_back(ctx, {{pu, {dpu, (size_t)tnp * 4}}, {pv, {dpv, (size_t)tnp * 4}}});
+}
+
 // ---- points_affect_panels (src/Influence.h:633-771)
 int obs_points_affect_panels_dev(obs_context* ctx, int accum, int flags, double fsx, double fsy,
                                  int ns, const float* sx, const float* sy, const float* ss,

@@ -29,6 +29,14 @@ struct WorkHeader {
 };
 static_assert(sizeof(WorkHeader) == 32, "header layout");
 
+// Checkpoints of a recorded forward time-stepping run (obs_advect_record_dev), kept for the
+// backward op: ctx->tape holds r | s | checkpoints (nck x 2N floats).
+struct AdvectTape {
+  bool valid = false;
+  int core = 0, accum = 0, order = 0, n = 0, nsteps = 0, every = 0, nck = 0;
+  double fsx = 0.0, fsy = 0.0, dt = 0.0;
+};
+
 struct Timing {
   bool on = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -47,7 +55,9 @@ struct obs_context {
   obs::DevBuf work;      // header | packed sources | split partials | other scratch
   obs::DevBuf io;        // staging for host-pointer calls
   obs::DevBuf dense;     // BEM matrix (FP64) and its LU factors + pivots
-  obs::DevBuf state;     // time stepping: stage velocities, checkpoints, adjoint vectors
+  obs::DevBuf state;     // time stepping: stage velocities, segment positions, adjoint vectors
+  obs::DevBuf tape;      // recorded forward run: radii, strengths, checkpoints
+  obs::AdvectTape tape_info;
   int bem_n = 0;         // order of the factored BEM matrix held in `dense` (0: none)
   int* d_status = nullptr;   // device status block: DEV_ERR_* bits + first failure record
   int last_failure[4] = {0, 0, 0, 0};   // copy of the block at the last synchronize that saw one

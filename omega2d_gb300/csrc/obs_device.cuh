@@ -13,6 +13,9 @@ namespace obs {
 enum : int { CORE_RM = 1, CORE_GAUSS = 2, CORE_V2 = 3, CORE_WL = 4, CORE_V3 = 5, CORE_SING = 6, CORE_CEXP = 7 };
 // result types (same values as the reference's results_t, src/ResultsType.h:26-32)
 enum : int { RES_VEL = 1, RES_GRAD = 2, RES_PSI = 3, RES_VORT = 4, RES_SHEAR = 5 };
+// Gaussian blob vorticity at field points (points_affect_points_vorticity, src/InfluenceVort.h);
+// internal result type of the generic kernel, not a results_t value
+enum : int { RES_BLOBVORT = 6 };
 
 // status bits written by kernels (read back by the host)
 enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BAD_ITEM = 2, DEV_ERR_BOUNDS = 4, DEV_ERR_SINGULAR = 8 };

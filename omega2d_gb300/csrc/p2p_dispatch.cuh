@@ -10,7 +10,7 @@ namespace obs {
 // Targets per thread for each result type (register budget: 4 for velocity/streamfunction,
 // 2 when the gradient-form core and extra accumulators are live).
 __host__ __device__ constexpr int p2p_tpt(int res) {
-  return (res == RES_VEL || res == RES_PSI) ? 4 : 2;
+  return (res == RES_VEL || res == RES_PSI || res == RES_BLOBVORT) ? 4 : 2;
 }
 
 // a == nullptr: report resident CTAs per SM in *occ; otherwise launch grid CTAs on st.
@@ -50,6 +50,8 @@ extern template cudaError_t p2p_dispatch<CORE_CEXP>(bool, int, bool, const P2PAr
 
 // streamfunction: core-independent (kernelp), instantiated once
 cudaError_t p2p_dispatch_psi(bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st, int* occ);
+// Gaussian blob vorticity at field points, instantiated once
+cudaError_t p2p_dispatch_blobvort(bool comp, const P2PArgs* a, int grid, cudaStream_t st, int* occ);
 cudaError_t p2p_reduce(int res, bool comp, const P2PArgs& a, cudaStream_t st);
 
 }  // namespace obs

@@ -54,6 +54,7 @@ int ncomp_of(int res) {
     case RES_VEL: return 2;
     case RES_GRAD: return 5;
     case RES_PSI: return 1;
+    case RES_BLOBVORT: return 1;
     default: return 3;
   }
 }
@@ -61,6 +62,7 @@ int ncomp_of(int res) {
 cudaError_t dispatch(int core, bool thick, int res, bool comp, const P2PArgs* a, int grid,
                      cudaStream_t st, int* occ) {
   if (res == RES_PSI) return p2p_dispatch_psi(thick, comp, a, grid, st, occ);
+  if (res == RES_BLOBVORT) return thick ? cudaErrorInvalidValue : p2p_dispatch_blobvort(comp, a, grid, st, occ);
   switch (core) {
     case CORE_RM: return p2p_dispatch<CORE_RM>(thick, res, comp, a, grid, st, occ);
     case CORE_GAUSS: return p2p_dispatch<CORE_GAUSS>(thick, res, comp, a, grid, st, occ);
@@ -116,6 +118,7 @@ double p2p_flops(int core, int result, bool thick, long long ns, long long nt) {
     case RES_PSI: per = 10 + (thick ? tvn[core] : tpn[core]); extra_per_target = 1; break;
     case RES_VORT: per = 19 + (thick ? tvg[core] : tpg[core]); extra_per_target = 3; break;
     case RES_SHEAR: per = 23 + (thick ? tvg[core] : tpg[core]); extra_per_target = 3; break;
+    case RES_BLOBVORT: per = 13; extra_per_target = 1; break;   // src/InfluenceVort.h:112
     default: return -1.0;
   }
   return (double)nt * ((double)extra_per_target + (double)per * (double)ns);

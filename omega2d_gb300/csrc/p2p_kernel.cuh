@@ -54,6 +54,7 @@ template <> struct NComp<RES_GRAD>  { static constexpr int v = 5; };  // u, v, S
 template <> struct NComp<RES_PSI>   { static constexpr int v = 1; };
 template <> struct NComp<RES_VORT>  { static constexpr int v = 3; };
 template <> struct NComp<RES_SHEAR> { static constexpr int v = 3; };
+template <> struct NComp<RES_BLOBVORT> { static constexpr int v = 1; };
 
 constexpr double kInv2Pi = 0.15915494309189535;   // 0.5/pi, src/ElementBase.h:216
 
@@ -72,7 +73,7 @@ __device__ __forceinline__ void store_target(const P2PArgs& a, int ib, const dou
     const double v = ((double)p[i] + add) * f + fs;
     p[i] = (float)v;
   };
-  if constexpr (RES == RES_PSI) {
+  if constexpr (RES == RES_PSI || RES == RES_BLOBVORT) {
     put(2, c[0], 0.0);
     return;
   }
@@ -112,6 +113,12 @@ __device__ __forceinline__ void p2p_tile(const float4* __restrict__ tile,
           // kernelp: -strength * 0.5 * log(d^2 + sr^2 (+ tr^2)), src/Kernels.h:52-74
           const float q = d2 + (THICK ? s.z + tz[k] : s.z);
           acc[k][0] = fmaf(-s.w * (0.5f * kLn2), lg2_a(q), acc[k][0]);
+        } else if constexpr (RES == RES_BLOBVORT) {
+          // points_affect_points_vorticity (src/InfluenceVort.h:96-110, the non-Vc branch: no
+          // cut-off): w += 2 G exp(-d^2/s^2) / s^2, s the source radius (s.z = s^2)
+          const float cf = UNIF ? ucf : rcp_a(s.z);
+          const float e = ex2_a(d2 * cf * -kLog2e);
+          acc[k][0] = fmaf(2.0f * s.w * cf, e, acc[k][0]);
         } else {
           float K, B = 0.0f;
           core_eval<CORE, THICK, GRADCORE, UNIF>(d2, s.z, tz[k], us2, ucf, K, B);

@@ -21,6 +21,9 @@ int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* 
 int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const float* sy, const float* ss,
                              const PanelSet& ps, int accum, int flags, double fsx, double fsy,
                              float* pu, float* pv);
+// panels_affect_panels (src/Influence.h:774-795) through the reference's collocation points
+int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
+                             int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv);
 int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const PanelSet& targ, int nunk, int self,
                                float* A32, double* A64);
 int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,

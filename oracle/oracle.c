@@ -30,6 +30,7 @@
 #define SQRT sqrtf
 #define CBRT cbrtf
 #define ATAN2 atan2f
+#define FMA fmaf
 #include "oracle_impl.h"
 #undef R
 #undef A
@@ -39,6 +40,7 @@
 #undef SQRT
 #undef CBRT
 #undef ATAN2
+#undef FMA
 
 /* double instantiation */
 #define R double
@@ -49,6 +51,7 @@
 #define SQRT sqrt
 #define CBRT cbrt
 #define ATAN2 atan2
+#define FMA fma
 #include "oracle_impl.h"
 #undef R
 #undef A
@@ -58,6 +61,7 @@
 #undef SQRT
 #undef CBRT
 #undef ATAN2
+#undef FMA
 
 /* ------------------------------------------------------------------ FP64 adjoint references */
 

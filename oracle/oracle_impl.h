@@ -197,6 +197,25 @@ void SFX(o_points_affect_points)(int core, int restype,
   }
 }
 
+/* points_affect_points_vorticity, src/InfluenceVort.h:96-110 (the non-Vc branch, no cut-off):
+ * Gaussian-blob vorticity at field points, tw += sum 2 ss exp(-d^2/sr^2) / sr^2; the
+ * differences are formed in R and the rest in A, as there. */
+void SFX(o_points_affect_points_vorticity)(int ns, const R* sx, const R* sy, const R* sr, const R* ss,
+                                           int nt, const R* tx, const R* ty, R* tw) {
+  #pragma omp parallel for schedule(static)
+  for (int i = 0; i < nt; ++i) {
+    A aw = 0;
+    for (int j = 0; j < ns; ++j) {
+      const A dx = (A)(tx[i] - sx[j]);
+      const A dy = (A)(ty[i] - sy[j]);
+      const A s2 = (A)sr[j] * (A)sr[j];
+      const A distsq = (dx*dx + dy*dy) / s2;
+      aw += (A)((R)2.0 * ss[j]) * exp(-distsq) / s2;
+    }
+    tw[i] = (R)((A)tw[i] + aw);
+  }
+}
+
 /* ---------------------------------------------------------------- panels */
 
 /* get_ustar, src/Kernels.h:256-268 (non-Vc): angle subtended by the panel, wrapped to [-pi, pi] */
@@ -433,4 +452,106 @@ void SFX(o_advect_2nd_ralston)(int core, int n, R* x, R* y, const R* r, const R*
     }
   }
   free(u1); free(v1); free(u2); free(v2); free(x2); free(y2);
+}
+
+
+/* panels_affect_panels, src/Influence.h:774-795: the target panels become collocation points
+ * as Surfaces::represent_as_particles(1e-4, -1) builds them (src/Surfaces.h:830-876, with the
+ * bases of compute_bases, :682-724): nshed = 1 + max(0, (int)(len_i / (1.2 len_0))) points per
+ * panel at weights (1+2j)/(2 nshed) along it, pushed 1e-4 along the normal into the fluid;
+ * the panels' influence on those points (from zero) is then added to the first ntp panel
+ * velocities, index by index, as the reference's std::transform does. */
+void SFX(o_panels_affect_panels)(const R* snx, const R* sny, int snp, const unsigned* sidx,
+                                 const R* vs, const R* ss,
+                                 const R* tnx, const R* tny, int tnp, const unsigned* tidx,
+                                 R* pu, R* pv) {
+  if (tnp <= 0) return;
+  R* px = (R*)malloc(sizeof(R) * (size_t)tnp);
+  R* py = (R*)malloc(sizeof(R) * (size_t)tnp);
+  R* qu = (R*)calloc((size_t)tnp, sizeof(R));
+  R* qv = (R*)calloc((size_t)tnp, sizeof(R));
+  const float off = 0.0001f;
+  float len0 = 0.0f;
+  int m = 0;
+  for (int i = 0; i < tnp && m < tnp; ++i) {
+    const float x0 = (float)tnx[tidx[2*i]], y0 = (float)tny[tidx[2*i]];
+    const float x1 = (float)tnx[tidx[2*i+1]], y1 = (float)tny[tidx[2*i+1]];
+    float tx = x1 - x0, ty = y1 - y0;
+    const float len = sqrtf(tx*tx + ty*ty);
+    tx = (float)(tx * (1.0 / len));
+    ty = (float)(ty * (1.0 / len));
+    const float nxv = -ty, nyv = tx;
+    if (i == 0) len0 = len;
+    const int q = (int)(len / (1.2 * len0));
+    const int nshed = 1 + (q > 0 ? q : 0);
+    for (int j = 0; j < nshed && m < tnp; ++j, ++m) {
+      const float w = (float)(1 + 2*j) / (float)(2*nshed);
+      px[m] = (R)(float)((double)(w * x1) + (1.0 - w) * x0 + (double)(off * nxv));
+      py[m] = (R)(float)((double)(w * y1) + (1.0 - w) * y0 + (double)(off * nyv));
+    }
+  }
+  SFX(o_panels_affect_points)(snx, sny, snp, sidx, vs, ss, tnp, px, py, qu, qv);
+  for (int i = 0; i < tnp; ++i) { pu[i] += qu[i]; pv[i] += qv[i]; }
+  free(px); free(py); free(qu); free(qv);
+}
+
+/* ElementBase::move with one weight 1.0 (src/ElementBase.h:276-296): x += (S)h * 1.0 * u,
+ * the product formed in double; into (xo, yo) */
+static void SFX(move_one)(int n, const R* x, const R* y, const R* u, const R* v, double h, R* xo, R* yo) {
+  const double hs = (double)(R)h;
+  for (int i = 0; i < n; ++i) {
+    xo[i] = (R)((double)x[i] + hs * (double)u[i]);
+    yo[i] = (R)((double)y[i] + hs * (double)v[i]);
+  }
+}
+
+/* ElementBase::move with two or three weights (src/ElementBase.h:299-359): u = sum w_k u_k in
+ * double, stored as S; x += (S)dt * u (one fused multiply-add, as the reference's optimised
+ * build contracts it) */
+static void SFX(move_comb)(int n, R* x, R* y, double dt, int nw, const double* w, R* const* us, R* const* vs) {
+  for (int i = 0; i < n; ++i) {
+    double cu = w[0] * us[0][i], cv = w[0] * vs[0][i];
+    for (int k = 1; k < nw; ++k) { cu += w[k] * us[k][i]; cv += w[k] * vs[k][i]; }
+    x[i] = FMA((R)dt, (R)cu, x[i]);
+    y[i] = FMA((R)dt, (R)cv, y[i]);
+  }
+}
+
+/* Convection::advect_2nd_heun without bodies (src/Convection.h:310-387):
+ * y = x + dt u(x); x += dt (1/2 u(x) + 1/2 u(y)) */
+void SFX(o_advect_2nd_heun)(int core, int n, R* x, R* y, const R* r, const R* s,
+                            double fsx, double fsy, double dt, int nsteps) {
+  R* buf = (R*)malloc(sizeof(R) * 6 * (size_t)n);
+  R *u1 = buf, *v1 = buf + n, *u2 = buf + 2*n, *v2 = buf + 3*n, *x2 = buf + 4*n, *y2 = buf + 5*n;
+  const double w[2] = {0.5, 0.5};
+  R* const us[2] = {u1, u2};
+  R* const vv[2] = {v1, v2};
+  for (int k = 0; k < nsteps; ++k) {
+    SFX(self_vels)(core, n, x, y, r, s, fsx, fsy, u1, v1);
+    SFX(move_one)(n, x, y, u1, v1, dt, x2, y2);
+    SFX(self_vels)(core, n, x2, y2, r, s, fsx, fsy, u2, v2);
+    SFX(move_comb)(n, x, y, dt, 2, w, us, vv);
+  }
+  free(buf);
+}
+
+/* Convection::advect_3rd without bodies (src/Convection.h:473-598):
+ * y1 = x + dt/2 u(x); y2 = x + 3/4 dt u(y1); x += dt (2/9 u(x) + 3/9 u(y1) + 4/9 u(y2)) */
+void SFX(o_advect_3rd)(int core, int n, R* x, R* y, const R* r, const R* s,
+                       double fsx, double fsy, double dt, int nsteps) {
+  R* buf = (R*)malloc(sizeof(R) * 10 * (size_t)n);
+  R *u1 = buf, *v1 = buf + n, *u2 = buf + 2*n, *v2 = buf + 3*n, *u3 = buf + 4*n, *v3 = buf + 5*n;
+  R *x1 = buf + 6*n, *y1 = buf + 7*n, *x2 = buf + 8*n, *y2 = buf + 9*n;
+  const double w[3] = {2.0 / 9.0, 3.0 / 9.0, 4.0 / 9.0};
+  R* const us[3] = {u1, u2, u3};
+  R* const vv[3] = {v1, v2, v3};
+  for (int k = 0; k < nsteps; ++k) {
+    SFX(self_vels)(core, n, x, y, r, s, fsx, fsy, u1, v1);
+    SFX(move_one)(n, x, y, u1, v1, 0.5 * dt, x1, y1);
+    SFX(self_vels)(core, n, x1, y1, r, s, fsx, fsy, u2, v2);
+    SFX(move_one)(n, x, y, u2, v2, 0.75 * dt, x2, y2);
+    SFX(self_vels)(core, n, x2, y2, r, s, fsx, fsy, u3, v3);
+    SFX(move_comb)(n, x, y, dt, 3, w, us, vv);
+  }
+  free(buf);
 }

@@ -134,10 +134,33 @@ class Restatement:
         x = np.array(x, dtype=dt); y = np.array(y, dtype=dt)
         r, s = _arr(r, dt), _arr(s, dt)
         sfx = "_d" if fp64 else "_f"
-        fn = getattr(self.lib, ("o_advect_1st" if order == 1 else "o_advect_2nd_ralston") + sfx)
+        name = {1: "o_advect_1st", 2: "o_advect_2nd_ralston", 3: "o_advect_3rd", 4: "o_advect_2nd_heun"}[order]
+        fn = getattr(self.lib, name + sfx)
         fn(ctypes.c_int(core), ctypes.c_int(x.size), _p(x), _p(y), _p(r), _p(s),
            ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(dt_), ctypes.c_int(nsteps))
         return x, y
+
+    def points_affect_points_vorticity(self, sx, sy, sr, ss, tx, ty, tw=None, fp64=False):
+        """Gaussian-blob vorticity at field points (src/InfluenceVort.h:47-126), accumulated."""
+        dt = np.float64 if fp64 else np.float32
+        sx, sy, sr, ss, tx, ty = (_arr(a, dt) for a in (sx, sy, sr, ss, tx, ty))
+        tw = np.zeros(tx.size, dt) if tw is None else np.array(tw, dtype=dt)
+        fn = self.lib.o_points_affect_points_vorticity_d if fp64 else self.lib.o_points_affect_points_vorticity_f
+        fn(ctypes.c_int(sx.size), _p(sx), _p(sy), _p(sr), _p(ss), ctypes.c_int(tx.size), _p(tx), _p(ty), _p(tw))
+        return tw
+
+    def panels_affect_panels(self, snx, sny, sidx, vs, ss, tnx, tny, tidx, pu=None, pv=None, fp64=False):
+        """Panel-centre velocities of the target panels (src/Influence.h:774-795), accumulated."""
+        dt = np.float64 if fp64 else np.float32
+        snx, sny, vs, ss, tnx, tny = (_arr(a, dt) for a in (snx, sny, vs, ss, tnx, tny))
+        sidx, tidx = _arr(sidx, np.uint32), _arr(tidx, np.uint32)
+        tnp = tidx.size // 2
+        pu = np.zeros(tnp, dt) if pu is None else np.array(pu, dtype=dt)
+        pv = np.zeros(tnp, dt) if pv is None else np.array(pv, dtype=dt)
+        fn = self.lib.o_panels_affect_panels_d if fp64 else self.lib.o_panels_affect_panels_f
+        fn(_p(snx), _p(sny), ctypes.c_int(sidx.size // 2), _p(sidx), _p(vs), _p(ss),
+           _p(tnx), _p(tny), ctypes.c_int(tnp), _p(tidx), _p(pu), _p(pv))
+        return pu, pv
 
     # ---- FP64 adjoints
     def probe_vjp(self, core, sx, sy, sr, ss, px, py, lu, lv):
@@ -260,10 +283,29 @@ class Reference:
     def advect(self, order, x, y, r, s, fs, dt_, nsteps):
         x = np.array(x, dtype=np.float32); y = np.array(y, dtype=np.float32)
         r, s = _arr(r, np.float32), _arr(s, np.float32)
-        fn = self.lib.ref_advect_1st_f if order == 1 else self.lib.ref_advect_2nd_ralston_f
+        fn = {1: self.lib.ref_advect_1st_f, 2: self.lib.ref_advect_2nd_ralston_f, 3: self.lib.ref_advect_3rd_f,
+              4: self.lib.ref_advect_2nd_heun_f}[order]
         fn(ctypes.c_int(x.size), _p(x), _p(y), _p(r), _p(s), ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
            ctypes.c_double(dt_), ctypes.c_int(nsteps))
         return x, y
+
+    def points_affect_points_vorticity(self, sx, sy, sr, ss, tx, ty, tw=None):
+        sx, sy, sr, ss, tx, ty = (_arr(a, np.float32) for a in (sx, sy, sr, ss, tx, ty))
+        tw = np.zeros(tx.size, np.float32) if tw is None else np.array(tw, dtype=np.float32)
+        self.lib.ref_points_affect_points_vorticity_f(ctypes.c_int(sx.size), _p(sx), _p(sy), _p(sr), _p(ss),
+                                                      ctypes.c_int(tx.size), _p(tx), _p(ty), _p(tw))
+        return tw
+
+    def panels_affect_panels(self, snx, sny, sidx, vs, ss, tnx, tny, tidx, pu=None, pv=None):
+        snx, sny, vs, ss, tnx, tny = (_arr(a, np.float32) for a in (snx, sny, vs, ss, tnx, tny))
+        sidx, tidx = _arr(sidx, np.uint32), _arr(tidx, np.uint32)
+        tnp = tidx.size // 2
+        pu = np.zeros(tnp, np.float32) if pu is None else np.array(pu, dtype=np.float32)
+        pv = np.zeros(tnp, np.float32) if pv is None else np.array(pv, dtype=np.float32)
+        self.lib.ref_panels_affect_panels_f(ctypes.c_int(snx.size), _p(snx), _p(sny), ctypes.c_int(sidx.size // 2),
+                                            _p(sidx), _p(vs), _p(ss), ctypes.c_int(tnx.size), _p(tnx), _p(tny),
+                                            ctypes.c_int(tnp), _p(tidx), _p(pu), _p(pv))
+        return pu, pv
 
     def flop_counts(self):
         out = (ctypes.c_int * 8)()

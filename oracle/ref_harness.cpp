@@ -14,6 +14,7 @@
 #include "Omega2D.h"
 #include "Collection.h"
 #include "Influence.h"
+#include "InfluenceVort.h"
 #include "Coefficients.h"
 #include "RHS.h"
 
@@ -355,6 +356,87 @@ int ref_advect_2nd_ralston_f(int n, float* x, float* y, const float* r, const fl
   }
   const auto& px = p.get_pos();
   for (int i = 0; i < n; ++i) { x[i] = px[0][i]; y[i] = px[1][i]; }
+  return 0;
+}
+
+// Convection::advect_2nd_heun (src/Convection.h:310-387) without bodies
+int ref_advect_2nd_heun_f(int n, float* x, float* y, const float* r, const float* s,
+                          double fsx, double fsy, double dt, int nsteps) {
+  Quiet q;
+  Points<float> p = make_points<float>(n, x, y, r, s, false);
+  double t = 0.0;
+  for (int k = 0; k < nsteps; ++k) {
+    p.zero_vels();
+    points_affect_points<float, double>(p, p, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p.finalize_vels({fsx, fsy});
+    Points<float> p2 = p;
+    p2.move(t, dt, 1.0, p2);
+    p2.zero_vels();
+    points_affect_points<float, double>(p2, p2, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p2.finalize_vels({fsx, fsy});
+    p.move(t, dt, 0.5, p, 0.5, p2);
+    t += dt;
+  }
+  const auto& px = p.get_pos();
+  for (int i = 0; i < n; ++i) { x[i] = px[0][i]; y[i] = px[1][i]; }
+  return 0;
+}
+
+// Convection::advect_3rd (src/Convection.h:473-598) without bodies
+int ref_advect_3rd_f(int n, float* x, float* y, const float* r, const float* s,
+                     double fsx, double fsy, double dt, int nsteps) {
+  Quiet q;
+  Points<float> p = make_points<float>(n, x, y, r, s, false);
+  double t = 0.0;
+  for (int k = 0; k < nsteps; ++k) {
+    p.zero_vels();
+    points_affect_points<float, double>(p, p, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p.finalize_vels({fsx, fsy});
+    Points<float> p1 = p;
+    p1.move(t, 0.5 * dt, 1.0, p1);
+    p1.zero_vels();
+    points_affect_points<float, double>(p1, p1, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p1.finalize_vels({fsx, fsy});
+    Points<float> p2 = p;
+    p2.move(t, 0.75 * dt, 1.0, p1);
+    p2.zero_vels();
+    points_affect_points<float, double>(p2, p2, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+    p2.finalize_vels({fsx, fsy});
+    p.move(t, dt, 2.0 / 9.0, p, 3.0 / 9.0, p1, 4.0 / 9.0, p2);
+    t += dt;
+  }
+  const auto& px = p.get_pos();
+  for (int i = 0; i < n; ++i) { x[i] = px[0][i]; y[i] = px[1][i]; }
+  return 0;
+}
+
+// points_affect_points_vorticity (src/InfluenceVort.h:47-126), x86 branch: tw accumulated
+int ref_points_affect_points_vorticity_f(int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+                                         int nt, const float* tx, const float* ty, float* tw) {
+  Quiet q;
+  Points<float> src = make_points<float>(ns, sx, sy, sr, ss, false);
+  Points<float> targ = make_points<float>(nt, tx, ty, nullptr, nullptr, true);
+  Vector<float>& w = targ.get_vort();
+  w.resize((size_t)nt);
+  for (int i = 0; i < nt; ++i) w[i] = tw[i];
+  points_affect_points_vorticity<float, double>(src, targ, ExecEnv(true, direct, cpu_x86));
+  for (int i = 0; i < nt; ++i) tw[i] = w[i];
+  return 0;
+}
+
+// panels_affect_panels (src/Influence.h:774-795): panel-centre velocities of the target body
+// (accumulated) from the active source panels, through the reference's collocation points
+int ref_panels_affect_panels_f(int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
+                               const float* vs, const float* ss,
+                               int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
+                               float* pu, float* pv) {
+  Quiet q;
+  Surfaces<float> src = make_surfaces<float>(snn, snx, sny, snp, sidx, vs, ss, active);
+  Surfaces<float> targ = make_surfaces<float>(tnn, tnx, tny, tnp, tidx, nullptr, nullptr, reactive);
+  auto& vel = targ.get_vel();
+  for (int i = 0; i < tnp; ++i) { vel[0][i] = pu[i]; vel[1][i] = pv[i]; }
+  panels_affect_panels<float, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  for (int i = 0; i < tnp; ++i) { pu[i] = vel[0][i]; pv[i] = vel[1][i]; }
   return 0;
 }
 

@@ -111,6 +111,39 @@ def make_advect(out):
     np.savez_compressed(out, **d)
 
 
+def make_extras(out):
+    """Blob vorticity (src/InfluenceVort.h), panels on panels (src/Influence.h:774-795) and the
+    Heun / RK3 integrators (src/Convection.h:310-387, 473-598)."""
+    rng = np.random.default_rng(20240604)
+    ns, nt = 300, 211
+    sx, sy, sr, ss = particles(rng, ns)
+    tx, ty, _, _ = particles(rng, nt)
+    tx[:30], ty[:30] = sx[:30], sy[:30]
+    tw0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    d = dict(sx=sx, sy=sy, sr=sr, ss=ss, tx=tx, ty=ty, tw0=tw0)
+    d["vort_w"] = po.Reference(po.GAUSS).points_affect_points_vorticity(sx, sy, sr, ss, tx, ty, tw0)
+    # panels on panels: a circle of 96 panels acting on an uneven open polyline (long panels
+    # shed several collocation points, the reference adds the first npan velocities back)
+    snx, sny, sidx = circle_panels(96)
+    vs = rng.normal(0, 1, 96).astype(np.float32)
+    sss = rng.normal(0, 1, 96).astype(np.float32)
+    tnx = np.array([0.7, 0.8, 1.2, 1.3, 2.0, 2.0, 2.1], np.float32)
+    tny = np.array([0.0, 0.0, 0.05, 0.1, 0.1, 0.5, 0.55], np.float32)
+    tidx = np.array([0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6], np.uint32)
+    pu0 = rng.normal(0, 0.1, 6).astype(np.float32)
+    pv0 = rng.normal(0, 0.1, 6).astype(np.float32)
+    d.update(snx=snx, sny=sny, sidx=sidx, vs=vs, sss=sss, tnx=tnx, tny=tny, tidx=tidx, pu0=pu0, pv0=pv0)
+    d["pap_u"], d["pap_v"] = po.Reference(po.V2).panels_affect_panels(snx, sny, sidx, vs, sss, tnx, tny, tidx,
+                                                                       pu0, pv0)
+    n = 300
+    x, y, _, s = particles(rng, n)
+    r = np.full(n, 0.05, np.float32)
+    d.update(x=x, y=y, r=r, s=s)
+    d["rk3_x"], d["rk3_y"] = po.Reference(po.GAUSS).advect(3, x, y, r, s, (0.5, 0.0), 0.01, 4)
+    d["heun_x"], d["heun_y"] = po.Reference(po.RM).advect(4, x, y, r, s, (0.0, 0.25), 0.01, 4)
+    np.savez_compressed(out, **d)
+
+
 def main():
     if not build_ref.available():
         raise SystemExit("the reference tree is needed to generate golden vectors")
@@ -118,6 +151,7 @@ def main():
     make_p2p(os.path.join(HERE, "p2p.npz"))
     make_panels(os.path.join(HERE, "panels.npz"))
     make_advect(os.path.join(HERE, "advect.npz"))
+    make_extras(os.path.join(HERE, "extras.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

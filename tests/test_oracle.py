@@ -182,3 +182,25 @@ def test_rk2_centroid_gradient_matches_finite_differences(restatement):
         fd = (restatement.rk2_centroid_loss(po.GAUSS, xp, y, r, s, lab, (0.0, 0.0), 0.02, 6)
               - restatement.rk2_centroid_loss(po.GAUSS, xm, y, r, s, lab, (0.0, 0.0), 0.02, 6)) / (2 * h)
         assert abs(fd - gx[j]) < 1e-6 * max(1.0, abs(fd)), (j, fd, gx[j])
+
+
+def test_restatement_blob_vorticity_golden(restatement, golden):
+    g = golden("extras")
+    w = restatement.points_affect_points_vorticity(g["sx"], g["sy"], g["sr"], g["ss"], g["tx"], g["ty"], g["tw0"])
+    assert rel_err(g["vort_w"], w) < 1e-6
+
+
+def test_restatement_panels_on_panels_golden(restatement, golden):
+    g = golden("extras")
+    pu, pv = restatement.panels_affect_panels(g["snx"], g["sny"], g["sidx"], g["vs"], g["sss"],
+                                              g["tnx"], g["tny"], g["tidx"], g["pu0"], g["pv0"])
+    # collocation points sit 1e-4 off the panels: FP32 atan2/log rounding is amplified there
+    assert rel_err(g["pap_u"], pu) < 5e-6 and rel_err(g["pap_v"], pv) < 5e-6
+
+
+@pytest.mark.parametrize("order,key,core,fs", [(3, "rk3", 2, (0.5, 0.0)), (4, "heun", 1, (0.0, 0.25))])
+def test_restatement_rk3_heun_golden(restatement, golden, order, key, core, fs):
+    g = golden("extras")
+    x, y = restatement.advect(order, core, g["x"], g["y"], g["r"], g["s"], fs, 0.01, 4)
+    disp = np.max(np.hypot(g[key + "_x"] - g["x"], g[key + "_y"] - g["y"]))
+    assert np.max(np.hypot(x - g[key + "_x"], y - g[key + "_y"])) < 2e-5 * disp
