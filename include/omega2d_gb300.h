@@ -75,11 +75,13 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 /* Kernel variant for particle-on-particle velocity sums.  AUTO uses the packed-FP32 kernels
  * (two targets per f32x2 register pair) where they exist (velocity only, Gaussian and RM
- * cores) and the generic kernels elsewhere; GENERIC forces the generic kernels; PACKED2 /
- * PACKED4 pick 2 or 4 target pairs per thread for the packed kernels. */
+ * cores; 4 target pairs per thread for the Gaussian core, 2 for RM) and the generic kernels
+ * elsewhere; GENERIC forces the generic kernels; PACKED2 / PACKED3 / PACKED4 pick 2, 3 or 4
+ * target pairs per thread for the packed kernels. */
 #define OBS_VARIANT_AUTO 0
 #define OBS_VARIANT_GENERIC 1
 #define OBS_VARIANT_PACKED2 2
+#define OBS_VARIANT_PACKED3 3   /* Gaussian only; other cores use 2 */
 #define OBS_VARIANT_PACKED4 4
 int obs_set_kernel_variant(obs_context* ctx, int variant);
 /* Processing order inside a packed Gaussian velocity sum.  Binning sorts points into a

@@ -33,7 +33,7 @@ CORE_RM, CORE_GAUSSIAN, CORE_V2, CORE_WL, CORE_V3, CORE_SINGULAR, CORE_COMPACT_E
 VELONLY, VELANDGRAD, PSIONLY, VELANDVORT, VELANDSHEAR = 1, 2, 3, 4, 5
 PLAIN_F32, COMPENSATED = 0, 1
 FLAG_FINALIZE = 1
-VARIANT_AUTO, VARIANT_GENERIC, VARIANT_PACKED2, VARIANT_PACKED4 = 0, 1, 2, 4
+VARIANT_AUTO, VARIANT_GENERIC, VARIANT_PACKED2, VARIANT_PACKED3, VARIANT_PACKED4 = 0, 1, 2, 3, 4
 ORDER_AUTO, ORDER_INPUT, ORDER_BINNED, ORDER_BINNED_TARGETS = 0, 1, 2, 3
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "allocation failed", -3: "CUDA runtime error",

@@ -232,7 +232,7 @@ int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2) {
 int obs_set_kernel_variant(obs_context* ctx, int variant) {
   if (!ctx) return OBS_ERR_ARG;
   if (variant != OBS_VARIANT_AUTO && variant != OBS_VARIANT_GENERIC && variant != OBS_VARIANT_PACKED2 &&
-      variant != OBS_VARIANT_PACKED4)
+      variant != OBS_VARIANT_PACKED3 && variant != OBS_VARIANT_PACKED4)
     return OBS_ERR_ARG;
   ctx->kernel_variant = variant;
   return OBS_OK;

@@ -135,7 +135,11 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   // ---- kernel choice: the packed-FP32 kernels serve velocity-only Gaussian / RM sums
   const int variant = ctx->kernel_variant;
   const bool packed = variant != OBS_VARIANT_GENERIC && packed_supported(rq.core, res);
-  const int np = (variant == OBS_VARIANT_PACKED4) ? 4 : 2;
+  // target pairs per thread: AUTO takes 4 for the Gaussian core (1M patch, Morton order: 4107 vs
+  // 3788 Ginter/s compensated, 4380 vs 4333 plain against 2 pairs) and 2 for RM
+  int np = 2;
+  if (variant == OBS_VARIANT_PACKED4 || (variant == OBS_VARIANT_AUTO && rq.core == CORE_GAUSS)) np = 4;
+  else if (variant == OBS_VARIANT_PACKED3 && rq.core == CORE_GAUSS) np = 3;
   auto launch = [&](const P2PArgs* args, int g, int* occ_out) -> cudaError_t {
     return packed ? packed_dispatch(rq.core, np, thick, comp, args, g, st, occ_out)
                   : dispatch(rq.core, thick, res, comp, args, g, st, occ_out);

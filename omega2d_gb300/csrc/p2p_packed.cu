@@ -62,8 +62,9 @@ bool packed_supported(int core, int res) {
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
                             int* occ) {
   if (core == CORE_GAUSS) {
-    return np == 4 ? packed_dispatch_np<CORE_GAUSS, 4>(thick, comp, a, grid, st, occ)
-                   : packed_dispatch_np<CORE_GAUSS, 2>(thick, comp, a, grid, st, occ);
+    if (np == 4) return packed_dispatch_np<CORE_GAUSS, 4>(thick, comp, a, grid, st, occ);
+    if (np == 3) return packed_dispatch_np<CORE_GAUSS, 3>(thick, comp, a, grid, st, occ);
+    return packed_dispatch_np<CORE_GAUSS, 2>(thick, comp, a, grid, st, occ);
   }
   if (core == CORE_RM) {
     return np == 4 ? packed_dispatch_np<CORE_RM, 4>(thick, comp, a, grid, st, occ)

@@ -151,7 +151,7 @@ __device__ __forceinline__ void general_block(const float4* __restrict__ blk, co
 // NP = 2 fits 64 registers without spills: 8 CTAs (32 warps) per SM; NP = 4 keeps its 128
 // registers (4 CTAs per SM).
 template <int CORE, bool THICK, bool COMP, int NP>
-__global__ void __launch_bounds__(P2P_THREADS, NP == 2 ? 8 : 4)
+__global__ void __launch_bounds__(P2P_THREADS, NP == 2 ? 8 : (NP == 3 ? 5 : 4))
 p2p_packed_kernel(const P2PArgs a) {
   constexpr int TPT = 2 * NP;
   constexpr int TB = P2P_THREADS * TPT;

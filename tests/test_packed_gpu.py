@@ -19,7 +19,7 @@ def cloud(rng, n, uniform):
 @pytest.mark.parametrize("thick", [True, False])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
 @pytest.mark.parametrize("uniform", [True, False])
-@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED4])
+@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4])
 def test_packed_matches_generic_and_fp64(ctx, restatement, core, thick, accum, uniform, variant):
     rng = np.random.default_rng(core * 100 + thick * 10 + accum + 2 * uniform + variant)
     ns, nt = 5000, 3001
@@ -72,7 +72,7 @@ def _vel(ctx, src, tx, ty, tr, core, accum, order, variant):
 @pytest.mark.parametrize("sigma", [1e-4, 2e-3, 0.05])
 @pytest.mark.parametrize("thick", [True, False])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
-@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED4])
+@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4])
 def test_binned_order_identities(ctx, sigma, thick, accum, variant):
     """Binned target order gives the same bits as the caller's order: the far-block fast form and
     the full form agree pair by pair, and each target's sum runs over the sources in one order."""
