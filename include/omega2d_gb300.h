@@ -32,6 +32,7 @@ extern "C" {
 #define OBS_ERR_SINGULAR (-6)   /* dense solve met a zero pivot                              */
 #define OBS_ERR_UNSUPPORTED (-7)
 #define OBS_ERR_SCRATCH_LIMIT (-8)  /* size exceeds obs_points_affect_points_noalloc's scratch */
+#define OBS_ERR_NO_CONVERGENCE (-9) /* an iterative solve stopped above its tolerance           */
 
 /* ---- core functions (src/CoreFunc.h:35-322 selects one at compile time; here at run time) */
 #define OBS_CORE_RM 1           /* Rosenhead-Moore, src/CoreFunc.h:42-82                     */
@@ -224,11 +225,25 @@ int obs_solve_dense_f64(obs_context* ctx, int n, const double* A, const double* 
 int obs_solve_dense_f64_dev(obs_context* ctx, int n, const double* A, const double* b, double* x,
                             double* rel_residual);
 
+/* Restarted GMRES in FP64 on the GPU (the reference's BEM solver method, Eigen GMRES in FP32,
+ * src/BEM.h:169-234): right diagonal preconditioning, classical Gram-Schmidt with one
+ * reorthogonalisation, Givens rotations on the device.  x holds the initial guess on entry and
+ * the solution on return; iterations and rel_residual = ||b - A x|| / ||b|| are optional
+ * outputs.  OBS_ERR_NO_CONVERGENCE when maxiter iterations end above tol (x then holds the
+ * last iterate). */
+int obs_solve_gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol,
+                        int restart, int maxiter, int* iterations, double* rel_residual);
+int obs_solve_gmres_f64_dev(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol,
+                            int restart, int maxiter, int* iterations, double* rel_residual);
+
 /* solve_bem for one fixed reactive body -- replaces src/BEMHelper.h:43-260 without rotation
  * augmentation: particles -> panel velocities, finalize with fs, RHS, influence matrix, FP64
- * solve, strengths out (vs_out; ss_out when nunk == 2).  OBS_BEM_REUSE_MATRIX keeps the
- * previous factorisation of the same order (the reference's is_A_current, src/BEM.h:49-51). */
+ * solve, strengths out (vs_out; ss_out when nunk == 2).  The solve is FP64 GMRES (restart 60,
+ * relative residual 1e-13, at most 2n iterations, zero initial guess); OBS_BEM_DIRECT_LU selects
+ * the FP64 LU instead.  OBS_BEM_REUSE_MATRIX keeps the previous matrix (and factorisation) of
+ * the same order (the reference's is_A_current, src/BEM.h:49-51). */
 #define OBS_BEM_REUSE_MATRIX 2
+#define OBS_BEM_DIRECT_LU 4      /* solve by the FP64 LU instead of FP64 GMRES */
 int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
                   int ns, const float* sx, const float* sy, const float* ss,
                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,

@@ -38,7 +38,8 @@ ORDER_AUTO, ORDER_INPUT, ORDER_BINNED, ORDER_BINNED_TARGETS = 0, 1, 2, 3
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "allocation failed", -3: "CUDA runtime error",
           -4: "device wait timed out", -5: "no usable CUDA device", -6: "singular matrix",
-          -7: "unsupported combination", -8: "size exceeds the no-allocation scratch"}
+          -7: "unsupported combination", -8: "size exceeds the no-allocation scratch",
+          -9: "iterative solve did not reach its tolerance"}
 
 
 class EngineError(RuntimeError):
@@ -481,8 +482,35 @@ def solve_dense_f64(A: np.ndarray, b: np.ndarray, context: Context | None = None
     return x, rel.value
 
 
+def solve_gmres_f64(A: np.ndarray, b: np.ndarray, x0=None, tol: float = 1e-13, restart: int = 60,
+                    maxiter: int | None = None, context: Context | None = None):
+    """FP64 GMRES on the GPU; returns (x, iterations, ||b - A x|| / ||b||)."""
+    ctx = context or default_context()
+    A = np.asarray(A, np.float64)
+    n = A.shape[0]
+    Ac = np.ascontiguousarray(A.T).ravel()            # column-major
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    it, rel = ctypes.c_int(), ctypes.c_double()
+    _check(lib().obs_solve_gmres_f64(ctx.handle, ctypes.c_int(n), _ptr(Ac), _ptr(b), _ptr(x), ctypes.c_double(tol),
+                                     ctypes.c_int(restart), ctypes.c_int(maxiter or 2 * n), ctypes.byref(it),
+                                     ctypes.byref(rel)), "obs_solve_gmres_f64")
+    return x, it.value, rel.value
+
+
+def solve_gmres_f64_dev(ctx: Context, A, b, x, tol: float = 1e-13, restart: int = 60, maxiter: int | None = None):
+    """Device FP64 GMRES (A column-major, x = initial guess in, solution out); returns
+    (iterations, relative residual)."""
+    it, rel = ctypes.c_int(), ctypes.c_double()
+    n = b.numel()
+    _check(lib().obs_solve_gmres_f64_dev(ctx.handle, ctypes.c_int(n), _ptr(A), _ptr(b), _ptr(x), ctypes.c_double(tol),
+                                         ctypes.c_int(restart), ctypes.c_int(maxiter or 2 * n), ctypes.byref(it),
+                                         ctypes.byref(rel)), "obs_solve_gmres_f64_dev")
+    return it.value, rel.value
+
+
 def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: ExecEnv | None = None,
-              reuse_matrix: bool = False) -> float:
+              reuse_matrix: bool = False, direct_lu: bool = False) -> float:
     """solve_bem for one fixed body (src/BEMHelper.h:43-260): sets bdry.vs (and bdry.ss for
     nunk == 2) from the particles' velocity and the freestream; returns the relative residual."""
     env = env or ExecEnv()
@@ -490,7 +518,8 @@ def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: E
     ss = np.zeros(bdry.npan, np.float32) if nunk == 2 else None
     rel = ctypes.c_double()
     st = lib().obs_solve_bem(env.ctx().handle, ctypes.c_int(nunk), ctypes.c_int(env.accum),
-                             ctypes.c_int(2 if reuse_matrix else 0), ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                             ctypes.c_int((2 if reuse_matrix else 0) | (4 if direct_lu else 0)),
+                             ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
                              ctypes.c_int(vort.n), _ptr(vort.x), _ptr(vort.y), _ptr(vort.s), *bdry._geo(),
                              _ptr(bdry.bcn), _ptr(vs), _ptr(ss), ctypes.byref(rel))
     _check(st, "obs_solve_bem")

@@ -131,6 +131,7 @@ const char* obs_status_string(int s) {
     case OBS_ERR_SINGULAR: return "singular matrix";
     case OBS_ERR_UNSUPPORTED: return "unsupported combination";
     case OBS_ERR_SCRATCH_LIMIT: return "size exceeds the fixed scratch of the no-allocation entry point";
+    case OBS_ERR_NO_CONVERGENCE: return "iterative solve did not reach its tolerance";
     default: return "unknown status";
   }
 }

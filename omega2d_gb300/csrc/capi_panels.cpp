@@ -348,6 +348,7 @@ int obs_solve_dense_f64_dev(obs_context* ctx, int n, const double* A, const doub
   if (e == cudaSuccess && x != b) e = cudaMemcpyAsync(x, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
   if (e != cudaSuccess) return obs::cuda_status(e);
   ctx->bem_n = 0;
+  ctx->bem_lu = false;
   obs::timing_begin(ctx);
   obs::timing_main_begin(ctx);
   s = obs::lu_factor_f64(ctx, n, lu, piv);
@@ -386,6 +387,40 @@ int obs_solve_dense_f64(obs_context* ctx, int n, const double* A, const double* 
  * flags & OBS_BEM_REUSE_MATRIX reuses the factorisation from the previous call of the same
  * order (the reference's is_A_current, src/BEM.h:49-51).  All arrays on the host.
  */
+int obs_solve_gmres_f64_dev(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol,
+                            int restart, int maxiter, int* iterations, double* rel_residual) {
+  if (!ctx || n <= 0 || !A || !b || !x || !(tol > 0.0) || restart <= 0 || maxiter <= 0) return OBS_ERR_ARG;
+  int s = obs::bind(ctx);
+  if (s) return s;
+  s = obs::gmres_f64(ctx, n, A, b, x, tol, restart, maxiter, iterations, rel_residual);
+  if (s && s != OBS_ERR_NO_CONVERGENCE) return s;
+  const int d = obs::take_device_status(ctx);
+  return d ? d : s;
+}
+
+int obs_solve_gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol,
+                        int restart, int maxiter, int* iterations, double* rel_residual) {
+  if (!ctx || n <= 0 || !A || !b || !x || !(tol > 0.0) || restart <= 0 || maxiter <= 0) return OBS_ERR_ARG;
+  int s = obs::bind(ctx);
+  if (s) return s;
+  const size_t nn = (size_t)n * n;
+  Stage g(ctx);
+  g.reserve(nn * 8);
+  g.reserve((size_t)n * 8);
+  g.reserve((size_t)n * 8);
+  if ((s = g.commit())) return s;
+  const double* dA = g.take(A, nn);
+  const double* db = g.take(b, (size_t)n);
+  double* dx = g.take(static_cast<const double*>(x), (size_t)n);
+  if (g.err) return obs::cuda_status(g.err);
+  s = obs::gmres_f64(ctx, n, dA, db, dx, tol, restart, maxiter, iterations, rel_residual);
+  if (s && s != OBS_ERR_NO_CONVERGENCE) return s;
+  const int d = obs::take_device_status(ctx);
+  if (d) return d;
+  const int c = copy_back(ctx, {{x, {dx, (size_t)n * 8}}});
+  return c ? c : s;
+}
+
 int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
                   int ns, const float* sx, const float* sy, const float* ss,
                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
@@ -399,7 +434,10 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   if ((s = obs::bind(ctx))) return s;
   const int n = npan * nunk;
   const size_t nn = (size_t)n * n;
-  const bool reuse = (flags & 2) && ctx->bem_n == n;
+  const bool use_lu = (flags & OBS_BEM_DIRECT_LU) != 0;
+  // ctx->dense: A (FP64, kept for reuse and residuals) | LU factors | pivots; bem_n > 0 marks a
+  // matrix of that order, bem_lu a factorisation of it
+  const bool reuse = (flags & OBS_BEM_REUSE_MATRIX) && ctx->bem_n == n && (!use_lu || ctx->bem_lu);
   Stage g(ctx);
   for (int k = 0; k < 3; ++k) g.reserve((size_t)ns * 4);
   for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
@@ -407,7 +445,6 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   for (int k = 0; k < 3; ++k) g.reserve((size_t)npan * 4);
   g.reserve((size_t)n * 8);   // rhs
   g.reserve((size_t)n * 8);   // x
-  g.reserve(reuse ? 0 : nn * 8);   // A (FP64)
   if ((s = g.commit())) return s;
   const float* dsx = g.take(sx, ns);
   const float* dsy = g.take(sy, ns);
@@ -421,7 +458,6 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   if (!bcn) g.take<float>(nullptr, npan);
   double* drhs = g.take<double>(nullptr, n);
   double* dx = g.take<double>(nullptr, n);
-  double* dA = reuse ? nullptr : g.take<double>(nullptr, nn);
   if (g.err) return obs::cuda_status(g.err);
   PanelSet ps{nnodes, dnx, dny, npan, didx};
   cudaError_t e = cudaSuccess;
@@ -440,33 +476,43 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   }
   if (!s) s = obs::run_vels_to_rhs(ctx, ps, nunk, dpu, dpv, dbc, nullptr, drhs);
   if (s) return s;
-  double* lu = nullptr;
-  int* piv = nullptr;
+  const size_t lu_bytes = use_lu ? nn * sizeof(double) : 0;
+  if (!reuse) {
+    ctx->bem_n = 0;
+    ctx->bem_lu = false;
+    s = ctx->dense.ensure(nn * sizeof(double) + lu_bytes + al((size_t)n * sizeof(int)) + 256, ctx->stream);
+    if (s) return s;
+  }
+  double* dA = ctx->dense.as<double>();
+  double* lu = ctx->dense.as<double>(nn * sizeof(double));
+  int* piv = ctx->dense.as<int>(nn * sizeof(double) + lu_bytes);
   if (!reuse) {
     s = obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
     if (s) return s;
-    s = ctx->dense.ensure(nn * sizeof(double) + al((size_t)n * sizeof(int)) + 256, ctx->stream);
-    if (s) return s;
-    lu = ctx->dense.as<double>();
-    piv = ctx->dense.as<int>(nn * sizeof(double));
-    e = cudaMemcpyAsync(lu, dA, nn * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+    ctx->bem_n = n;
+  }
+  if (use_lu) {
+    if (!reuse) {
+      e = cudaMemcpyAsync(lu, dA, nn * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+      if (e != cudaSuccess) return obs::cuda_status(e);
+      if ((s = obs::lu_factor_f64(ctx, n, lu, piv))) return s;
+      ctx->bem_lu = true;
+    }
+    e = cudaMemcpyAsync(dx, drhs, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream);
     if (e != cudaSuccess) return obs::cuda_status(e);
-    ctx->bem_n = 0;
-    s = obs::lu_factor_f64(ctx, n, lu, piv);
+    s = obs::lu_solve_f64(ctx, n, lu, piv, dx);
+    if (!s) s = obs::take_device_status(ctx);
+    if (!s && rel_residual) s = obs::residual_f64(ctx, n, dA, dx, drhs, rel_residual);
     if (s) return s;
   } else {
-    lu = ctx->dense.as<double>();
-    piv = ctx->dense.as<int>(nn * sizeof(double));
-  }
-  e = cudaMemcpyAsync(dx, drhs, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream);
-  if (e != cudaSuccess) return obs::cuda_status(e);
-  s = obs::lu_solve_f64(ctx, n, lu, piv, dx);
-  if (!s) s = obs::take_device_status(ctx);
-  if (s) return s;
-  ctx->bem_n = n;
-  if (rel_residual) {
-    if (reuse) *rel_residual = -1.0;   // the unfactored matrix is not kept
-    else if ((s = obs::residual_f64(ctx, n, dA, dx, drhs, rel_residual))) return s;
+    // the reference's method (src/BEM.h:169-234), in FP64: GMRES from a zero guess
+    e = cudaMemsetAsync(dx, 0, (size_t)n * 8, ctx->stream);
+    if (e != cudaSuccess) return obs::cuda_status(e);
+    double rel = 0.0;
+    s = obs::gmres_f64(ctx, n, dA, drhs, dx, 1e-13, std::min(n, 60), 2 * n, nullptr, &rel);
+    if (rel_residual) *rel_residual = rel;
+    if (!s) s = obs::take_device_status(ctx);
+    if (s) return s;
   }
   std::vector<double> hx(n);
   e = cudaMemcpyAsync(hx.data(), dx, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream);

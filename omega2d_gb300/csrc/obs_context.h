@@ -58,7 +58,8 @@ struct obs_context {
   obs::DevBuf state;     // time stepping: stage velocities, segment positions, adjoint vectors
   obs::DevBuf tape;      // recorded forward run: radii, strengths, checkpoints
   obs::AdvectTape tape_info;
-  int bem_n = 0;         // order of the factored BEM matrix held in `dense` (0: none)
+  int bem_n = 0;         // order of the BEM matrix held in `dense` (0: none)
+  bool bem_lu = false;   // `dense` also holds its LU factorisation
   int* d_status = nullptr;   // device status block: DEV_ERR_* bits + first failure record
   int last_failure[4] = {0, 0, 0, 0};   // copy of the block at the last synchronize that saw one
   obs::Timing timing;

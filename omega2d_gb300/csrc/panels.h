@@ -34,6 +34,10 @@ int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float*
 // pivot rows.  rel_residual (optional) = ||A x - b|| / ||b|| using the unfactored A.
 int lu_factor_f64(obs_context* ctx, int n, double* lu, int* piv);
 int lu_solve_f64(obs_context* ctx, int n, const double* lu, const int* piv, double* x /* in: b, out: x */);
+// Restarted GMRES in FP64 (gmres.cu): x in = initial guess, out = solution; OBS_ERR_NO_CONVERGENCE
+// when maxiter iterations end above tol (relative residual ||b - A x|| / ||b||).
+int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol, int restart,
+              int maxiter, int* iters_out, double* rel_residual);
 int residual_f64(obs_context* ctx, int n, const double* A, const double* x, const double* b, double* rel_residual);
 
 }  // namespace obs

@@ -128,8 +128,9 @@ def _restated_bem(restatement, surf, x, y, s, fs, nunk):
     return np.linalg.solve(A, rhs)
 
 
+@pytest.mark.parametrize("direct_lu", [False, True])
 @pytest.mark.parametrize("nunk", [2, 1])
-def test_solve_bem_matches_fp64_restatement(ctx, restatement, nunk):
+def test_solve_bem_matches_fp64_restatement(ctx, restatement, nunk, direct_lu):
     rng = np.random.default_rng(41)
     surf = og.circle_panels(512)
     n = 20_000
@@ -138,7 +139,8 @@ def test_solve_bem_matches_fp64_restatement(ctx, restatement, nunk):
     x, y = (r * np.cos(a)).astype(np.float32), (r * np.sin(a)).astype(np.float32)
     s = rng.normal(0, 1e-2, n).astype(np.float32)
     vort = og.Points(x, y, np.full(n, 0.01, np.float32), s)
-    rel = og.solve_bem(vort, surf, fs=(1.0, 0.0), nunk=nunk, env=og.ExecEnv(accum=og.COMPENSATED, context=ctx))
+    rel = og.solve_bem(vort, surf, fs=(1.0, 0.0), nunk=nunk, env=og.ExecEnv(accum=og.COMPENSATED, context=ctx),
+                       direct_lu=direct_lu)
     assert rel < 1e-12
     xr = _restated_bem(restatement, surf, x, y, s, (1.0, 0.0), nunk)
     got = np.stack([surf.vs, surf.ss], 1).ravel() if nunk == 2 else surf.vs
@@ -148,7 +150,7 @@ def test_solve_bem_matches_fp64_restatement(ctx, restatement, nunk):
     # reuse the factorisation: same answer
     vs0 = surf.vs.copy()
     og.solve_bem(vort, surf, fs=(1.0, 0.0), nunk=nunk, env=og.ExecEnv(accum=og.COMPENSATED, context=ctx),
-                 reuse_matrix=True)
+                 reuse_matrix=True, direct_lu=direct_lu)
     np.testing.assert_allclose(surf.vs, vs0, rtol=0, atol=1e-6 * np.max(np.abs(vs0)))
 
 
@@ -162,3 +164,36 @@ def test_solve_bem_cylinder_in_uniform_flow(ctx):
     th = -2 * np.pi * (np.arange(npan) + 0.5) / npan
     assert np.max(np.abs(np.abs(surf.vs) - 2.0 * np.abs(np.sin(th)))) < 5e-3
     assert np.max(np.abs(surf.ss)) < 5e-3
+
+
+def test_gmres_and_lu_agree_on_the_bem_system(ctx):
+    rng = np.random.default_rng(77)
+    surf = og.circle_panels(1024)
+    n = 30_000
+    r = np.sqrt(rng.uniform(0.55 ** 2, 9.0, n))
+    a = rng.uniform(0, 2 * np.pi, n)
+    vort = og.Points((r * np.cos(a)).astype(np.float32), (r * np.sin(a)).astype(np.float32),
+                     np.full(n, 0.01, np.float32), rng.normal(0, 1e-2, n).astype(np.float32))
+    env = og.ExecEnv(accum=og.COMPENSATED, context=ctx)
+    og.solve_bem(vort, surf, fs=(0.3, -0.2), env=env)
+    g = np.concatenate([surf.vs, surf.ss])
+    og.solve_bem(vort, surf, fs=(0.3, -0.2), env=env, direct_lu=True)
+    d = np.concatenate([surf.vs, surf.ss])
+    assert rel_err(d, g) < 1e-6       # both FP64 solves of one FP64 matrix; outputs are FP32
+
+
+def test_gmres_dense_and_no_convergence(ctx):
+    rng = np.random.default_rng(78)
+    n = 700
+    A = np.eye(n) * 4.0 + rng.normal(0, 1.0 / np.sqrt(n), (n, n))
+    xt = rng.normal(size=n)
+    b = A @ xt
+    x, it, rel = og.solve_gmres_f64(A, b, tol=1e-13, restart=50, context=ctx)
+    assert rel < 1e-13 and it < 100
+    assert np.max(np.abs(x - xt)) < 1e-10 * np.max(np.abs(xt))
+    # restart from the solution: converged on entry
+    x2, it2, rel2 = og.solve_gmres_f64(A, b, x0=x, tol=1e-12, context=ctx)
+    assert it2 == 0 and rel2 < 1e-12
+    with pytest.raises(og.EngineError) as ei:
+        og.solve_gmres_f64(A, b, tol=1e-15, restart=3, maxiter=4, context=ctx)
+    assert ei.value.status == -9
