@@ -635,7 +635,8 @@ def run_rk2adjoint2M(args):
         torch.cuda.synchronize()
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         e[0].record(stream)
-        og.advect_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, K)
+        # the forward op records its checkpoints for the backward op
+        og.advect_record_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, K, every)
         e[1].record(stream)
         e[1].synchronize()
         # loss and its seed on the host in FP64 (the loss is not part of the engine)
@@ -658,8 +659,7 @@ def run_rk2adjoint2M(args):
         LY = torch.from_numpy(gyT.astype(np.float32)).to(dev)
         torch.cuda.synchronize()
         e[2].record(stream)
-        peak = og.advect_vjp_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X0, Y0, R, S, (0.0, 0.0), dt, K, every, LX, LY,
-                                 GS, GX, GY)
+        peak = og.advect_vjp_tape_dev(ctx, LX, LY, GS, GX, GY)
         e[3].record(stream)
         e[3].synchronize()
     ctx.synchronize()
@@ -670,7 +670,8 @@ def run_rk2adjoint2M(args):
            "unit": UNIT, "data": "synthetic (seed 5)", "n": n, "rk2_steps": K, "dt": dt, "checkpoint_every": every,
            "forward_ms": f_ms, "forward_ginter_s": evals / (f_ms * 1e-3) / 1e9,
            "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
-           "adjoint_note": "recomputes the trajectory from checkpoints (2K velocity sums) and runs 2K self VJP gathers",
+           "adjoint_note": "from the recorded checkpoints: recomputes each segment (about 2K velocity sums) and "
+                           "runs 2K self-interaction VJP gathers",
            "value": evals / (f_ms * 1e-3) / 1e9, "loss": L, "grad_strength_norm": float(np.linalg.norm(gs)),
            "grad_strength_finite": bool(np.isfinite(gs).all()),
            "peak_hbm_bytes": {"engine": int(peak), "caller_tensors": int(torch.cuda.max_memory_allocated(dev))},

@@ -607,6 +607,15 @@ def points_affect_points_vjp_self(p: Points, lu, lv, env: ExecEnv | None = None)
     return gx, gy, gs
 
 
+def points_affect_points_vjp_self_dev(ctx: Context, core: int, accum: int, x, y, r, s, lu, lv, gx=None, gy=None,
+                                      gs=None):
+    """Device-resident self-interaction backward (CUDA tensors), asynchronous; outputs accumulate."""
+    _check(lib().obs_points_affect_points_vjp_self_dev(ctx.handle, ctypes.c_int(core), ctypes.c_int(accum),
+                                                       ctypes.c_int(x.numel()), _ptr(x), _ptr(y), _ptr(r), _ptr(s),
+                                                       _ptr(lu), _ptr(lv), _ptr(gx), _ptr(gy), _ptr(gs)),
+           "obs_points_affect_points_vjp_self_dev")
+
+
 def advect(p: Points, fs=(0.0, 0.0), dt: float = 0.01, nsteps: int = 1, order: int = 2,
            env: ExecEnv | None = None):
     """Convection::advect_1st (order 1), advect_2nd_ralston (2), advect_3rd (3) or

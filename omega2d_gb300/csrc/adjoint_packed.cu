@@ -397,7 +397,10 @@ __global__ void pa_reduce_kernel(const PAArgs a) {
 #ifndef OBS_PA_SRC_NP
 #define OBS_PA_SRC_NP 2
 #endif
-constexpr int pa_np(int mode) { return mode == PA_SRC ? OBS_PA_SRC_NP : 1; }
+#ifndef OBS_PA_SELF_NP
+#define OBS_PA_SELF_NP 1
+#endif
+constexpr int pa_np(int mode) { return mode == PA_SRC ? OBS_PA_SRC_NP : OBS_PA_SELF_NP; }
 
 cudaError_t pa_dispatch(int mode, bool thick, bool comp, const PAArgs* a, int grid, cudaStream_t st, int* occ) {
   auto run = [&](auto kern) -> cudaError_t {
