@@ -138,6 +138,25 @@ def aggregate_rate(units_per_rank: float, world_size: int, max_ms: float) -> flo
     return world_size * units_per_rank / (max_ms * 1e-3) / 1e9
 
 
+def time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args):
+    """Velocity + velocity gradient of the headline patch (VELANDGRAD, generic kernel):
+    one timed call per accumulation mode after one warm-up, CUDA events, L2 flushed."""
+    n = X.numel()
+    U, V = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    G = [torch.zeros(n, device=dev) for _ in range(4)]
+    out = {"kernel": "p2p_kernel<GAUSS, thick, VELANDGRAD> (generic)", "flops_per_interaction": 41}
+    for name, accum in (("compensated", og.COMPENSATED), ("plain", og.PLAIN_F32)):
+        def call():
+            for t in (U, V, *G):
+                t.zero_()
+            og.points_affect_points_dev(ctx, og.CORE_GAUSSIAN, og.VELANDGRAD, accum, X, Y, R, S, X, Y, R, U, V,
+                                        extra=G)
+        ms = _event_time(torch, stream, flush, call, 1, 1)
+        out[name] = {"ms": ms, "ginter_s": float(n) * n / (ms * 1e-3) / 1e9}
+        out["_grad_" + name] = [t.cpu().numpy() for t in G]
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -321,6 +340,7 @@ def run_engine(args):
         ms_comp, main_comp, launches = timed(og.COMPENSATED, args.steps, args.warmup)
         ms_plain, main_plain, _ = timed(og.PLAIN_F32, max(1, args.steps // 2), 1)
         adjoint, adj_launches, adj_host = time_adjoint(og, torch, ctx, stream, dev, flush, args.steps, args.warmup)
+        gradient = time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args)
     clocks = clk.summary()
 
     # end to end through the host-pointer C ABI call (copies in the timed region)
@@ -359,6 +379,13 @@ def run_engine(args):
         got = np.concatenate([TU.cpu().numpy()[sub], TV.cpu().numpy()[sub]])
         mx, rms = rel_errs(ref64, got)
         prec[name] = {"max_rel": mx, "rms_rel": rms}
+    # velocity-gradient precision on the same 1024 targets (du/dx, dv/dx, du/dy, dv/dy)
+    _, _, g64 = orc.points_affect_points(po.GAUSS, po.VELANDGRAD, x, y, r, s, x[sub], y[sub], r[sub], fp64=True)
+    ref_g = np.concatenate(g64)
+    for name in ("compensated", "plain"):
+        got = np.concatenate([a[sub] for a in gradient.pop("_grad_" + name)])
+        mx, rms = rel_errs(ref_g, got)
+        gradient[name]["max_rel"], gradient[name]["rms_rel"] = mx, rms
     # backward precision: the FP64 reference adjoint for 1024 seeded sources, with the same
     # cotangents (twice the engine's probe velocities)
     asx, asy, asr, ass, apx, apy, apu, apv, agx, agy, ags = adj_host
@@ -403,6 +430,7 @@ def run_engine(args):
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": f"{args.cpu_sample} seeded targets x {N} sources"},
         "adjoint": adjoint,
+        "gradient": gradient,
         "gpu_launches": launches,
         "clocks": clocks,
     }

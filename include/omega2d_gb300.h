@@ -249,6 +249,24 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
                   float* vs_out, float* ss_out, double* rel_residual);
 
+/* Rotation augmentation (src/Coefficients.h:429-572, src/BEMHelper.h:114-135, 197-205): the self
+ * block of one body gains a bottom row of panel lengths (under the vortex unknowns), a right
+ * column of the unit-rotation velocity along each panel (Surfaces::add_unit_rot_strengths about
+ * the body's centroid, their panels_affect_panels velocity, finalized) and the corner 2 * area
+ * (Surfaces::set_geom_center).  obs_panels_on_panels_coeff_augmented returns that
+ * (nunk*npan+1)^2 column-major block in FP64 and geom = (area, centroid x, centroid y);
+ * obs_solve_bem_augmented solves it with circ_rhs as the extra right-hand side (the
+ * reference's self + re-absorbed circulation + previous error) and returns the body's rotation
+ * rate in omega_out. */
+int obs_panels_on_panels_coeff_augmented(obs_context* ctx, int nunk, int accum, int nnodes, const float* nx,
+                                         const float* ny, int npan, const unsigned* idx, double* A64,
+                                         double* geom);
+int obs_solve_bem_augmented(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                            int ns, const float* sx, const float* sy, const float* ss,
+                            int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                            const float* bcn, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
+                            double* rel_residual);
+
 /*
  * Reverse mode (no counterpart in the reference, which has no adjoint).  Cotangents lu, lv are
  * on the FINALIZED velocities u = fs + (1/2 pi) sum (OBS_FLAG_FINALIZE); gradient outputs are

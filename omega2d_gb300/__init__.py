@@ -576,6 +576,40 @@ def solve_dense_f64_dev(ctx: Context, A, b, x) -> float:
     return rel.value
 
 
+def panels_on_panels_coeff_augmented(body: Surfaces, nunk: int = 2, accum: int = COMPENSATED,
+                                     context: Context | None = None):
+    """The rotation-augmented self block of one body (src/Coefficients.h:429-572) as an
+    (nunk*npan+1)^2 (rows, cols) FP64 array, and (area, centroid x, centroid y)."""
+    ctx = context or default_context()
+    m = body.npan * nunk + 1
+    out = np.zeros(m * m)
+    geom = np.zeros(3)
+    _check(lib().obs_panels_on_panels_coeff_augmented(ctx.handle, ctypes.c_int(nunk), ctypes.c_int(accum),
+                                                      *body._geo(), _ptr(out), _ptr(geom)),
+           "obs_panels_on_panels_coeff_augmented")
+    return out.reshape(m, m).T.copy(), tuple(geom)
+
+
+def solve_bem_augmented(vort: Points, bdry: Surfaces, circ_rhs: float = 0.0, fs=(0.0, 0.0), nunk: int = 2,
+                        env: ExecEnv | None = None, direct_lu: bool = False):
+    """solve_bem with the rotation augmentation (src/BEMHelper.h:114-135): sets bdry.vs (and
+    bdry.ss) and returns (rotation rate, relative residual)."""
+    env = env or ExecEnv()
+    vs = np.zeros(bdry.npan, np.float32)
+    ss = np.zeros(bdry.npan, np.float32) if nunk == 2 else None
+    om, rel = ctypes.c_double(), ctypes.c_double()
+    _check(lib().obs_solve_bem_augmented(env.ctx().handle, ctypes.c_int(nunk), ctypes.c_int(env.accum),
+                                         ctypes.c_int(4 if direct_lu else 0), ctypes.c_double(fs[0]),
+                                         ctypes.c_double(fs[1]), ctypes.c_int(vort.n), _ptr(vort.x), _ptr(vort.y),
+                                         _ptr(vort.s), *bdry._geo(), _ptr(bdry.bcn), ctypes.c_double(circ_rhs),
+                                         _ptr(vs), _ptr(ss), ctypes.byref(om), ctypes.byref(rel)),
+           "obs_solve_bem_augmented")
+    bdry.vs = vs
+    if ss is not None:
+        bdry.ss = ss
+    return om.value, rel.value
+
+
 # ---------------------------------------------------------------- reverse mode and time stepping
 
 def points_affect_points_vjp(src: Points, targ: Points, lu, lv, env: ExecEnv | None = None,

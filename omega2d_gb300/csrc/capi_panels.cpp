@@ -421,10 +421,18 @@ int obs_solve_gmres_f64(obs_context* ctx, int n, const double* A, const double* 
   return c ? c : s;
 }
 
-int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
-                  int ns, const float* sx, const float* sy, const float* ss,
-                  int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
-                  float* vs_out, float* ss_out, double* rel_residual) {
+}  // extern "C"
+
+namespace {
+
+// solve_bem for one body (src/BEMHelper.h:43-260); with `augment`, the system gains the rotation
+// row and column (src/Coefficients.h:429-572) and the right-hand side the circulation value
+// circ_rhs (src/BEMHelper.h:114-135); the extra unknown is the body's rotation rate.
+int solve_bem_impl(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                   int ns, const float* sx, const float* sy, const float* ss,
+                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
+                   bool augment, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
+                   double* rel_residual) {
   if (!ctx || (nunk != 1 && nunk != 2) || npan <= 0 || !vs_out || (nunk == 2 && !ss_out)) return OBS_ERR_ARG;
   if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
   int s = check_panels(nnodes, nx, ny, npan, idx);
@@ -432,12 +440,13 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   if (ns < 0 || (ns > 0 && (!sx || !sy || !ss))) return OBS_ERR_ARG;
   if ((s = check_host_idx(nnodes, npan, idx))) return s;
   if ((s = obs::bind(ctx))) return s;
-  const int n = npan * nunk;
+  const int nb = npan * nunk;               // panel unknowns
+  const int n = nb + (augment ? 1 : 0);     // system order
   const size_t nn = (size_t)n * n;
   const bool use_lu = (flags & OBS_BEM_DIRECT_LU) != 0;
   // ctx->dense: A (FP64, kept for reuse and residuals) | LU factors | pivots; bem_n > 0 marks a
   // matrix of that order, bem_lu a factorisation of it
-  const bool reuse = (flags & OBS_BEM_REUSE_MATRIX) && ctx->bem_n == n && (!use_lu || ctx->bem_lu);
+  const bool reuse = !augment && (flags & OBS_BEM_REUSE_MATRIX) && ctx->bem_n == n && (!use_lu || ctx->bem_lu);
   Stage g(ctx);
   for (int k = 0; k < 3; ++k) g.reserve((size_t)ns * 4);
   for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
@@ -476,6 +485,11 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   }
   if (!s) s = obs::run_vels_to_rhs(ctx, ps, nunk, dpu, dpv, dbc, nullptr, drhs);
   if (s) return s;
+  if (augment) {
+    e = cudaMemcpyAsync(drhs + nb, &circ_rhs, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // circ_rhs is a stack value
+    if (e != cudaSuccess) return obs::cuda_status(e);
+  }
   const size_t lu_bytes = use_lu ? nn * sizeof(double) : 0;
   if (!reuse) {
     ctx->bem_n = 0;
@@ -487,9 +501,15 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
   double* lu = ctx->dense.as<double>(nn * sizeof(double));
   int* piv = ctx->dense.as<int>(nn * sizeof(double) + lu_bytes);
   if (!reuse) {
-    s = obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
+    if (augment) {
+      double vol, cx, cy;
+      obs::geom_center_host(nnodes, nx, ny, npan, idx, &vol, &cx, &cy);
+      s = obs::run_panels_on_panels_coeff_augmented(ctx, ps, nunk, accum, vol, cx, cy, dA);
+    } else {
+      s = obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
+    }
     if (s) return s;
-    ctx->bem_n = n;
+    ctx->bem_n = augment ? 0 : n;   // an augmented matrix is not offered for reuse
   }
   if (use_lu) {
     if (!reuse) {
@@ -526,7 +546,61 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
       vs_out[i] = (float)hx[i];
     }
   }
+  if (augment && omega_out) *omega_out = hx[nb];
   return OBS_OK;
+}
+
+
+}  // namespace
+
+extern "C" {
+
+int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                  int ns, const float* sx, const float* sy, const float* ss,
+                  int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
+                  float* vs_out, float* ss_out, double* rel_residual) {
+  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, false, 0.0,
+                        vs_out, ss_out, nullptr, rel_residual);
+}
+
+int obs_solve_bem_augmented(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                            int ns, const float* sx, const float* sy, const float* ss,
+                            int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                            const float* bcn, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
+                            double* rel_residual) {
+  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, true,
+                        circ_rhs, vs_out, ss_out, omega_out, rel_residual);
+}
+
+int obs_panels_on_panels_coeff_augmented(obs_context* ctx, int nunk, int accum, int nnodes, const float* nx,
+                                         const float* ny, int npan, const unsigned* idx, double* A64,
+                                         double* geom) {
+  if (!ctx || (nunk != 1 && nunk != 2) || npan <= 0 || !A64) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  const int n = npan * nunk + 1;
+  const size_t nn = (size_t)n * n;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  g.reserve(nn * 8);
+  if ((s = g.commit())) return s;
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  double* dA = g.take<double>(nullptr, nn);
+  if (g.err) return obs::cuda_status(g.err);
+  double vol, cx, cy;
+  obs::geom_center_host(nnodes, nx, ny, npan, idx, &vol, &cx, &cy);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  s = obs::run_panels_on_panels_coeff_augmented(ctx, ps, nunk, accum, vol, cx, cy, dA);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  if (geom) { geom[0] = vol; geom[1] = cx; geom[2] = cy; }
+  return copy_back(ctx, {{A64, {dA, nn * 8}}});
 }
 
 }  // extern "C"

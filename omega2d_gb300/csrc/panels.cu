@@ -66,7 +66,11 @@ __device__ __forceinline__ void panel_uv_star(float4 P, float tx, float ty, floa
   us = atan2f(dy0 * dx1 - dx0 * dy1, dx0 * dx1 + dy0 * dy1);
   const float r1 = dx1 * dx1 + dy1 * dy1;
   const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
-  vs = 0.5f * log1pf(diff / r1);
+  // log(r0^2 / r1^2) in whichever form is well conditioned: log1p of the difference quotient
+  // when the ratio is near 1 (far from the panel), the ratio itself when the target is much
+  // closer to node 0 than to node 1 (there 1 + diff/r1 would cancel)
+  const float q = diff / r1;
+  vs = (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
 }
 
 // kernelu_1vs_0p (vortex + source sheet) on one target; ss = 0 gives kernelu_1v_0p.

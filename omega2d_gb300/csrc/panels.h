@@ -24,6 +24,12 @@ int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const fl
 // panels_affect_panels (src/Influence.h:774-795) through the reference's collocation points
 int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
                              int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv);
+// Rotation augmentation of one body's self block (src/Coefficients.h:429-572): Aa receives the
+// (n+1)^2 column-major block, n = npan * nunk; vol, (cx, cy) from geom_center_host.
+void geom_center_host(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, double* vol,
+                      double* cx, double* cy);
+int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, int nunk, int accum, double vol,
+                                         double cx, double cy, double* Aa);
 int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const PanelSet& targ, int nunk, int self,
                                float* A32, double* A64);
 int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,

@@ -1,4 +1,5 @@
-// panels_pap.cu -- panels_affect_panels (src/Influence.h:774-795) on the device.
+// panels_pap.cu -- panels_affect_panels (src/Influence.h:774-795) on the device, and the
+// rotation augmentation of the BEM self block that uses it (src/Coefficients.h:429-572).
 //
 // The reference evaluates panel-on-panel velocities through temporary collocation points:
 // Surfaces::represent_as_particles(1e-4, -1) (src/Surfaces.h:830-876) puts
@@ -8,6 +9,8 @@
 // the first npan point velocities are added to the npan panel velocities, index by index.
 // Here one block builds the first npan points (a block-wide scan of the per-panel counts) and
 // the panel kernel of panels.cu accumulates straight into the panel velocities.
+#include <cmath>
+
 #include "obs_context.h"
 #include "obs_device.cuh"
 #include "panels.h"
@@ -85,7 +88,107 @@ __global__ void __launch_bounds__(1024) collocation_kernel(const float* __restri
   }
 }
 
+// Surfaces::add_rot_strengths_base with unit rotation (src/Surfaces.h:566-605): per panel, the
+// vortex and source strengths whose sheet reproduces solid-body rotation about (cx, cy)
+__global__ void unit_rot_strengths_kernel(const float* __restrict__ nx, const float* __restrict__ ny, int nnodes,
+                                          const unsigned* __restrict__ idx, int npan, float cx, float cy,
+                                          float* __restrict__ vs, float* __restrict__ ss, int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npan) return;
+  const PanelGeom g = panel_geom(nx, ny, idx, nnodes, i, status);
+  const float dx = (float)(0.5 * (double)(g.x0 + g.x1) - (double)cx);
+  const float dy = (float)(0.5 * (double)(g.y0 + g.y1) - (double)cy);
+  const float ui = -dy, vi = dx;
+  const float oop = (float)(1.0 / (double)g.len);
+  const float px = (g.x1 - g.x0) * oop, py = (g.y1 - g.y0) * oop;
+  vs[i] = (float)(-1.0 * (double)(ui * px + vi * py));
+  ss[i] = (float)(-1.0 * (double)(ui * py - vi * px));
+}
+
+// (n+1) x (n+1) column-major augmented block from the n x n block An (src/Coefficients.h:429-572):
+// bottom row = panel lengths under the vortex unknowns, right column = the unit-rotation panel
+// velocity along each target panel's tangent (and normal for the source unknowns), corner 2 vol
+__global__ void augment_kernel(const double* __restrict__ An, int n, int nunk, const float* __restrict__ nx,
+                               const float* __restrict__ ny, int nnodes, const unsigned* __restrict__ idx,
+                               const float* __restrict__ pu, const float* __restrict__ pv, double vol,
+                               double* __restrict__ Aa, int* status) {
+  const int np1 = n + 1;
+  const size_t total = (size_t)np1 * np1;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / np1), i = (int)(k % np1);
+    double v;
+    if (i < n && j < n) {
+      v = An[(size_t)j * n + i];
+    } else if (i == n && j < n) {
+      const int pj = (nunk == 1) ? j : j / 2;
+      v = (nunk == 1 || (j % 2) == 0) ? (double)panel_geom(nx, ny, idx, nnodes, pj, status).len : 0.0;
+    } else if (j == n && i < n) {
+      const int pi = (nunk == 1) ? i : i / 2;
+      const PanelGeom g = panel_geom(nx, ny, idx, nnodes, pi, status);
+      const float tx = g.ny, ty = -g.nx;   // tangent from the normal (n = (-t_y, t_x))
+      const bool tang = (nunk == 1) || (i % 2) == 0;
+      v = tang ? (double)(pu[pi] * tx + pv[pi] * ty) : (double)(pu[pi] * g.nx + pv[pi] * g.ny);
+    } else {
+      v = 2.0 * vol;
+    }
+    Aa[k] = v;
+  }
+}
+
 }  // namespace
+
+// Surfaces::set_geom_center (src/Surfaces.h:623-678) on the host: signed triangle areas from the
+// origin accumulated in double; returns the enclosed area and its centroid
+void geom_center_host(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, double* vol,
+                      double* cx, double* cy) {
+  double asum = 0.0, xsum = 0.0, ysum = 0.0;
+  for (int i = 0; i < npan; ++i) {
+    const unsigned j = idx[2 * i], jp1 = idx[2 * i + 1];
+    if (j >= (unsigned)nnodes || jp1 >= (unsigned)nnodes) continue;
+    const double xj = nx[j], yj = ny[j], xk = nx[jp1], yk = ny[jp1];
+    const double xc = (0.0 + xj + xk) / 3.0, yc = (0.0 + yj + yk) / 3.0;
+    const double px = xk - xj, py = yk - yj;
+    const double a = std::sqrt(xj * xj + yj * yj), b = std::sqrt(px * px + py * py), c = std::sqrt(xk * xk + yk * yk);
+    const double hs = 0.5 * (a + b + c);
+    const double a2 = hs * (hs - a) * (hs - b) * (hs - c);
+    double ar = a2 > 0.0 ? std::sqrt(a2) : 0.0;
+    if (yj * px - xj * py < 0.0) ar = -ar;
+    asum += ar;
+    xsum += xc * ar;
+    ysum += yc * ar;
+  }
+  *vol = (double)(float)asum;
+  *cx = (double)(float)(xsum / asum);
+  *cy = (double)(float)(ysum / asum);
+}
+
+int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, int nunk, int accum, double vol,
+                                         double cx, double cy, double* Aa) {
+  const int n = ps.npan * nunk;
+  const size_t N = (size_t)ps.npan;
+  const size_t nn = (size_t)n * n;
+  // state: An (n^2 doubles) | unit strengths vs, ss | induced pu, pv
+  int s = ctx->state.ensure(nn * 8 + 4 * N * 4 + 1024, ctx->stream);
+  if (s) return s;
+  double* An = ctx->state.as<double>();
+  float* vs = reinterpret_cast<float*>(An + nn);
+  float* ss = vs + N;
+  float* pu = ss + N;
+  float* pv = pu + N;
+  cudaStream_t st = ctx->stream;
+  unit_rot_strengths_kernel<<<(ps.npan + 255) / 256, 256, 0, st>>>(ps.nx, ps.ny, ps.nnodes, ps.idx, ps.npan,
+                                                                  (float)cx, (float)cy, vs, ss, ctx->d_status);
+  ctx->launches++;
+  cudaError_t e = cudaMemsetAsync(pu, 0, 2 * N * 4, st);
+  if (e != cudaSuccess) return cuda_status(e);
+  // the unit-rotation velocity at the body's own panels, finalized with zero freestream
+  if ((s = run_panels_affect_panels(ctx, ps, vs, ss, accum, OBS_FLAG_FINALIZE, 0.0, 0.0, ps, pu, pv))) return s;
+  if ((s = run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, An))) return s;
+  augment_kernel<<<2 * ctx->num_sms, 256, 0, st>>>(An, n, nunk, ps.nx, ps.ny, ps.nnodes, ps.idx, pu, pv, vol, Aa,
+                                                   ctx->d_status);
+  ctx->launches++;
+  return cuda_status(cudaGetLastError());
+}
 
 int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
                              int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv) {

@@ -440,6 +440,34 @@ int ref_panels_affect_panels_f(int snn, const float* snx, const float* sny, int 
   return 0;
 }
 
+// The augmented self block of one rotating-capable body (src/Coefficients.h:155-573 with the
+// preparation of src/BEMHelper.h:197-205): the reactive surface gets a Body, its geometric
+// centre and area (Surfaces::set_geom_center), the unit-rotation strengths, their induced
+// panel velocities (panels_affect_panels, finalized with zero freestream), then
+// panels_on_panels_coeff returns the (2 npan + 1)^2 column-major block.
+int ref_panels_on_panels_coeff_augmented_f(int nnodes, const float* nx, const float* ny, int npan,
+                                           const unsigned* idx, float* out, double* geom) {
+  Quiet q;
+  std::shared_ptr<Body> bp = std::make_shared<Body>();
+  std::vector<float> xy(2 * (size_t)nnodes);
+  for (int i = 0; i < nnodes; ++i) { xy[2*i] = nx[i]; xy[2*i+1] = ny[i]; }
+  std::vector<Int> id(idx, idx + 2 * (size_t)npan);
+  std::vector<float> val(2 * (size_t)npan, 0.0f);
+  ElementPacket<float> pk(xy, id, val, (size_t)npan, 1);
+  Surfaces<float> surf(pk, reactive, fixed, bp);
+  surf.set_geom_center();
+  surf.zero_vels();
+  surf.zero_strengths();
+  surf.add_unit_rot_strengths();
+  panels_affect_panels<float, double>(surf, surf, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  surf.zero_strengths();
+  surf.finalize_vels(std::array<double, Dimensions>({0.0, 0.0}));
+  Vector<float> c = panels_on_panels_coeff<float>(surf, surf);
+  std::copy(c.begin(), c.end(), out);
+  geom[0] = surf.get_vol();
+  return (int)c.size();
+}
+
 // flop counts the reference attaches to each kernel (src/Kernels.h flops*, src/CoreFunc.h flops_*)
 int ref_flop_counts(int* out) {
   out[0] = (int)flopsu_0v_0b<float, double>();

@@ -144,6 +144,31 @@ def make_extras(out):
     np.savez_compressed(out, **d)
 
 
+def make_augment(out):
+    """The reference's rotation-augmented self block (src/Coefficients.h:429-572, prepared as
+    src/BEMHelper.h:197-205 does) for a circle and an irregular closed polygon."""
+    import ctypes
+    ref = po.Reference(po.V2)
+    d = {}
+    rng = np.random.default_rng(20240605)
+    th = -2.0 * np.pi * np.sort(rng.uniform(0, 1, 40))
+    rad = 0.5 + 0.1 * np.sin(3 * th)
+    shapes = {"circle": circle_panels(48),
+              "poly": ((0.2 + rad * np.cos(th)).astype(np.float32), (-0.1 + rad * np.sin(th)).astype(np.float32),
+                       np.stack([np.arange(40), (np.arange(40) + 1) % 40], 1).ravel().astype(np.uint32))}
+    for name, (nx, ny, idx) in shapes.items():
+        npan = idx.size // 2
+        m = 2 * npan + 1
+        A = np.zeros(m * m, np.float32)
+        geom = np.zeros(4)
+        ref.lib.ref_panels_on_panels_coeff_augmented_f(ctypes.c_int(nx.size), po._p(nx), po._p(ny),
+                                                       ctypes.c_int(npan), po._p(idx), po._p(A), po._p(geom))
+        d[name + "_nx"], d[name + "_ny"], d[name + "_idx"] = nx, ny, idx
+        d[name + "_A"] = A.reshape(m, m).T.copy()     # (rows, cols)
+        d[name + "_vol"] = geom[:1]
+    np.savez_compressed(out, **d)
+
+
 def main():
     if not build_ref.available():
         raise SystemExit("the reference tree is needed to generate golden vectors")
@@ -152,6 +177,7 @@ def main():
     make_panels(os.path.join(HERE, "panels.npz"))
     make_advect(os.path.join(HERE, "advect.npz"))
     make_extras(os.path.join(HERE, "extras.npz"))
+    make_augment(os.path.join(HERE, "augment.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -197,3 +197,36 @@ def test_gmres_dense_and_no_convergence(ctx):
     with pytest.raises(og.EngineError) as ei:
         og.solve_gmres_f64(A, b, tol=1e-15, restart=3, maxiter=4, context=ctx)
     assert ei.value.status == -9
+
+
+@pytest.mark.parametrize("shape", ["circle", "poly"])
+def test_augmented_block_matches_reference(ctx, golden, shape):
+    g = golden("augment")
+    body = og.Surfaces(g[shape + "_nx"], g[shape + "_ny"], g[shape + "_idx"])
+    A, (vol, cx, cy) = og.panels_on_panels_coeff_augmented(body, context=ctx)
+    R = g[shape + "_A"].astype(np.float64)
+    assert abs(vol - g[shape + "_vol"][0]) < 1e-6 * abs(vol)
+    np.testing.assert_allclose(A[-1, :], R[-1, :], rtol=0, atol=1e-6 * np.max(np.abs(R[-1, :])))   # lengths, 2 area
+    # the rotation column comes through panels_affect_panels (collocation points 1e-4 off the panels)
+    assert rel_err(R[:-1, -1], A[:-1, -1]) < 2e-6
+    # the reference forms the block in FP32 (src/Coefficients.h:155-427)
+    assert rel_err(R[:-1, :-1], A[:-1, :-1]) < 3e-6
+
+
+def test_augmented_solve_circulation_and_rotation(ctx):
+    """A cylinder in uniform flow: with zero net circulation the solved rotation rate is ~0 and
+    the strengths match the plain solve; a prescribed circulation C gives sum(vs * len) = C."""
+    surf = og.circle_panels(512)
+    empty = og.Points(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0))
+    env = og.ExecEnv(accum=og.COMPENSATED, context=ctx)
+    og.solve_bem(empty, surf, fs=(1.0, 0.0), env=env)
+    vs0 = surf.vs.copy()
+    om, rel = og.solve_bem_augmented(empty, surf, circ_rhs=0.0, fs=(1.0, 0.0), env=env)
+    assert rel < 1e-12 and abs(om) < 1e-4
+    assert rel_err(vs0, surf.vs) < 1e-4
+    L = np.hypot(np.diff(np.append(surf.nx, surf.nx[0])), np.diff(np.append(surf.ny, surf.ny[0])))
+    om, rel = og.solve_bem_augmented(empty, surf, circ_rhs=0.7, fs=(1.0, 0.0), env=env)
+    A, (vol, _, _) = og.panels_on_panels_coeff_augmented(surf, context=ctx)
+    assert rel < 1e-12
+    # the bottom row of the system: sum(vs * len) + 2 area * omega = C
+    assert abs(np.sum(surf.vs.astype(np.float64) * L) + 2 * vol * om - 0.7) < 1e-4
