@@ -56,7 +56,7 @@ cudaError_t packed_dispatch_np(bool thick, bool comp, const P2PArgs* a, int grid
 }  // namespace
 
 bool packed_supported(int core, int res) {
-  return res == RES_VEL && (core == CORE_GAUSS || core == CORE_RM);
+  return res == RES_VEL && core >= CORE_RM && core <= CORE_CEXP;
 }
 
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
@@ -70,7 +70,14 @@ cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PAr
     return np == 4 ? packed_dispatch_np<CORE_RM, 4>(thick, comp, a, grid, st, occ)
                    : packed_dispatch_np<CORE_RM, 2>(thick, comp, a, grid, st, occ);
   }
-  return cudaErrorInvalidValue;
+  switch (core) {   // the other cores: 2 target pairs per thread
+    case CORE_V2: return packed_dispatch_np<CORE_V2, 2>(thick, comp, a, grid, st, occ);
+    case CORE_WL: return packed_dispatch_np<CORE_WL, 2>(thick, comp, a, grid, st, occ);
+    case CORE_V3: return packed_dispatch_np<CORE_V3, 2>(thick, comp, a, grid, st, occ);
+    case CORE_SING: return packed_dispatch_np<CORE_SING, 2>(thick, comp, a, grid, st, occ);
+    case CORE_CEXP: return packed_dispatch_np<CORE_CEXP, 2>(thick, comp, a, grid, st, occ);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, const int* perm,

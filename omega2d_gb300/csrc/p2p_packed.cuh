@@ -18,7 +18,10 @@
 // and skip the exponential.  Marked blocks evaluate all three branches, so a pair gets the same
 // value whichever path its warp takes.
 // Rosenhead-Moore core (src/CoreFunc.h:47-59): G K = G / (d^2 + s^2).
-// With varying radii the kernel evaluates the reference forms per target (scalar).
+// Vatistas n=2 (src/CoreFunc.h:238-274): G K = G / sqrt(d^4 + s^4); Winckelmans-Leonard
+// (:189-229): G K = G (dd + s^2) / dd^2.  Every other core, and every core with varying radii,
+// evaluates the reference forms per target (core_eval, scalar) inside the packed difference /
+// accumulation arithmetic.
 #pragma once
 
 #include "p2p_kernel.cuh"
@@ -113,6 +116,58 @@ __device__ __forceinline__ void rm_block(const float4* __restrict__ blk, const P
       float2 w = __ffma2_rn(ndy, ndy, q.s22);
       w = __ffma2_rn(ndx, ndx, w);
       const float2 k = f2(rcp_a(w.x), rcp_a(w.y));
+      const float2 r2 = __fmul2_rn(g2, k);
+      u[p] = __ffma2_rn(r2, ndy, u[p]);
+      vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+    }
+  }
+}
+
+// Vatistas n=2, uniform radii (src/CoreFunc.h:238-274): G K = G / sqrt(d^4 + s^4 (+ t^4))
+template <int NP>
+__device__ __forceinline__ void v2_block(const float4* __restrict__ blk, const PackedUni& q, const float2 (&ntx)[NP],
+                                         const float2 (&nty)[NP], float2 (&u)[NP], float2 (&vn)[NP]) {
+#pragma unroll 2
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+      const float2 ndy = __fadd2_rn(sy2, nty[p]);
+      float2 d2 = __fmul2_rn(ndy, ndy);
+      d2 = __ffma2_rn(ndx, ndx, d2);
+      const float2 a = __ffma2_rn(d2, d2, q.s22);
+      const float2 k = f2(rsqrt_a(a.x), rsqrt_a(a.y));
+      const float2 r2 = __fmul2_rn(g2, k);
+      u[p] = __ffma2_rn(r2, ndy, u[p]);
+      vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+    }
+  }
+}
+
+// Winckelmans-Leonard, uniform radii (src/CoreFunc.h:189-229): K = (dd + s^2) / dd^2, dd = d^2 + s^2
+template <int NP>
+__device__ __forceinline__ void wl_block(const float4* __restrict__ blk, const PackedUni& q, const float2 (&ntx)[NP],
+                                         const float2 (&nty)[NP], float2 (&u)[NP], float2 (&vn)[NP]) {
+#pragma unroll 2
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+      const float2 ndy = __fadd2_rn(sy2, nty[p]);
+      float2 d2 = __fmul2_rn(ndy, ndy);
+      d2 = __ffma2_rn(ndx, ndx, d2);
+      const float2 dd = __fadd2_rn(d2, q.s22);
+      const float2 dq = __fmul2_rn(dd, dd);
+      const float2 o = f2(rcp_a(dq.x), rcp_a(dq.y));
+      const float2 k = __fmul2_rn(__fadd2_rn(dd, q.s22), o);
       const float2 r2 = __fmul2_rn(g2, k);
       u[p] = __ffma2_rn(r2, ndy, u[p]);
       vn[p] = __ffma2_rn(r2, ndx, vn[p]);
@@ -262,9 +317,17 @@ p2p_packed_kernel(const P2PArgs a) {
           } else {
             general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
           }
-        } else {
+        } else if constexpr (CORE == CORE_RM) {
           if (unif) rm_block<NP>(blk, q, ntx, nty, u, vn);
           else general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+        } else if constexpr (CORE == CORE_V2) {
+          if (unif) v2_block<NP>(blk, q, ntx, nty, u, vn);
+          else general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+        } else if constexpr (CORE == CORE_WL) {
+          if (unif) wl_block<NP>(blk, q, ntx, nty, u, vn);
+          else general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+        } else {
+          general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
         }
         if constexpr (COMP) {
 #pragma unroll

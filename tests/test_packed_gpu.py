@@ -15,11 +15,16 @@ def cloud(rng, n, uniform):
     return x, y, r, s
 
 
-@pytest.mark.parametrize("core", [og.CORE_GAUSSIAN, og.CORE_RM])
+CORE_VARIANTS = ([(c, v) for c in (og.CORE_GAUSSIAN, og.CORE_RM)
+                  for v in (og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4)]
+                 + [(c, og.VARIANT_PACKED2) for c in (og.CORE_V2, og.CORE_WL, og.CORE_V3, og.CORE_SINGULAR,
+                                                      og.CORE_COMPACT_EXP)])
+
+
+@pytest.mark.parametrize("core,variant", CORE_VARIANTS)
 @pytest.mark.parametrize("thick", [True, False])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
 @pytest.mark.parametrize("uniform", [True, False])
-@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4])
 def test_packed_matches_generic_and_fp64(ctx, restatement, core, thick, accum, uniform, variant):
     rng = np.random.default_rng(core * 100 + thick * 10 + accum + 2 * uniform + variant)
     ns, nt = 5000, 3001
