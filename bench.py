@@ -157,6 +157,12 @@ def time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args):
     return out
 
 
+def workload_config() -> dict:
+    """The headline workload, named the same way by both arms."""
+    return {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian", "sigma": SIGMA,
+            "targets": "thick (the particles)", "seed": SEED, "l2": "flushed between steps (256 MB write)"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -275,8 +281,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs, f64 accum",
-            "data": "synthetic", "config": {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian",
-                                            "sigma": SIGMA, "targets_per_step": sample},
+            "data": "synthetic", "config": workload_config(),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": f"{sample} seeded targets x {N} sources per step"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -411,8 +416,7 @@ def run_engine(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_comp, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 pairs, compensated f32 + f64 reduce", "data": "synthetic",
-        "config": {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian", "sigma": SIGMA,
-                   "targets": "thick (the particles)", "seed": SEED, "l2": "flushed between steps (256 MB write)"},
+        "config": workload_config(),
         "plain_fp32": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain,
                        "compensated_over_plain": value / plain_value},
         "precision": prec,
