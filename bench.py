@@ -711,6 +711,180 @@ def run_rk2adjoint2M(args):
     print(json.dumps(out), flush=True)
 
 
+def run_rows(args):
+    """Every row of the hot-path scope on its own: device time (CUDA events, L2 flushed), the
+    interactions per second, the achieved FLOP/s at the reference's flop count per interaction
+    and its fraction of the FP32 peak (HBM peak for the GMRES matrix-vector products), and the
+    C restatement (float pairs, double sums, all host cores) on a target sample beside it."""
+    torch, og, dev, ctx, stream, flush = _engine_setup()
+    from oracle import pyoracle as po
+    orc = po.Restatement()
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    peaks = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz") or 2070.0
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = 2.0 * FMA_PER_CLK_PER_SM * nsm * sm_max * 1e6
+    hbm_peak = float(peaks.get("hbm_gbs") or 6800.0) * 1e9
+    n = 131072
+    x, y, r, s = make_workload(7, n)
+    T = {k: torch.from_numpy(v).to(dev) for k, v in dict(x=x, y=y, r=r, s=s).items()}
+    U, V = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    E = [torch.zeros(n, device=dev) for _ in range(4)]
+    rows = []
+
+    def cpu_rate(fn, pairs):
+        t0 = time.perf_counter()
+        fn()
+        return pairs / (time.perf_counter() - t0) / 1e9
+
+    def row(name, ref, fn, pairs, flops_per, cpu=None, bound="fp32", bytes_per_call=None):
+        ms = _event_time(torch, stream, flush, fn, args.steps, 1)
+        d = {"row": name, "reference": ref, "ms": round(ms, 4), "ginter_s": round(pairs / (ms * 1e-3) / 1e9, 1)}
+        if flops_per:
+            tf = pairs * flops_per / (ms * 1e-3)
+            d.update(flops_per_interaction=flops_per, tflops=round(tf / 1e12, 2), frac_fp32=round(tf / fp32_peak, 3))
+        if bytes_per_call:
+            bw = bytes_per_call / (ms * 1e-3)
+            d.update(gb_s=round(bw / 1e9, 1), frac_hbm=round(bw / hbm_peak, 3))
+        if cpu:
+            d["cpu_ginter_s"] = round(cpu, 3)
+        rows.append(d)
+
+    sub = np.random.default_rng(8).choice(n, 256, replace=False)
+    acc = og.COMPENSATED
+    cores = {"K1/C1 RM": og.CORE_RM, "K1/C2 Gaussian": og.CORE_GAUSSIAN, "K1/C3 Vatistas-2": og.CORE_V2,
+             "K1/C4 Winckelmans-Leonard": og.CORE_WL, "K1/C4 Vatistas-3": og.CORE_V3,
+             "K1/C5 singular": og.CORE_SINGULAR, "K1/C6 compact exponential": og.CORE_COMPACT_EXP}
+    for name, core in cores.items():
+        def f(core=core):
+            U.zero_(); V.zero_()
+            og.points_affect_points_dev(ctx, core, og.VELONLY, acc, T["x"], T["y"], T["r"], T["s"], T["x"], T["y"],
+                                        T["r"], U, V)
+        cpu = cpu_rate(lambda core=core: orc.points_affect_points(core, 1, x, y, r, s, x[sub], y[sub], r[sub]),
+                       256 * n)
+        fp = og.flops_per_pair(core, og.VELONLY, True)
+        row(name + " (0v_0b velocity)", "src/Kernels.h:81-92, src/CoreFunc.h", f, float(n) * n, fp if fp > 0 else None,
+            cpu)
+
+    def fp_(g=og.CORE_GAUSSIAN, res=og.VELONLY, thick=True):
+        v = og.flops_per_pair(g, res, thick)
+        return v if v > 0 else None
+
+    def p2p(res, thick, extra):
+        def f():
+            U.zero_(); V.zero_()
+            for e in E:
+                e.zero_()
+            og.points_affect_points_dev(ctx, og.CORE_GAUSSIAN, res, acc, T["x"], T["y"], T["r"], T["s"], T["x"],
+                                        T["y"], T["r"] if thick else None, U, V, extra=E[:extra])
+        return f
+    for name, ref, res, thick, extra in (
+            ("K2 Gaussian field points (0v_0p)", "src/Kernels.h:95-106", og.VELONLY, False, 0),
+            ("K3 velocity + gradient", "src/Kernels.h:112-133", og.VELANDGRAD, True, 4),
+            ("K4 velocity + vorticity", "src/Kernels.h:139-179", og.VELANDVORT, True, 1),
+            ("K4 velocity + shear rate", "src/Kernels.h:185-231", og.VELANDSHEAR, True, 1),
+            ("K5 streamfunction", "src/Kernels.h:52-74", og.PSIONLY, True, 1)):
+        cpu = cpu_rate(lambda res=res, thick=thick: orc.points_affect_points(
+            og.CORE_GAUSSIAN, res, x, y, r, s, x[sub], y[sub], r[sub] if thick else None), 256 * n)
+        row(name, ref, p2p(res, thick, extra), float(n) * n, fp_(res=res, thick=thick), cpu)
+
+    def vort():
+        E[0].zero_()
+        og.points_affect_points_vorticity_dev(ctx, acc, T["x"], T["y"], T["r"], T["s"], T["x"], T["y"], E[0])
+    row("D5 blob vorticity", "src/InfluenceVort.h:47-126", vort, float(n) * n, 13,
+        cpu_rate(lambda: orc.points_affect_points_vorticity(x, y, r, s, x[sub], y[sub]), 256 * n))
+
+    # panels: unit circle of 2048 panels, 200,000 points in the annulus
+    npan, npt = 2048, 200_000
+    rng = np.random.default_rng(3)
+    rad = np.sqrt(rng.uniform(0.55 ** 2, 9.0, npt))
+    th = rng.uniform(0, 2 * np.pi, npt)
+    px, py = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    pg = rng.normal(0, 1e-2, npt).astype(np.float32)
+    bd = og.circle_panels(npan)
+    vsh = rng.normal(0, 1, npan).astype(np.float32)
+    ssh = rng.normal(0, 1, npan).astype(np.float32)
+    P = {k: torch.from_numpy(v).to(dev) for k, v in dict(px=px, py=py, pg=pg, nx=bd.nx, ny=bd.ny, vs=vsh, ss=ssh).items()}
+    IDX = torch.from_numpy(bd.idx.astype(np.int32)).to(dev)
+    PU, PV = torch.zeros(npt, device=dev), torch.zeros(npt, device=dev)
+    QU, QV = torch.zeros(npan, device=dev), torch.zeros(npan, device=dev)
+    psub = np.random.default_rng(9).choice(npt, 4096, replace=False)
+
+    def d2():
+        PU.zero_(); PV.zero_()
+        og.panels_affect_points_dev(ctx, acc, P["nx"], P["ny"], IDX, P["vs"], P["ss"], P["px"], P["py"], PU, PV)
+    row("D2 panels on points (1vs)", "src/Influence.h:422-614", d2, float(npan) * npt, 47,
+        cpu_rate(lambda: orc.panels_affect_points(bd.nx, bd.ny, bd.idx, vsh, ssh, px[psub], py[psub]), npan * 4096.0))
+
+    def d3():
+        QU.zero_(); QV.zero_()
+        og.points_affect_panels_dev(ctx, acc, P["px"], P["py"], P["pg"], P["nx"], P["ny"], IDX, QU, QV)
+    row("D3 points on panels (reversed 1v)", "src/Influence.h:633-771", d3, float(npan) * npt, 39,
+        cpu_rate(lambda: orc.points_affect_panels(px[psub], py[psub], pg[psub], bd.nx, bd.ny, bd.idx), npan * 4096.0))
+
+    def d4():
+        QU.zero_(); QV.zero_()
+        og.panels_affect_panels_dev(ctx, acc, P["nx"], P["ny"], IDX, P["vs"], P["ss"], P["nx"], P["ny"], IDX, QU, QV)
+    row("D4 panels on panels", "src/Influence.h:774-795", d4, float(npan) * npan, 47,
+        cpu_rate(lambda: orc.panels_affect_panels(bd.nx, bd.ny, bd.idx, vsh, ssh, bd.nx, bd.ny, bd.idx),
+                 float(npan) * npan))
+    m = 2 * npan
+    A = torch.zeros(m * m, dtype=torch.float64, device=dev)
+
+    def b1():
+        og.panels_on_panels_coeff_dev(ctx, 2, P["nx"], P["ny"], IDX, None, A)
+    row("B1 panels-on-panels matrix (two-way, 1vos)", "src/Coefficients.h:155-427", b1, 2.0 * npan * npan, 45,
+        cpu_rate(lambda: orc.panels_on_panels_coeff(2, bd.nx, bd.ny, bd.idx), 2.0 * npan * npan))
+    RHS = torch.from_numpy(np.random.default_rng(10).normal(size=m)).to(dev)
+    SOL = torch.zeros(m, dtype=torch.float64, device=dev)
+    it_box = {}
+
+    def b3():
+        SOL.zero_()
+        it_box["it"], it_box["rel"] = og.solve_gmres_f64_dev(ctx, A, RHS, SOL)
+    b1()
+    _event_time(torch, stream, flush, b3, 1, 1)
+    row("B3 FP64 GMRES solve (4096 unknowns)", "src/BEM.h:169-234", b3, float(m) * m * (it_box["it"] or 1), None,
+        None, bytes_per_call=8.0 * m * m * (it_box["it"] or 1))
+    rows[-1]["iterations"] = it_box["it"]
+    rows[-1]["relative_residual"] = it_box["rel"]
+
+    # time stepping: one step of each scheme on the 131072-particle patch
+    for order, name in ((1, "E3 Euler step"), (2, "E3 Ralston RK2 step"), (3, "E3 RK3 step"), (4, "E3 Heun RK2 step")):
+        X2, Y2 = T["x"].clone(), T["y"].clone()
+
+        def stepf(order=order, X2=X2, Y2=Y2):
+            og.advect_dev(ctx, og.CORE_GAUSSIAN, acc, order, X2, Y2, T["r"], T["s"], (0.0, 0.0), 1e-4, 1)
+        stages = {1: 1, 2: 2, 3: 3, 4: 2}[order]
+        row(name, "src/Convection.h:274-598", stepf, stages * float(n) * n, fp_())
+
+    # reverse mode
+    LU, LV = [torch.from_numpy(a).to(dev) for a in np.random.default_rng(11).normal(size=(2, n)).astype(np.float32)]
+    G = [torch.zeros(n, device=dev) for _ in range(3)]
+
+    def vjp_self():
+        for g in G:
+            g.zero_()
+        og.points_affect_points_vjp_self_dev(ctx, og.CORE_GAUSSIAN, acc, T["x"], T["y"], T["r"], T["s"], LU, LV, *G)
+    row("adjoint: self-interaction VJP", "(no reference counterpart)", vjp_self, float(n) * n, None,
+        cpu_rate(lambda: orc.self_vjp(po.GAUSS, x[:4096], y[:4096], r[:4096], s[:4096], LU.cpu().numpy()[:4096],
+                                      LV.cpu().numpy()[:4096]), 4096.0 * 4096))
+    rows[-1]["cpu_note"] = "FP64 reference adjoint, 4096 particles"
+
+    def vjp_src():
+        for g in G:
+            g.zero_()
+        og.points_affect_points_vjp_dev(ctx, og.CORE_GAUSSIAN, acc, T["x"], T["y"], T["r"], T["s"], T["x"][:16384],
+                                        T["y"][:16384], None, LU[:16384], LV[:16384], *G)
+    row("adjoint: source-side VJP (16384 probes)", "(no reference counterpart)", vjp_src, float(n) * 16384, None)
+    ctx.synchronize()
+    out = {"workload": "rows", "metric": "per-row device throughput", "n_particles": n, "panels": npan,
+           "panel_points": npt, "fp32_peak_tflops": fp32_peak / 1e12, "hbm_peak_gbs": hbm_peak / 1e9,
+           "cpu_cores": threads, "rows": rows}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -719,7 +893,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--n", type=int, default=N, help="particles (the headline workload is 1,000,000)")
-    ap.add_argument("--workload", default="patch1M", choices=["patch1M", "euler20k", "bem2048", "rk2adjoint2M"],
+    ap.add_argument("--workload", default="patch1M", choices=["patch1M", "euler20k", "bem2048", "rk2adjoint2M", "rows"],
                     help="patch1M is the headline line; the others measure the remaining configurations")
     ap.add_argument("--rk-steps", type=int, default=64, help="RK2 steps of rk2adjoint2M")
     args = ap.parse_args()
@@ -732,6 +906,8 @@ def main():
         run_bem2048(args)
     elif args.workload == "rk2adjoint2M":
         run_rk2adjoint2M(args)
+    elif args.workload == "rows":
+        run_rows(args)
     else:
         run_engine(args)
 

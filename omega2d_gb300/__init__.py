@@ -555,6 +555,18 @@ def panels_affect_points_dev(ctx: Context, accum: int, nx, ny, idx, vs, ss, tx, 
            "obs_panels_affect_points_dev")
 
 
+def panels_affect_panels_dev(ctx: Context, accum: int, snx, sny, sidx, vs, ss, tnx, tny, tidx, pu, pv,
+                             finalize=False, fs=(0.0, 0.0)):
+    _check(lib().obs_panels_affect_panels_dev(ctx.handle, ctypes.c_int(accum),
+                                              ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+                                              ctypes.c_double(fs[0]), ctypes.c_double(fs[1]),
+                                              ctypes.c_int(snx.numel()), _ptr(snx), _ptr(sny),
+                                              ctypes.c_int(sidx.numel() // 2), _ptr(sidx), _ptr(vs), _ptr(ss),
+                                              ctypes.c_int(tnx.numel()), _ptr(tnx), _ptr(tny),
+                                              ctypes.c_int(tidx.numel() // 2), _ptr(tidx), _ptr(pu), _ptr(pv)),
+           "obs_panels_affect_panels_dev")
+
+
 def panels_on_panels_coeff_dev(ctx: Context, nunk: int, nx, ny, idx, A32=None, A64=None):
     """Self block of one body into device buffers (column-major, (nunk*npan)^2 elements)."""
     geo = (ctypes.c_int(nx.numel()), _ptr(nx), _ptr(ny), ctypes.c_int(idx.numel() // 2), _ptr(idx))
