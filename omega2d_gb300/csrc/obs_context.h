@@ -109,6 +109,11 @@ int p2p_ncomp(int res);
 bool packed_supported(int core, int res);
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
                             int* occ);
+// packed Gaussian kernels for the gradient, vorticity and shear results (p2p_packed_res.cu):
+// target pairs per thread and the launcher
+int packed_res_np(int res);
+cudaError_t packed_res_dispatch(int res, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
+                                int* occ);
 cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, const int* perm,
                                int ns, int ns_pad, int core, float4* out, unsigned* meta, cudaStream_t st);
 // Spatial (Morton) order of n points (bin_order.cu).  `scratch` holds bin_scratch_bytes(n)

@@ -143,9 +143,11 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   int np = 2;
   if (variant == OBS_VARIANT_PACKED4 || (variant == OBS_VARIANT_AUTO && rq.core == CORE_GAUSS)) np = 4;
   else if (variant == OBS_VARIANT_PACKED3 && rq.core == CORE_GAUSS) np = 3;
+  if (packed && res != RES_VEL) np = packed_res_np(res);
   auto launch = [&](const P2PArgs* args, int g, int* occ_out) -> cudaError_t {
-    return packed ? packed_dispatch(rq.core, np, thick, comp, args, g, st, occ_out)
-                  : dispatch(rq.core, thick, res, comp, args, g, st, occ_out);
+    if (!packed) return dispatch(rq.core, thick, res, comp, args, g, st, occ_out);
+    if (res != RES_VEL) return packed_res_dispatch(res, thick, comp, args, g, st, occ_out);
+    return packed_dispatch(rq.core, np, thick, comp, args, g, st, occ_out);
   };
 
   // ---- plan the split

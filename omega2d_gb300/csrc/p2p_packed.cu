@@ -6,7 +6,7 @@ namespace obs {
 
 namespace {
 
-// Sources staged for the packed kernels: (x, x, y, y), (G, G, -G, -G), (z, z, 0, 0); padded
+// Sources staged for the packed kernels: (x, x, y, y), (G, G, -G, -G), (z, z, |G|, |G|); padded
 // with zero-strength sources at the origin and radius term 1 (finite for both cores).  With a
 // permutation, staged source i is the caller's source perm[i].
 __global__ void pack_sources_dup_kernel(const float* __restrict__ sx, const float* __restrict__ sy,
@@ -21,7 +21,7 @@ __global__ void pack_sources_dup_kernel(const float* __restrict__ sx, const floa
     const float x = sx[j], y = sy[j], g = ss[j], z = radius_term(core, r);
     out[PK_ELEM * i] = make_float4(x, x, y, y);
     out[PK_ELEM * i + 1] = make_float4(g, g, -g, -g);
-    out[PK_ELEM * i + 2] = make_float4(z, z, 0.0f, 0.0f);
+    out[PK_ELEM * i + 2] = make_float4(z, z, fabsf(g), fabsf(g));
   } else if (i < ns_pad) {
     out[PK_ELEM * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     out[PK_ELEM * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -56,7 +56,8 @@ cudaError_t packed_dispatch_np(bool thick, bool comp, const P2PArgs* a, int grid
 }  // namespace
 
 bool packed_supported(int core, int res) {
-  return res == RES_VEL && core >= CORE_RM && core <= CORE_CEXP;
+  if (res == RES_VEL) return core >= CORE_RM && core <= CORE_CEXP;
+  return core == CORE_GAUSS && (res == RES_GRAD || res == RES_VORT || res == RES_SHEAR);
 }
 
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,

@@ -28,7 +28,7 @@
 
 namespace obs {
 
-constexpr int PK_ELEM = 3;   // float4 per staged source
+constexpr int PK_ELEM = 3;   // float4 per staged source: (x,x,y,y) (G,G,-G,-G) (z,z,|G|,|G|)
 constexpr int PK_BLK = 32;   // sources per near-mask bit word / compensated block
 constexpr int PK_NB = SRC_TILE / PK_BLK;
 

@@ -211,3 +211,43 @@ def test_morton_order_matches_host_stable_sort(ctx, n, dist):
     og.morton_order_dev(ctx, X, Y, P)
     ctx.synchronize()
     assert np.array_equal(P.cpu().numpy(), _morton_ref(x, y))
+
+
+@pytest.mark.parametrize("result", [og.VELANDGRAD, og.VELANDVORT, og.VELANDSHEAR])
+@pytest.mark.parametrize("thick", [True, False])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+@pytest.mark.parametrize("uniform", [True, False])
+@pytest.mark.parametrize("order", [og.ORDER_INPUT, og.ORDER_BINNED])
+def test_packed_gradient_results_vs_generic_and_fp64(ctx, restatement, result, thick, accum, uniform, order):
+    """Gaussian velocity + gradient / vorticity / shear: the packed kernel (far blocks without the
+    exponential) against the generic kernel and the FP64 oracle."""
+    rng = np.random.default_rng(result * 10 + thick + 2 * accum + 4 * uniform + order)
+    ns, nt = 7000, 4001
+    sigma = 0.004
+    sx, sy = rng.normal(0, 0.3, (2, ns)).astype(np.float32)
+    sr = np.full(ns, sigma, np.float32) if uniform else rng.uniform(0.5 * sigma, 2 * sigma, ns).astype(np.float32)
+    ss = rng.normal(0, 1e-3, ns).astype(np.float32)
+    tx, ty = rng.normal(0, 0.3, (2, nt)).astype(np.float32)
+    tx[:100], ty[:100] = sx[:100], sy[:100]
+    tx[100:300], ty[100:300] = sx[100:300] + 4.5 * sigma, sy[100:300]     # between the 16 and 25 cut-offs
+    tr = (np.full(nt, sigma, np.float32) if uniform else rng.uniform(0.5 * sigma, 2 * sigma, nt).astype(np.float32))
+    outs = {}
+    try:
+        ctx.set_target_order(order)
+        for v in (og.VARIANT_GENERIC, og.VARIANT_AUTO):
+            ctx.set_kernel_variant(v)
+            t = og.Points(tx, ty, tr if thick else None, None)
+            og.points_affect_points(og.Points(sx, sy, sr, ss), t, result, og.ExecEnv(og.CORE_GAUSSIAN, accum, ctx))
+            ex = t.grad if result == og.VELANDGRAD else [t.vort if result == og.VELANDVORT else t.shear]
+            outs[v] = [t.u, t.v] + list(ex)
+    finally:
+        ctx.set_kernel_variant(og.VARIANT_AUTO)
+        ctx.set_target_order(og.ORDER_AUTO)
+    u64, v64, ex64 = restatement.points_affect_points(og.CORE_GAUSSIAN, result, sx, sy, sr, ss, tx, ty,
+                                                      tr if thick else None, fp64=True)
+    ref = [u64, v64] + list(ex64)
+    tol = 2e-6 if accum == og.COMPENSATED else 3e-5
+    for v, got in outs.items():
+        for k, (a, b) in enumerate(zip(ref, got)):
+            ok = np.isfinite(a)
+            assert rel_err(a[ok], b[ok]) < tol, (v, k)
