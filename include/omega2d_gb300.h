@@ -74,11 +74,12 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
 /* Device-side failure record seen by the last synchronizing call that reported one: DEV_ERR
  * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
-/* Kernel variant for particle-on-particle velocity sums.  AUTO uses the packed-FP32 kernels
- * (two targets per f32x2 register pair) where they exist (velocity only, Gaussian and RM
- * cores; 4 target pairs per thread for the Gaussian core, 2 for RM) and the generic kernels
- * elsewhere; GENERIC forces the generic kernels; PACKED2 / PACKED3 / PACKED4 pick 2, 3 or 4
- * target pairs per thread for the packed kernels. */
+/* Kernel variant for particle-on-particle sums.  AUTO uses the packed-FP32 kernels (two
+ * targets per f32x2 register pair) where they exist (velocity for every core but the compact
+ * exponential, 4 target pairs per thread for the Gaussian core and 2 for the others; velocity
+ * gradient, vorticity and shear for the Gaussian core) and the generic kernels elsewhere;
+ * GENERIC forces the generic kernels (and the one-kernel-per-step GMRES); PACKED2 / PACKED3 /
+ * PACKED4 pick 2, 3 or 4 target pairs per thread for the packed velocity kernels. */
 #define OBS_VARIANT_AUTO 0
 #define OBS_VARIANT_GENERIC 1
 #define OBS_VARIANT_PACKED2 2
@@ -227,7 +228,8 @@ int obs_solve_dense_f64_dev(obs_context* ctx, int n, const double* A, const doub
 
 /* Restarted GMRES in FP64 on the GPU (the reference's BEM solver method, Eigen GMRES in FP32,
  * src/BEM.h:169-234): right diagonal preconditioning, classical Gram-Schmidt with one
- * reorthogonalisation, Givens rotations on the device.  x holds the initial guess on entry and
+ * reorthogonalisation, Givens rotations on the device; for restart <= 64 each restart cycle is
+ * one cooperative launch with grid barriers.  x holds the initial guess on entry and
  * the solution on return; iterations and rel_residual = ||b - A x|| / ||b|| are optional
  * outputs.  OBS_ERR_NO_CONVERGENCE when maxiter iterations end above tol (x then holds the
  * last iterate). */

@@ -11,6 +11,7 @@
 //
 // Cost per iteration: one FP64 matrix-vector product (n^2 doubles from HBM: the bound) plus
 // O(n j) vector work.  Every reduction has a fixed order, so results are reproducible.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -185,6 +186,335 @@ __global__ void diag_inv_kernel(const double* __restrict__ A, int n, double* __r
   dinv[i] = (d != 0.0) ? 1.0 / d : 1.0;
 }
 
+// ---------------------------------------------------------------- one restart cycle in one launch
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU, so the operator
+// product of the fused cycle multiplies in double-float: A is held as two FP32 planes
+// (hi = fl(a), lo = fl(a - hi): 48 of a's 53 significand bits) and the vector the same way;
+// each product is formed exactly with an FMA and summed in an unevaluated (S, s) pair.
+// Everything else (Gram-Schmidt, norms, Givens, back substitution, the restart residual)
+// stays FP64.
+
+constexpr int GC_THREADS = 1024;
+constexpr int GC_WARPS = GC_THREADS / 32;
+constexpr int GC_MAXM = 64;                     // restart length supported by the fused kernel
+
+// hi/lo planes of A; flags entries outside 2^+-99 (other than 0), where the planes would lose
+// precision or overflow
+__global__ void split_planes_kernel(const double* __restrict__ A, size_t nn, float2* __restrict__ AP,
+                                    int* __restrict__ range_flag) {
+  int bad = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x) {
+    const double a = A[k];
+    const float hi = __double2float_rn(a);
+    const float lo = __double2float_rn(a - (double)hi);
+    const int ex = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+    bad |= (ex != 0 && (ex < 1023 - 99 || ex > 1023 + 99)) || (ex == 0 && (__double_as_longlong(a) << 1) != 0);
+    AP[k] = make_float2(hi, lo);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(range_flag, 1);
+}
+
+struct GcArgs {
+  const float2* AP;                             // hi/lo planes of A, column-major
+  const double* dinv;
+  int n, m, mc;                                 // order, restart length, iterations this cycle
+  int gpb;                                      // row groups a block owns (at most)
+  const double* V0;                             // v_0 (n)
+  float2* vs;                                   // hi/lo of Dinv v_j
+  double* x;
+  double* P;                                    // partials: [2][grid][m+2]
+  unsigned* bar;                                // arrival counter, zeroed before each launch
+  GmState* st;
+  int* status;
+};
+
+__device__ __forceinline__ void red_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// grid barrier number `nb` (0, 1, 2, ...) over co-resident blocks: a monotone arrival counter
+// with release adds and acquire polls; the poll is bounded (about a second), after which the
+// block records where it gave up and every block returns false
+__device__ bool gc_barrier(unsigned* bar, int* status, unsigned nb) {
+  __syncthreads();
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    const unsigned target = (nb + 1) * gridDim.x;
+    red_release_gpu(bar, 1u);
+    unsigned it = 0;
+    while (ld_acquire_gpu(bar) < target) {
+      if (++it > (1u << 21)) {
+        record_failure(status, DEV_ERR_TIMEOUT, 700, (int)blockIdx.x, (int)nb);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// out[k] = sum over blocks of P[b * ld + k], k < cnt: one warp per k, fixed order
+__device__ void gc_sum_partials(const double* P, int ld, int cnt, double* out) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  for (int k = wp; k < cnt; k += GC_WARPS) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += P[(size_t)b * ld + k];
+    s = warp_sum(s);
+    if (lane == 0) out[k] = s;
+  }
+  __syncthreads();
+}
+
+// The block's rows of the basis live in shared memory: Vs[k * RB + r], r = q * 32 + lane for
+// the block's q-th row group (global row (blockIdx.x + q * grid) * 32 + lane; rows past n
+// hold 0), and w likewise in ws[r].
+struct GcRows {
+  double* Vs;
+  double* ws;
+  int RB;     // 32 * gpb
+  int nq;     // row groups this block owns
+};
+
+// this block's share of V_k . w (k <= j) into P[blockIdx.x * ld + k]; with `norm`, also w . w
+// into slot j + 1
+__device__ void gc_partial_dots(const GcRows& R, int j, bool norm, int ld, double* P, double* sh) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int kmax = norm ? j + 1 : j;
+  for (int k = wp; k <= kmax; k += GC_WARPS) {
+    const double* vk = (k <= j) ? R.Vs + (size_t)k * R.RB : R.ws;
+    double s = 0.0;
+    for (int q = 0; q < R.nq; ++q) s = fma(vk[q * 32 + lane], R.ws[q * 32 + lane], s);
+    s = warp_sum(s);
+    if (lane == 0) sh[k] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= kmax; k += GC_THREADS) P[(size_t)blockIdx.x * ld + k] = sh[k];
+}
+
+// sum_{k <= j} V_k[r] c[k] for local row group q (warps split k, fixed-order sum); valid in
+// warp 0
+__device__ double gc_vsum(const GcRows& R, int j, int q, const double* c, double (*red)[32]) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  double s = 0.0;
+  for (int k = wp; k <= j; k += GC_WARPS) s = fma(R.Vs[(size_t)k * R.RB + q * 32 + lane], c[k], s);
+  red[wp][lane] = s;
+  __syncthreads();
+  double t = 0.0;
+  if (wp == 0)
+    for (int p = 0; p < GC_WARPS; ++p) t += red[p][lane];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ float2 split_f64(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+// S + s += a * x in double-float, a = a.x + a.y and x = x.x + x.y (the a.y * x.y term, 2^-48
+// relative, is dropped); the product a.x * x.x is split exactly with an FMA and added to S with
+// Knuth's two-sum
+__device__ __forceinline__ void df_fma(float2 av, float2 xv, float& S, float& s) {
+  const float p = __fmul_rn(av.x, xv.x);
+  const float e = __fmaf_rn(av.x, xv.x, -p);
+  const float t = __fmaf_rn(av.x, xv.y, __fmaf_rn(av.y, xv.x, e));
+  const float u = __fadd_rn(S, p);
+  const float bv = __fsub_rn(u, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bv)), __fsub_rn(p, bv));
+  S = u;
+  s = __fadd_rn(s, __fadd_rn(err, t));
+}
+
+// (S, s) += (T, t) in double-float: two-sum of the leading parts, the trailing parts added to
+// the error term
+__device__ __forceinline__ void df_add(float& S, float& s, float T, float t) {
+  const float u = __fadd_rn(S, T);
+  const float bv = __fsub_rn(u, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bv)), __fsub_rn(T, bv));
+  S = u;
+  s = __fadd_rn(s, __fadd_rn(err, t));
+}
+
+// One restart cycle of right-preconditioned GMRES(m) with CGS2, back substitution and the
+// update of x, in one cooperative launch.  Blocks own groups of 32 consecutive rows
+// (column-major A: a warp reads 256 contiguous bytes of the planes per column) and keep those
+// rows of the basis in shared memory; only the split vector Dinv v_j and the per-block partial
+// sums cross between blocks.  Iteration j:
+//   (1) w = A Dinv v_j on the owned rows; partial V^T w                         -> barrier
+//   (2) h = V^T w; w -= V h; partial V^T w and w^T w                            -> barrier
+//   (3) h2 = V^T w; ||w - V h2||^2 = w^T w - h2^T h2 (V orthonormal);
+//       v_{j+1} = (w - V h2) / ||.|| on the owned rows; H column h + h2; Givens   -> barrier
+// Every block keeps H, the rotations and g in shared memory and runs the (tiny) Givens and
+// back-substitution steps itself, so no step waits on one block; the rotations of column j
+// run on one warp during the product of step j+1 (FP64 latency on this GPU makes them slow,
+// not costly).  All sums over blocks run in block order, so the result does not depend on
+// timing.
+__global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs a) {
+  __shared__ double red[GC_WARPS][32];
+  __shared__ double Hs[GC_MAXM][GC_MAXM + 1];   // Hs[j][k]: rotated column j (R factor)
+  __shared__ double h1[GC_MAXM + 2];
+  __shared__ double sh[GC_MAXM + 2];
+  __shared__ double gs[GC_MAXM + 1];
+  __shared__ double css[GC_MAXM], sns[GC_MAXM];
+  __shared__ double nrm_inv[2];
+  __shared__ int sdone;
+  extern __shared__ double dyn[];
+  float2 (*redf)[32] = reinterpret_cast<float2 (*)[32]>(red);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int ngroups = (a.n + 31) / 32;
+  const int ld = a.m + 2;
+  GcRows R;
+  R.RB = 32 * a.gpb;
+  R.Vs = dyn;
+  R.ws = dyn + (size_t)(a.m + 1) * R.RB;
+  R.nq = ((int)blockIdx.x < ngroups) ? (ngroups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  double* P1 = a.P;
+  double* P2 = a.P + (size_t)gridDim.x * ld;
+  // the last warp applies the Givens rotations to column j-1 while the others form A Dinv v_j
+  const bool gwarp = (wp == GC_WARPS - 1);
+  const int per = (a.n + GC_WARPS - 2) / (GC_WARPS - 1);
+  const int c0 = gwarp ? a.n : min(a.n, wp * per), c1 = gwarp ? a.n : min(a.n, c0 + per);
+  auto row = [&](int q) { return ((int)blockIdx.x + q * (int)gridDim.x) * 32 + lane; };
+  unsigned nb = 0;
+
+  if (threadIdx.x == 0) {
+    gs[0] = a.st->beta;
+    sdone = a.st->done;
+  }
+  for (int k = 1 + threadIdx.x; k <= GC_MAXM; k += GC_THREADS) gs[k] = 0.0;
+  // v_0 on the owned rows into shared memory; Dinv v_0 split for the operator product
+  if (wp == 0)
+    for (int q = 0; q < R.nq; ++q) {
+      const int i = row(q);
+      const double v = (i < a.n) ? a.V0[i] : 0.0;
+      R.Vs[q * 32 + lane] = v;
+      if (i < a.n) a.vs[i] = split_f64(v * a.dinv[i]);
+    }
+  if (!gc_barrier(a.bar, a.status, nb++)) return;
+
+  int kd = 0;
+  for (int j = 0;; ++j) {
+    if (gwarp && lane == 0 && j > 0) {
+      // column j-1 of H (assembled in step 3): previous rotations, a new one, g, convergence
+      const int jc = j - 1;
+      double* hc = Hs[jc];
+      for (int k = 0; k < jc; ++k) {
+        const double t = css[k] * hc[k] + sns[k] * hc[k + 1];
+        hc[k + 1] = -sns[k] * hc[k] + css[k] * hc[k + 1];
+        hc[k] = t;
+      }
+      const double x0 = hc[jc], x1 = hc[jc + 1];
+      const double r = hypot(x0, x1);
+      const double c = (r == 0.0) ? 1.0 : x0 / r, sg = (r == 0.0) ? 0.0 : x1 / r;
+      css[jc] = c;
+      sns[jc] = sg;
+      hc[jc] = r;
+      hc[jc + 1] = 0.0;
+      gs[jc + 1] = -sg * gs[jc];
+      gs[jc] = c * gs[jc];
+      sdone = (fabs(gs[jc + 1]) <= a.st->tolabs || x1 == 0.0) ? 1 : 0;
+    }
+    const bool more = j < a.mc;
+    // (1) w = A Dinv v_j on the owned rows, double-float; columns split over the warps, the
+    //     warps' (S, s) pairs combined in double-float and converted to FP64 once per row
+    for (int q = 0; q < R.nq && more; ++q) {
+      const int i = row(q);
+      const int ic = min(i, a.n - 1);            // rows past n compute a dummy sum, never stored
+      float S0 = 0.f, s0 = 0.f, S1 = 0.f, s1 = 0.f;
+      const float2* col = a.AP + (size_t)c0 * a.n + ic;
+      int c = c0;
+#pragma unroll 4
+      for (; c + 1 < c1; c += 2, col += 2 * (size_t)a.n) {
+        df_fma(__ldg(col), a.vs[c], S0, s0);
+        df_fma(__ldg(col + a.n), a.vs[c + 1], S1, s1);
+      }
+      if (c < c1) df_fma(__ldg(col), a.vs[c], S0, s0);
+      df_add(S0, s0, S1, s1);
+      redf[wp][lane] = make_float2(S0, s0);
+      __syncthreads();
+      if (wp == 0) {
+        float2 t = redf[0][lane];
+        for (int p = 1; p < GC_WARPS; ++p) df_add(t.x, t.y, redf[p][lane].x, redf[p][lane].y);
+        R.ws[q * 32 + lane] = (i < a.n) ? (double)t.x + (double)t.y : 0.0;
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (sdone || !more) {   // converged at column j-1 (the last product is discarded), or m steps
+      kd = j;
+      break;
+    }
+    gc_partial_dots(R, j, false, ld, P1, sh);
+    if (!gc_barrier(a.bar, a.status, nb++)) return;
+    // (2)
+    gc_sum_partials(P1, ld, j + 1, h1);
+    for (int q = 0; q < R.nq; ++q) {
+      const double t = gc_vsum(R, j, q, h1, red);
+      if (wp == 0) R.ws[q * 32 + lane] -= t;
+    }
+    __syncthreads();
+    gc_partial_dots(R, j, true, ld, P2, sh);
+    if (!gc_barrier(a.bar, a.status, nb++)) return;
+    // (3)
+    gc_sum_partials(P2, ld, j + 2, sh);
+    if (wp == 0) {
+      double s2 = 0.0;
+      for (int k = lane; k <= j; k += 32) s2 = fma(sh[k], sh[k], s2);
+      s2 = warp_sum(s2);
+      if (lane == 0) {
+        const double nrm2 = sh[j + 1] - s2;
+        const double nr = nrm2 > 0.0 ? sqrt(nrm2) : 0.0;
+        nrm_inv[0] = nr;
+        nrm_inv[1] = nr > 0.0 ? 1.0 / nr : 0.0;
+      }
+    }
+    __syncthreads();
+    const double nrm = nrm_inv[0], inv = nrm_inv[1];
+    for (int q = 0; q < R.nq; ++q) {
+      const double t = gc_vsum(R, j, q, sh, red);
+      if (wp == 0) {
+        const int i = row(q);
+        const double v = (R.ws[q * 32 + lane] - t) * inv;
+        R.Vs[(size_t)(j + 1) * R.RB + q * 32 + lane] = v;
+        if (i < a.n) a.vs[i] = split_f64(v * a.dinv[i]);
+      }
+    }
+    for (int k = threadIdx.x; k <= j; k += GC_THREADS) Hs[j][k] = h1[k] + sh[k];
+    if (threadIdx.x == 0) Hs[j][j + 1] = nrm;
+    if (!gc_barrier(a.bar, a.status, nb++)) return;
+  }
+  // y = R^{-1} g (every block), then x += Dinv V y on the owned rows
+  if (threadIdx.x == 0) {
+    for (int i = kd - 1; i >= 0; --i) {
+      double t = gs[i];
+      for (int q = i + 1; q < kd; ++q) t -= Hs[q][i] * h1[q];
+      h1[i] = t / Hs[i][i];
+    }
+    if (blockIdx.x == 0) {
+      a.st->kdone = kd;
+      a.st->done = sdone;
+    }
+  }
+  __syncthreads();
+  if (kd > 0)
+    for (int q = 0; q < R.nq; ++q) {
+      const double t = gc_vsum(R, kd - 1, q, h1, red);
+      const int i = row(q);
+      if (wp == 0 && i < a.n) a.x[i] += t * a.dinv[i];
+    }
+}
+
 }  // namespace
 
 int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol, int restart,
@@ -207,7 +537,39 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   const size_t o_w = o_d + al(N * 8);
   const size_t o_p = o_w + al(N * 8);
   const size_t o_n = o_p + al((size_t)nchunk * N * 8);
-  const size_t total = o_n + 256;
+  // fused cycle: co-resident grid, partials [2][grid][m+2], split vector, planes of A, counters
+  int gc_occ = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gc_occ, gmres_cycle_kernel, GC_THREADS, 0);
+  if (e != cudaSuccess) return cuda_status(e);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+  // one block per SM (1024 threads at 64 registers fill an SM's register file); each block's
+  // rows of the basis (m+1 vectors) and of w sit in dynamic shared memory
+  const int ngroups = (n + 31) / 32;
+  const int gc_grid = std::min(ngroups, std::max(1, gc_occ) * ctx->num_sms);
+  const int gc_gpb = (ngroups + gc_grid - 1) / gc_grid;
+  const size_t gc_smem = (size_t)(m + 2) * 32 * gc_gpb * sizeof(double);
+  bool fused = coop && gc_occ > 0 && m <= GC_MAXM && ctx->kernel_variant != OBS_VARIANT_GENERIC;
+  if (fused) {
+    cudaFuncAttributes fa{};
+    int smem_optin = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    if ((e = cudaFuncGetAttributes(&fa, gmres_cycle_kernel)) != cudaSuccess) return cuda_status(e);
+    fused = fa.sharedSizeBytes + gc_smem <= (size_t)smem_optin;
+    if (fused) {
+      e = cudaFuncSetAttribute(gmres_cycle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gc_smem);
+      if (e != cudaSuccess) return cuda_status(e);
+      int occ2 = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, gmres_cycle_kernel, GC_THREADS, gc_smem);
+      if (e != cudaSuccess) return cuda_status(e);
+      fused = occ2 * ctx->num_sms >= gc_grid;
+    }
+  }
+  const size_t o_gp = o_n + 256;
+  const size_t o_gv = o_gp + al((size_t)2 * gc_grid * (m + 2) * 8);
+  const size_t o_gb = o_gv + al(N * 8);
+  const size_t o_ap = o_gb + 256;
+  const size_t total = fused ? o_ap + al(N * N * 8) : o_gb + 256;
   int s = ctx->work.ensure(total, ctx->stream);
   if (s) return s;
   GmState* st = ctx->work.as<GmState>(o_st);
@@ -222,6 +584,10 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   double* w = ctx->work.as<double>(o_w);
   double* part = ctx->work.as<double>(o_p);
   double* nrm = ctx->work.as<double>(o_n);
+  double* gpart = ctx->work.as<double>(o_gp);
+  float2* gvs = ctx->work.as<float2>(o_gv);
+  unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag
+  float2* AP = fused ? ctx->work.as<float2>(o_ap) : nullptr;
   cudaStream_t strm = ctx->stream;
   const int gb = (n + GM_THREADS - 1) / GM_THREADS;
   const dim3 ggrid(gb, nchunk);
@@ -230,56 +596,84 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   diag_inv_kernel<<<gb, GM_THREADS, 0, strm>>>(A, n, dinv);
   norm_kernel<<<1, 1024, 0, strm>>>(b, n, nrm, nullptr);
   launched(2);
+  if ((e = cudaMemsetAsync(gbar, 0, 2 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
+  if (fused) {
+    split_planes_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, N * N, AP, reinterpret_cast<int*>(gbar + 1));
+    launched(1);
+  }
   double bnorm = 0.0;
-  cudaError_t e = cudaMemcpyAsync(&bnorm, nrm, 8, cudaMemcpyDeviceToHost, strm);
+  int range_bad = 0;
+  e = cudaMemcpyAsync(&bnorm, nrm, 8, cudaMemcpyDeviceToHost, strm);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&range_bad, gbar + 1, 4, cudaMemcpyDeviceToHost, strm);
   if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
   if (e != cudaSuccess) return cuda_status(e);
+  if (range_bad) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
   const double bref = (bnorm == 0.0) ? 1.0 : bnorm;   // src/BEM.h:227-229 divides by 1 then
   GmState h0{0, 0, 0.0, tol * bref};
   if ((e = cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, strm)) != cudaSuccess) return cuda_status(e);
 
-  int total_it = 0;
-  double rel = 0.0;
-  for (;;) {
-    // r = b - A Dinv (D x) ... x is the unpreconditioned iterate: r = b - A x
+  // r = b - A x in FP64 (the true residual), its norm into nrm
+  auto residual = [&]() {
     gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, x, nullptr, part, nullptr);
     gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, b, w, nullptr);
     norm_kernel<<<1, 1024, 0, strm>>>(w, n, nrm, nullptr);
     launched(3);
+  };
+  residual();
+  int total_it = 0;
+  double rel = 0.0;
+  for (;;) {
     double rn = 0.0;
     e = cudaMemcpyAsync(&rn, nrm, 8, cudaMemcpyDeviceToHost, strm);
     if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
     if (e != cudaSuccess) return cuda_status(e);
+    if (total_it > 0) {
+      // the cycle's iteration count; a barrier that gave up leaves its record in the status block
+      int kd = 0, flag = 0;
+      e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess && fused) e = cudaMemcpyAsync(&flag, ctx->d_status, 4, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
+      if (e != cudaSuccess) return cuda_status(e);
+      if (flag) return take_device_status(ctx);
+      total_it += std::max(kd, 1) - 1;
+    }
     rel = rn / bref;
     if (!(rn > tol * bref) || total_it >= maxiter) break;   // converged (or NaN) / out of budget
     cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m);
     scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, nrm, V, nullptr);
     launched(2);
     const int mc = std::min(m, maxiter - total_it);
-    for (int j = 0; j < mc; ++j) {
-      double* Hj = H + (size_t)j * (m + 1);
-      // w = A Dinv v_j
-      gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, V + (size_t)j * N, dinv, part, st);
-      gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, nullptr, w, st);
-      // CGS2: h = V^T w; w -= V h; h2 = V^T w; w -= V h2; h += h2
-      dots_kernel<<<j + 1, GM_THREADS, 0, strm>>>(V, n, w, Hj, 0, st);
-      update_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, j, Hj, w, st);
-      dots_kernel<<<j + 1, GM_THREADS, 0, strm>>>(V, n, w, h2, 0, st);
-      update_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, j, h2, w, st);
-      hadd_kernel<<<1, 64, 0, strm>>>(Hj, h2, j + 1, st);
-      norm_kernel<<<1, 1024, 0, strm>>>(w, n, Hj + j + 1, st);
-      scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, Hj + j + 1, V + (size_t)(j + 1) * N, st);
-      givens_kernel<<<1, 1, 0, strm>>>(H, m + 1, j, cs, sn, g, st);
-      launched(10);
+    if (fused) {
+      if ((e = cudaMemsetAsync(gbar, 0, sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
+      GcArgs ga{AP, dinv, n, m, mc, gc_gpb, V, gvs, x, gpart, gbar, st, ctx->d_status};
+      void* args[] = {&ga};
+      e = cudaLaunchCooperativeKernel((const void*)gmres_cycle_kernel, dim3(gc_grid), dim3(GC_THREADS), args, gc_smem,
+                                      strm);
+      if (e != cudaSuccess) return cuda_status(e);
+      launched(1);
+    } else {
+      for (int j = 0; j < mc; ++j) {
+        double* Hj = H + (size_t)j * (m + 1);
+        // w = A Dinv v_j
+        gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, V + (size_t)j * N, dinv, part, st);
+        gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, nullptr, w, st);
+        // CGS2: h = V^T w; w -= V h; h2 = V^T w; w -= V h2; h += h2
+        dots_kernel<<<j + 1, GM_THREADS, 0, strm>>>(V, n, w, Hj, 0, st);
+        update_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, j, Hj, w, st);
+        dots_kernel<<<j + 1, GM_THREADS, 0, strm>>>(V, n, w, h2, 0, st);
+        update_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, j, h2, w, st);
+        hadd_kernel<<<1, 64, 0, strm>>>(Hj, h2, j + 1, st);
+        norm_kernel<<<1, 1024, 0, strm>>>(w, n, Hj + j + 1, st);
+        scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, Hj + j + 1, V + (size_t)(j + 1) * N, st);
+        givens_kernel<<<1, 1, 0, strm>>>(H, m + 1, j, cs, sn, g, st);
+        launched(10);
+      }
+      backsub_kernel<<<1, 1, 0, strm>>>(H, m + 1, g, yv, st);
+      xupdate_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, yv, dinv, x, st);
+      launched(2);
     }
-    backsub_kernel<<<1, 1, 0, strm>>>(H, m + 1, g, yv, st);
-    xupdate_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, yv, dinv, x, st);
-    launched(2);
-    int kd = 0;
-    e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
-    if (e != cudaSuccess) return cuda_status(e);
-    total_it += std::max(kd, 1);
+    residual();
+    total_it += 1;   // completed below from kdone
   }
   if (iters_out) *iters_out = total_it;
   if (rel_residual) *rel_residual = rel;
