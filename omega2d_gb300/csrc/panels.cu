@@ -5,10 +5,12 @@
 // panels_affect_points (src/Influence.h:422-614), points_affect_panels (:633-771),
 // panels_on_panels_coeff (src/Coefficients.h:155-427), vels_to_rhs_panels (src/RHS.h:54-115).
 //
-// Pair arithmetic is FP32 like the reference, with two accuracy changes that leave the
-// mathematics unchanged: the subtended angle is one atan2 of (cross, dot) instead of the
-// difference of two atan2 values, and 0.5*log(r0^2/r1^2) is log1p of an exactly formed
-// (r0^2 - r1^2)/r1^2.  Both remove cancellations the reference suffers at distant targets.
+// Pair arithmetic is FP32 like the reference, with accuracy changes that leave the mathematics
+// unchanged: the subtended angle is one atan2 of (cross, dot) instead of the difference of two
+// atan2 values, with the cross product taken against the panel vector, and
+// 0.5*log(r0^2/r1^2) is formed from the exactly computed difference r0^2 - r1^2 (log1p, or
+// atanh of (rho-1)/(rho+1)).  These remove cancellations the reference suffers at distant
+// targets.
 #include <algorithm>
 #include <cstring>
 
@@ -63,7 +65,9 @@ __device__ __forceinline__ void panel_uv_star(float4 P, float tx, float ty, floa
   const float dx0 = tx - P.x, dy0 = ty - P.y;
   const float dx1 = tx - P.z, dy1 = ty - P.w;
   const float px = P.z - P.x, py = P.w - P.y;
-  us = atan2f(dy0 * dx1 - dx0 * dy1, dx0 * dx1 + dy0 * dy1);
+  // (t - p0) x (t - p1) = (t - p0) x (p1 - p0): the second form has no cancellation at distant
+  // targets, where the first differences two products of size d^2 to get one of size d L
+  us = atan2f(dx0 * py - dy0 * px, dx0 * dx1 + dy0 * dy1);
   const float r1 = dx1 * dx1 + dy1 * dy1;
   const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
   // log(r0^2 / r1^2) in whichever form is well conditioned: log1p of the difference quotient
@@ -73,15 +77,62 @@ __device__ __forceinline__ void panel_uv_star(float4 P, float tx, float ty, floa
   vs = (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
 }
 
-// kernelu_1vs_0p (vortex + source sheet) on one target; ss = 0 gives kernelu_1v_0p.
-__device__ __forceinline__ void panel_vel(float4 P, float4 Q, float tx, float ty, float& u, float& v) {
-  float us, vs;
-  panel_uv_star(P, tx, ty, us, vs);
-  const float a = us * Q.x - vs * Q.y;   // vortex part, x
-  const float b = us * Q.y + vs * Q.x;   // vortex part, y == source part, x
-  const float c = vs * Q.y - us * Q.x;   // source part, y
-  u = Q.z * a + Q.w * b;
-  v = Q.z * b + Q.w * c;
+// ---- the same two quantities with fewer instructions, for the panel <-> particle sums, which
+// are issue-bound: a polynomial arctangent, and the half-log as atanh of s = (rho-1)/(rho+1),
+// rho = r0^2/r1^2, from its odd series where |s| <= 0.2 (every target more than a few panel
+// lengths from the panel).  Both keep full relative accuracy at small angles and logs.
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// atan(r), r in [0, 1], as r * P(r^2): P of degree 8 fitted to atan(r)/r for minimum maximum
+// relative error (omega2d_gb300/poly_fit.py); 1.5e-7 relative error in FP32
+__device__ __forceinline__ float atan_unit(float r) {
+  const float t = r * r;
+  float p = 2.849889686e-03f;
+  p = fmaf(p, t, -1.606862992e-02f);
+  p = fmaf(p, t, 4.269152135e-02f);
+  p = fmaf(p, t, -7.504294813e-02f);
+  p = fmaf(p, t, 1.064093411e-01f);
+  p = fmaf(p, t, -1.420364380e-01f);
+  p = fmaf(p, t, 1.999261975e-01f);
+  p = fmaf(p, t, -3.333307207e-01f);
+  p = fmaf(p, t, 1.0f);
+  return r * p;
+}
+
+// atan2(y, x) over the whole circle: atan_unit of min/max, reflected into the octant
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  const float r = (mx > 0.0f) ? mn * rcp_approx(mx) : 0.0f;
+  float p = atan_unit(r);
+  p = (ay > ax) ? 1.57079632679f - p : p;
+  p = (x < 0.0f) ? 3.14159265359f - p : p;
+  return copysignf(p, y);
+}
+
+// u* and v* of the panel (x0, y0)-(x1, y1), px = x1 - x0, py = y1 - y0, seen from (tx, ty)
+__device__ __forceinline__ void panel_uv_star_fast(float x0, float y0, float x1, float y1, float px, float py,
+                                                   float tx, float ty, float& us, float& vs) {
+  const float dx0 = tx - x0, dy0 = ty - y0;
+  const float dx1 = tx - x1, dy1 = ty - y1;
+  us = atan2_poly(dx0 * py - dy0 * px, dx0 * dx1 + dy0 * dy1);   // cross product as in panel_uv_star
+  const float r1 = dx1 * dx1 + dy1 * dy1;
+  const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
+  const float sv = diff * rcp_approx(fmaf(2.0f, r1, diff));  // (rho - 1) / (rho + 1)
+  const float t = sv * sv;
+  float p = fmaf(t, 1.0f / 9.0f, 1.0f / 7.0f);
+  p = fmaf(p, t, 1.0f / 5.0f);
+  p = fmaf(p, t, 1.0f / 3.0f);
+  vs = fmaf(sv * t, p, sv);                                  // atanh(s), truncation < 1e-9
+  if (!(fabsf(sv) <= 0.2f)) {
+    const float q = diff / r1;
+    vs = (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
+  }
 }
 
 struct PanArgs {
@@ -114,18 +165,22 @@ __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, do
 // One thread per target, sources (panels or particles) staged through shared memory in tiles;
 // grid = (target blocks, source splits).  Compensated: FP32 partials over 32 sources folded
 // into two-sum pairs, FP64 out; plain: FP32 throughout.
+//   panels -> points: with the panel's unit tangent (tx, ty) and strengths (g, s), the sheet
+//     velocity (kernelu_1vs_0p) is u = u* A + v* B, v = v* A - u* B with A = g tx + s ty,
+//     B = s tx - g ty, formed once per panel when the tile is staged;
+//   points -> panels: the target panel's tangent is fixed per thread, so the particle sums
+//     are of w u* and w v* and the tangent is applied once at the end.
 template <bool COMP>
 __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
   __shared__ float4 sP[PAN_TILE];
   __shared__ float4 sQ[PAN_TILE];
-  __shared__ float sL[PAN_TILE];
   const int i = blockIdx.x * PAN_THREADS + threadIdx.x;
   const int sp = blockIdx.y;
   const int ic = i < a.nt ? i : a.nt - 1;
   // this thread's target: a point, or a panel (its geometry and inverse length)
   float tx = 0.0f, ty = 0.0f;
   float4 TP = make_float4(0, 0, 0, 0), TQ = make_float4(0, 0, 0, 0);
-  float tinv = 0.0f;
+  float tinv = 0.0f, tpx = 0.0f, tpy = 0.0f;
   if (a.mode == 0) {
     tx = a.tx[ic];
     ty = a.ty[ic];
@@ -133,6 +188,8 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
     TP = a.P[ic];
     TQ = a.Q[ic];
     tinv = 1.0f / a.plen[ic];
+    tpx = TP.z - TP.x;
+    tpy = TP.w - TP.y;
   }
   float au = 0.0f, av = 0.0f, hu = 0.0f, lu = 0.0f, hv = 0.0f, lv = 0.0f;
   const int t0 = sp * a.tiles_per_split;
@@ -142,28 +199,35 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
     for (int k = threadIdx.x; k < PAN_TILE; k += PAN_THREADS) {
       const int j = t * PAN_TILE + k;
       if (a.mode == 0) {
-        sP[k] = a.P[j];
-        sQ[k] = a.Q[j];
+        const float4 P = a.P[j], Q = a.Q[j];
+        sP[k] = P;
+        sQ[k] = make_float4(P.z - P.x, P.w - P.y, Q.z * Q.x + Q.w * Q.y, Q.w * Q.x - Q.z * Q.y);
       } else {
         sP[k] = a.pts[j];
       }
     }
     __syncthreads();
     for (int b = 0; b < PAN_TILE; b += PAN_COMP_BLOCK) {
+      if (a.mode == 0) {
 #pragma unroll 4
-      for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
-        float u, v;
-        if (a.mode == 0) {
-          panel_vel(sP[b + k], sQ[b + k], tx, ty, u, v);
-        } else {
-          // the panel is the "source" of kernelu_1v_0p with the particle strength, the particle
-          // the "target"; the sum is used with a minus sign (src/Influence.h:737-759)
-          const float4 s = sP[b + k];
-          const float4 q = make_float4(TQ.x, TQ.y, s.w, 0.0f);
-          panel_vel(TP, q, s.x, s.y, u, v);
+        for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
+          const float4 P = sP[b + k], Q = sQ[b + k];
+          float us, vs;
+          panel_uv_star_fast(P.x, P.y, P.z, P.w, Q.x, Q.y, tx, ty, us, vs);
+          au = fmaf(us, Q.z, fmaf(vs, Q.w, au));
+          av = fmaf(vs, Q.z, fmaf(-us, Q.w, av));
         }
-        au += u;
-        av += v;
+      } else {
+        // the panel is the "source" of kernelu_1v_0p with the particle strength, the particle
+        // the "target"; the sum is used with a minus sign (src/Influence.h:737-759)
+#pragma unroll 4
+        for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
+          const float4 q = sP[b + k];
+          float us, vs;
+          panel_uv_star_fast(TP.x, TP.y, TP.z, TP.w, tpx, tpy, q.x, q.y, us, vs);
+          au = fmaf(q.w, us, au);
+          av = fmaf(q.w, vs, av);
+        }
       }
       if (COMP) {
         two_sum_acc(hu, lu, au);
@@ -173,13 +237,15 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
       }
     }
   }
-  (void)sL;
   if (i >= a.nt) return;
   double su = COMP ? (double)hu + (double)lu : (double)au;
   double sv = COMP ? (double)hv + (double)lv : (double)av;
   if (a.mode == 1) {
-    su *= -(double)tinv;
-    sv *= -(double)tinv;
+    // (sum w u*, sum w v*) -> velocity along the fixed tangent, times -1/len
+    const double ux = TQ.x, uy = TQ.y;
+    const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
+    su = -vu * (double)tinv;
+    sv = -vv * (double)tinv;
   }
   if (a.nsplit == 1) {
     pan_store(a, i, su, sv);

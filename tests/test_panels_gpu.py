@@ -45,6 +45,40 @@ def test_points_affect_panels(ctx, golden, restatement, accum):
     assert rel_err(g["pt2p_u"], targ.pu) < TOLREF and rel_err(g["pt2p_v"], targ.pv) < TOLREF
 
 
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+def test_panel_sums_near_and_far_targets(ctx, restatement, accum):
+    """Targets from a hundredth of a panel length off the body to a thousand radii away mix
+    the series form of the log (|s| <= 0.2) and the near forms inside one warp."""
+    rng = np.random.default_rng(41)
+    c = og.circle_panels(256)
+    surf = og.Surfaces(c.nx, c.ny, c.idx, vs=rng.normal(0, 1, 256).astype(np.float32),
+                       ss=rng.normal(0, 1, 256).astype(np.float32))
+    h = np.pi / 256
+    n = 4096
+    rad = 0.5 + np.concatenate([rng.choice([-1, 1], n // 2) * h * 10.0 ** rng.uniform(-2, 1, n // 2),
+                                10.0 ** rng.uniform(-1, 3, n // 2)])
+    th = rng.uniform(0, 2 * np.pi, n)
+    x, y = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    targ = og.Points(x, y)
+    og.panels_affect_points(surf, targ, og.ExecEnv(accum=accum, context=ctx))
+    u64, v64 = restatement.panels_affect_points(surf.nx, surf.ny, surf.idx, surf.vs, surf.ss, x, y, fp64=True)
+    # per target: relative to the largest term of that target's sum
+    scale = np.abs(surf.vs).max() + np.abs(surf.ss).max()
+    assert np.max(np.abs(targ.u - u64)) < 2e-5 * scale * np.pi
+    # far targets: sums of 256 random-sign terms cancel to a small result, so plain FP32
+    # accumulation shows its rounding; the compensated sums hold the FP64 restatement's value
+    far = rad > 2.0
+    tol = TOL64 if accum == og.COMPENSATED else 5e-5
+    assert rel_err(u64[far], targ.u[far]) < tol and rel_err(v64[far], targ.v[far]) < tol
+    # points -> panels with the same cloud as particles
+    s = rng.normal(0, 1e-2, n).astype(np.float32)
+    surf2 = og.circle_panels(256)
+    og.points_affect_panels(og.Points(x, y, np.full(n, 0.01, np.float32), s), surf2,
+                            og.ExecEnv(accum=accum, context=ctx))
+    pu64, pv64 = restatement.points_affect_panels(x, y, s, surf2.nx, surf2.ny, surf2.idx, fp64=True)
+    assert rel_err(pu64, surf2.pu) < 2e-5 and rel_err(pv64, surf2.pv) < 2e-5
+
+
 def test_points_affect_panels_many_sources_split(ctx, restatement):
     """200k particles on 256 panels: exercises the source splits and the FP64 split reduction."""
     rng = np.random.default_rng(31)
