@@ -75,8 +75,8 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
  * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 /* Kernel variant for particle-on-particle sums.  AUTO uses the packed-FP32 kernels (two
- * targets per f32x2 register pair) where they exist (velocity for every core but the compact
- * exponential, 4 target pairs per thread for the Gaussian core and 2 for the others; velocity
+ * targets per f32x2 register pair) where they exist (velocity for every core, 4 target pairs
+ * per thread for the Gaussian and compact-exponential cores and 2 for the others; velocity
  * gradient, vorticity and shear for the Gaussian core) and the generic kernels elsewhere;
  * GENERIC forces the generic kernels (and the one-kernel-per-step GMRES); PACKED2 / PACKED3 /
  * PACKED4 pick 2, 3 or 4 target pairs per thread for the packed velocity kernels. */
@@ -84,13 +84,14 @@ int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 #define OBS_VARIANT_GENERIC 1
 #define OBS_VARIANT_PACKED2 2
 #define OBS_VARIANT_PACKED3 3   /* Gaussian only; other cores use 2 */
-#define OBS_VARIANT_PACKED4 4
+#define OBS_VARIANT_PACKED4 4   /* Gaussian, RM and compact exponential; other cores use 2 */
 int obs_set_kernel_variant(obs_context* ctx, int variant);
-/* Processing order inside a packed Gaussian velocity sum.  Binning sorts points into a
- * 256 x 256 Morton-ordered grid over their bounding box (a stable sort), so that each warp's
- * targets and each block of 32 sources lie close together; (warp, block) pairs farther apart
- * than 4 core radii then take the reference's far-field form G/d^2 (d^2/s^2 > 16) without the
- * exponential.  Results are always written in the caller's order.
+/* Processing order inside a packed Gaussian or compact-exponential velocity sum.  Binning
+ * sorts points into a 256 x 256 Morton-ordered grid over their bounding box (a stable sort), so
+ * that each warp's targets and each block of 32 sources lie close together; (warp, block) pairs
+ * beyond the core's far radius (4 core radii for the Gaussian, 16^(1/3) for the compact
+ * exponential) then take the reference's far-field form G/d^2 without the exponential.
+ * Results are always written in the caller's order.
  *   INPUT          : caller's order for targets and sources;
  *   BINNED_TARGETS : binned targets; results are bit-identical to INPUT;
  *   BINNED         : binned targets and sources; sources are summed in the binned order, so

@@ -132,16 +132,16 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int kcore = (res == RES_PSI) ? CORE_RM : rq.core;
   cudaStream_t st = ctx->stream;
 
-  // ---- kernel choice: the packed-FP32 kernels serve velocity-only Gaussian / RM sums
+  // ---- kernel choice: the packed-FP32 kernels serve velocity sums of every core and the
+  // Gaussian gradient-type results
   const int variant = ctx->kernel_variant;
-  // AUTO takes the packed kernels for every core but the compact exponential, whose generic
-  // kernel is faster (N = 262144 patch: 1627 vs 1363 Ginter/s with uniform radii)
-  const bool packed = variant != OBS_VARIANT_GENERIC && packed_supported(rq.core, res) &&
-                      !(variant == OBS_VARIANT_AUTO && rq.core == CORE_CEXP);
+  const bool packed = variant != OBS_VARIANT_GENERIC && packed_supported(rq.core, res);
   // target pairs per thread: AUTO takes 4 for the Gaussian core (1M patch, Morton order: 4107 vs
-  // 3788 Ginter/s compensated, 4380 vs 4333 plain against 2 pairs) and 2 for RM
+  // 3788 Ginter/s compensated, 4380 vs 4333 plain against 2 pairs) and the compact exponential
+  // (whose far blocks run the same 1/d^2 form), 2 for the others
+  const bool masked_core = rq.core == CORE_GAUSS || rq.core == CORE_CEXP;
   int np = 2;
-  if (variant == OBS_VARIANT_PACKED4 || (variant == OBS_VARIANT_AUTO && rq.core == CORE_GAUSS)) np = 4;
+  if (variant == OBS_VARIANT_PACKED4 || (variant == OBS_VARIANT_AUTO && masked_core)) np = 4;
   else if (variant == OBS_VARIANT_PACKED3 && rq.core == CORE_GAUSS) np = 3;
   if (packed && res != RES_VEL) np = packed_res_np(res);
   auto launch = [&](const P2PArgs* args, int g, int* occ_out) -> cudaError_t {
@@ -167,9 +167,10 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int nitems = ntb * nsplit;
   const int grid = std::min(nitems, slots);
   const int nc = ncomp_of(res);
-  // spatial (Morton) order lets the packed Gaussian kernel skip the exponential for far (warp, block) pairs
+  // spatial (Morton) order lets the packed Gaussian and compact-exponential kernels skip the
+  // exponential for far (warp, block) pairs
   const int order = ctx->target_order;
-  const bool gauss_packed = packed && rq.core == CORE_GAUSS;
+  const bool gauss_packed = packed && masked_core;
   const bool big = (double)rq.ns * rq.nt >= 2e9 && rq.nt >= 4096 && rq.ns >= 4096;
   const bool bin_t = gauss_packed && (order == OBS_ORDER_BINNED || order == OBS_ORDER_BINNED_TARGETS ||
                                       (order == OBS_ORDER_AUTO && big));

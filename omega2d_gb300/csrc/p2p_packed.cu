@@ -76,7 +76,9 @@ cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PAr
     case CORE_WL: return packed_dispatch_np<CORE_WL, 2>(thick, comp, a, grid, st, occ);
     case CORE_V3: return packed_dispatch_np<CORE_V3, 2>(thick, comp, a, grid, st, occ);
     case CORE_SING: return packed_dispatch_np<CORE_SING, 2>(thick, comp, a, grid, st, occ);
-    case CORE_CEXP: return packed_dispatch_np<CORE_CEXP, 2>(thick, comp, a, grid, st, occ);
+    case CORE_CEXP:
+      return np == 4 ? packed_dispatch_np<CORE_CEXP, 4>(thick, comp, a, grid, st, occ)
+                     : packed_dispatch_np<CORE_CEXP, 2>(thick, comp, a, grid, st, occ);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -175,6 +175,46 @@ __device__ __forceinline__ void wl_block(const float4* __restrict__ blk, const P
   }
 }
 
+// compact exponential, uniform radii, one 32-source block with some pair inside the far
+// radius (blocks entirely beyond it take gauss_block<false>: both cores are exactly 1/d^2
+// there): y = (d^2/s^2)^(3/2); y > 16 -> 1/d^2; y < 0.001 -> (d/s^3)(1 - y/2); else
+// (1 - e^-y)/d^2, the forms of core_eval
+template <int NP>
+__device__ __forceinline__ void cexp_block(const float4* __restrict__ blk, const PackedUni& q,
+                                           const float2 (&ntx)[NP], const float2 (&nty)[NP], float2 (&u)[NP],
+                                           float2 (&vn)[NP]) {
+  const float2 ucf2 = f2(q.ucf, q.ucf);
+  const float2 nl2e = f2(-kLog2e, -kLog2e);
+#pragma unroll 2
+  for (int jj = 0; jj < PK_BLK; ++jj) {
+    const float4 A = blk[PK_ELEM * jj];
+    const float4 B = blk[PK_ELEM * jj + 1];
+    const float2 sx2 = f2(A.x, A.y), sy2 = f2(A.z, A.w);
+    const float2 g2 = f2(B.x, B.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 ndx = __fadd2_rn(sx2, ntx[p]);
+      const float2 ndy = __fadd2_rn(sy2, nty[p]);
+      float2 d2 = __fmul2_rn(ndy, ndy);
+      d2 = __ffma2_rn(ndx, ndx, d2);
+      const float2 x = __fmul2_rn(d2, ucf2);
+      const float2 sq = f2(sqrt_a(x.x), sqrt_a(x.y));
+      const float2 y = __fmul2_rn(x, sq);
+      const float2 t = __fmul2_rn(y, nl2e);
+      const float2 e = f2(ex2_a(t.x), ex2_a(t.y));
+      const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
+      float2 k = __ffma2_rn(make_float2(-ood2.x, -ood2.y), e, ood2);
+      k.x = (y.x > 16.0f) ? ood2.x : k.x;
+      k.y = (y.y > 16.0f) ? ood2.y : k.y;
+      k.x = (y.x < 0.001f) ? sq.x * q.ucf * fmaf(-0.5f, y.x, 1.0f) : k.x;
+      k.y = (y.y < 0.001f) ? sq.y * q.ucf * fmaf(-0.5f, y.y, 1.0f) : k.y;
+      const float2 r2 = __fmul2_rn(g2, k);
+      u[p] = __ffma2_rn(r2, ndy, u[p]);
+      vn[p] = __ffma2_rn(r2, ndx, vn[p]);
+    }
+  }
+}
+
 // varying radii: the reference forms per target, one 32-source block
 template <int CORE, bool THICK, int NP>
 __device__ __forceinline__ void general_block(const float4* __restrict__ blk, const float2 (&ntx)[NP],
@@ -237,7 +277,9 @@ p2p_packed_kernel(const P2PArgs a) {
   q.thr_far = -16.0f * kLog2e;                     // x > 16     <=>  t < thr_far
   q.cfl2 = f2(q.cfl, q.cfl);
   q.s22 = f2(q.us2, q.us2);
-  const float lim = 16.16f * q.us2;               // near test with a 1 % margin (d < 4.02 s)
+  // near test with a 1 % margin: Gaussian far beyond d^2/s^2 = 16, compact exponential beyond
+  // (d/s)^3 = 16, i.e. d^2/s^2 = 16^(2/3) = 6.3496
+  const float lim = (CORE == CORE_CEXP ? 6.4131f : 16.16f) * q.us2;
 
   uint32_t kt = 0;
   for (;;) {
@@ -296,7 +338,7 @@ p2p_packed_kernel(const P2PArgs a) {
         return;
       }
       const float4* tl = &tile[st][0];
-      if (CORE == CORE_GAUSS && unif) {
+      if ((CORE == CORE_GAUSS || CORE == CORE_CEXP) && unif) {
         // near-mask of this warp: bit j of word b set when source b*32+j may be within 4 s
 #pragma unroll
         for (int b = 0; b < PK_NB; ++b) {
@@ -326,6 +368,13 @@ p2p_packed_kernel(const P2PArgs a) {
         } else if constexpr (CORE == CORE_WL) {
           if (unif) wl_block<NP>(blk, q, ntx, nty, u, vn);
           else general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+        } else if constexpr (CORE == CORE_CEXP) {
+          if (unif) {
+            if (smask[warp][b] == 0u) gauss_block<false, NP>(blk, q, ntx, nty, u, vn);
+            else cexp_block<NP>(blk, q, ntx, nty, u, vn);
+          } else {
+            general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
+          }
         } else {
           general_block<CORE, THICK, NP>(blk, ntx, nty, tz, u, vn);
         }

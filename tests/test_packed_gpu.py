@@ -18,7 +18,8 @@ def cloud(rng, n, uniform):
 CORE_VARIANTS = ([(c, v) for c in (og.CORE_GAUSSIAN, og.CORE_RM)
                   for v in (og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4)]
                  + [(c, og.VARIANT_PACKED2) for c in (og.CORE_V2, og.CORE_WL, og.CORE_V3, og.CORE_SINGULAR,
-                                                      og.CORE_COMPACT_EXP)])
+                                                      og.CORE_COMPACT_EXP)]
+                 + [(og.CORE_COMPACT_EXP, og.VARIANT_PACKED4)])
 
 
 @pytest.mark.parametrize("core,variant", CORE_VARIANTS)
@@ -74,39 +75,45 @@ def _vel(ctx, src, tx, ty, tr, core, accum, order, variant):
     return t.u, t.v
 
 
+# the far radius of each masked core and an offset that lands in its exponential branch
+MASKED = {og.CORE_GAUSSIAN: 3.0, og.CORE_COMPACT_EXP: 1.5}
+
+
+@pytest.mark.parametrize("core", list(MASKED))
 @pytest.mark.parametrize("sigma", [1e-4, 2e-3, 0.05])
 @pytest.mark.parametrize("thick", [True, False])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
 @pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED3, og.VARIANT_PACKED4])
-def test_binned_order_identities(ctx, sigma, thick, accum, variant):
+def test_binned_order_identities(ctx, core, sigma, thick, accum, variant):
     """Binned target order gives the same bits as the caller's order: the far-block fast form and
     the full form agree pair by pair, and each target's sum runs over the sources in one order."""
-    rng = np.random.default_rng(int(sigma * 1e5) + 7 * thick + accum + variant)
+    rng = np.random.default_rng(int(sigma * 1e5) + 7 * thick + accum + variant + core)
     ns, nt = 9000, 7001
     sx, sy = rng.normal(0, 0.3, (2, ns)).astype(np.float32)
     ss = rng.normal(0, 1e-3, ns).astype(np.float32)
     sr = np.full(ns, sigma, np.float32)
     tx, ty = rng.normal(0, 0.3, (2, nt)).astype(np.float32)
     tx[:300], ty[:300] = sx[:300], sy[:300]                        # coincident pairs: x < 0.001
-    tx[300:600] = sx[300:600] + 3 * sigma                          # the exponential branch
+    tx[300:600] = sx[300:600] + MASKED[core] * sigma               # the exponential branch
     ty[300:600] = sy[300:600]
     tr = np.full(nt, sigma, np.float32) if thick else None
     src = og.Points(sx, sy, sr, ss)
-    a = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_INPUT, variant)
-    b = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED_TARGETS, variant)
+    a = _vel(ctx, src, tx, ty, tr, core, accum, og.ORDER_INPUT, variant)
+    b = _vel(ctx, src, tx, ty, tr, core, accum, og.ORDER_BINNED_TARGETS, variant)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     # binned sources change the summation order only: reproducible, and equal up to rounding
-    c = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED, variant)
-    d = _vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED, variant)
+    c = _vel(ctx, src, tx, ty, tr, core, accum, og.ORDER_BINNED, variant)
+    d = _vel(ctx, src, tx, ty, tr, core, accum, og.ORDER_BINNED, variant)
     assert np.array_equal(c[0], d[0]) and np.array_equal(c[1], d[1])
     tol = 1e-6 if accum == og.COMPENSATED else 2e-5
     assert rel_err(a[0], c[0]) < tol and rel_err(a[1], c[1]) < tol
 
 
+@pytest.mark.parametrize("core", list(MASKED))
 @pytest.mark.parametrize("sigma", [1e-4, 2e-3])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
-def test_binned_targets_vs_fp64(ctx, restatement, sigma, accum):
-    rng = np.random.default_rng(11 + accum)
+def test_binned_targets_vs_fp64(ctx, restatement, core, sigma, accum):
+    rng = np.random.default_rng(11 + accum + core)
     ns, nt = 6000, 5003
     sx, sy = rng.normal(0, 0.3, (2, ns)).astype(np.float32)
     ss = rng.normal(0, 1e-3, ns).astype(np.float32)
@@ -115,9 +122,8 @@ def test_binned_targets_vs_fp64(ctx, restatement, sigma, accum):
     tx[:200], ty[:200] = sx[:200], sy[:200]
     tx[200:400], ty[200:400] = sx[200:400] + 2.5 * sigma, sy[200:400]
     tr = np.full(nt, sigma, np.float32)
-    u, v = _vel(ctx, og.Points(sx, sy, sr, ss), tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_BINNED,
-                og.VARIANT_AUTO)
-    u64, v64, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, tx, ty, tr, fp64=True,
+    u, v = _vel(ctx, og.Points(sx, sy, sr, ss), tx, ty, tr, core, accum, og.ORDER_BINNED, og.VARIANT_AUTO)
+    u64, v64, _ = restatement.points_affect_points(core, 1, sx, sy, sr, ss, tx, ty, tr, fp64=True,
                                                    tu=np.full(nt, 0.5), tv=np.zeros(nt))
     u64, v64 = 1.0 + u64 / (2 * np.pi), -0.25 + v64 / (2 * np.pi)
     tol = 2e-6 if accum == og.COMPENSATED else 2e-5
