@@ -75,16 +75,17 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
  * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 /* Kernel variant for particle-on-particle sums.  AUTO uses the packed-FP32 kernels (two
- * targets per f32x2 register pair) where they exist (velocity for every core, 4 target pairs
- * per thread for the Gaussian and compact-exponential cores and 2 for the others; velocity
- * gradient, vorticity and shear for the Gaussian core) and the generic kernels elsewhere;
- * GENERIC forces the generic kernels (and the one-kernel-per-step GMRES); PACKED2 / PACKED3 /
- * PACKED4 pick 2, 3 or 4 target pairs per thread for the packed velocity kernels. */
+ * targets per f32x2 register pair) where they exist -- velocity for every core, with 4 target
+ * pairs per thread (2 for Vatistas n=3 and the singular core); velocity gradient, vorticity
+ * and shear for the Gaussian core -- and the generic kernels elsewhere.  GENERIC forces the
+ * generic kernels (and the one-kernel-per-step GMRES); PACKED2 / PACKED3 / PACKED4 pick 2, 3
+ * (Gaussian only; 2 for the other cores) or 4 target pairs per thread for the packed velocity
+ * kernels. */
 #define OBS_VARIANT_AUTO 0
 #define OBS_VARIANT_GENERIC 1
 #define OBS_VARIANT_PACKED2 2
-#define OBS_VARIANT_PACKED3 3   /* Gaussian only; other cores use 2 */
-#define OBS_VARIANT_PACKED4 4   /* Gaussian, RM and compact exponential; other cores use 2 */
+#define OBS_VARIANT_PACKED3 3
+#define OBS_VARIANT_PACKED4 4
 int obs_set_kernel_variant(obs_context* ctx, int variant);
 /* Processing order inside a packed Gaussian or compact-exponential velocity sum.  Binning
  * sorts points into a 256 x 256 Morton-ordered grid over their bounding box (a stable sort), so

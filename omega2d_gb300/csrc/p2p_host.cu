@@ -136,13 +136,10 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   // Gaussian gradient-type results
   const int variant = ctx->kernel_variant;
   const bool packed = variant != OBS_VARIANT_GENERIC && packed_supported(rq.core, res);
-  // target pairs per thread: AUTO takes 4 for the Gaussian core (1M patch, Morton order: 4107 vs
-  // 3788 Ginter/s compensated, 4380 vs 4333 plain against 2 pairs) and the compact exponential
-  // (whose far blocks run the same 1/d^2 form), 2 for the others
+  // target pairs per thread: one table (packed_np) sizes the target blocks here and picks the
+  // kernel instantiation in packed_dispatch
   const bool masked_core = rq.core == CORE_GAUSS || rq.core == CORE_CEXP;
-  int np = 2;
-  if (variant == OBS_VARIANT_PACKED4 || (variant == OBS_VARIANT_AUTO && masked_core)) np = 4;
-  else if (variant == OBS_VARIANT_PACKED3 && rq.core == CORE_GAUSS) np = 3;
+  int np = packed_np(rq.core, variant);
   if (packed && res != RES_VEL) np = packed_res_np(res);
   auto launch = [&](const P2PArgs* args, int g, int* occ_out) -> cudaError_t {
     if (!packed) return dispatch(rq.core, thick, res, comp, args, g, st, occ_out);

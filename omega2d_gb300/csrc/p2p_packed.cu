@@ -60,27 +60,37 @@ bool packed_supported(int core, int res) {
   return core == CORE_GAUSS && (res == RES_GRAD || res == RES_VORT || res == RES_SHEAR);
 }
 
+int packed_np(int core, int variant) {
+  if (variant == OBS_VARIANT_PACKED2) return 2;
+  if (variant == OBS_VARIANT_PACKED3) return core == CORE_GAUSS ? 3 : 2;
+  if (variant == OBS_VARIANT_PACKED4) return 4;
+  // AUTO, from the 1M Gaussian patch (compensated, Ginter/s with 4 vs 2 target pairs):
+  // Gaussian 4111 vs 3785 (Morton order), RM 4116 vs 4017, Vatistas-2 3810 vs 3776,
+  // Winckelmans-Leonard 2996 vs 2762; the singular core 3694 vs 3732 and Vatistas-3 keep 2
+  return (core == CORE_V3 || core == CORE_SING) ? 2 : 4;
+}
+
+// np must come from packed_np: the host sizes the target blocks with it
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
                             int* occ) {
-  if (core == CORE_GAUSS) {
-    if (np == 4) return packed_dispatch_np<CORE_GAUSS, 4>(thick, comp, a, grid, st, occ);
-    if (np == 3) return packed_dispatch_np<CORE_GAUSS, 3>(thick, comp, a, grid, st, occ);
-    return packed_dispatch_np<CORE_GAUSS, 2>(thick, comp, a, grid, st, occ);
-  }
-  if (core == CORE_RM) {
-    return np == 4 ? packed_dispatch_np<CORE_RM, 4>(thick, comp, a, grid, st, occ)
-                   : packed_dispatch_np<CORE_RM, 2>(thick, comp, a, grid, st, occ);
-  }
-  switch (core) {   // the other cores: 2 target pairs per thread
-    case CORE_V2: return packed_dispatch_np<CORE_V2, 2>(thick, comp, a, grid, st, occ);
-    case CORE_WL: return packed_dispatch_np<CORE_WL, 2>(thick, comp, a, grid, st, occ);
-    case CORE_V3: return packed_dispatch_np<CORE_V3, 2>(thick, comp, a, grid, st, occ);
-    case CORE_SING: return packed_dispatch_np<CORE_SING, 2>(thick, comp, a, grid, st, occ);
-    case CORE_CEXP:
-      return np == 4 ? packed_dispatch_np<CORE_CEXP, 4>(thick, comp, a, grid, st, occ)
-                     : packed_dispatch_np<CORE_CEXP, 2>(thick, comp, a, grid, st, occ);
+  if (np == 3 && core != CORE_GAUSS) return cudaErrorInvalidValue;
+  if (np != 2 && np != 3 && np != 4) return cudaErrorInvalidValue;
+#define OBS_PACKED_NP24(C)                                                      \
+  return np == 4 ? packed_dispatch_np<C, 4>(thick, comp, a, grid, st, occ)      \
+                 : packed_dispatch_np<C, 2>(thick, comp, a, grid, st, occ)
+  switch (core) {
+    case CORE_GAUSS:
+      if (np == 3) return packed_dispatch_np<CORE_GAUSS, 3>(thick, comp, a, grid, st, occ);
+      OBS_PACKED_NP24(CORE_GAUSS);
+    case CORE_RM: OBS_PACKED_NP24(CORE_RM);
+    case CORE_V2: OBS_PACKED_NP24(CORE_V2);
+    case CORE_WL: OBS_PACKED_NP24(CORE_WL);
+    case CORE_V3: OBS_PACKED_NP24(CORE_V3);
+    case CORE_SING: OBS_PACKED_NP24(CORE_SING);
+    case CORE_CEXP: OBS_PACKED_NP24(CORE_CEXP);
     default: return cudaErrorInvalidValue;
   }
+#undef OBS_PACKED_NP24
 }
 
 cudaError_t packed_launch_pack(const float* sx, const float* sy, const float* sr, const float* ss, const int* perm,
