@@ -248,7 +248,8 @@ __global__ void __launch_bounds__(P2P_THREADS, 4) p2p_packed_res_kernel(const P2
 }  // namespace
 
 int packed_res_np(int res) {
-  return res == RES_GRAD ? PRes<RES_GRAD>::NP : PRes<RES_VORT>::NP;
+  if (res == RES_GRAD) return PRes<RES_GRAD>::NP;
+  return res == RES_SHEAR ? PRes<RES_SHEAR>::NP : PRes<RES_VORT>::NP;
 }
 
 cudaError_t packed_res_dispatch(int res, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
