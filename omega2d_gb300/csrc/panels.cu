@@ -141,12 +141,12 @@ struct PanArgs {
   const float* plen;    // panel lengths (points -> panels)
   const float4* pts;    // packed particles (x, y, z, strength) for points -> panels
   int nsrc;             // panels (pan->pt) or particles (pt->pan), padded count
-  int ntiles;
+  int nblk;             // 32-source blocks (nsrc / 32)
   const float* tx;
   const float* ty;
   int nt;               // targets (points or panels)
   int nsplit;
-  int tiles_per_split;
+  int blks_per_split;
   float* out_u;
   float* out_v;
   void* part;
@@ -192,12 +192,14 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
     tpy = TP.w - TP.y;
   }
   float au = 0.0f, av = 0.0f, hu = 0.0f, lu = 0.0f, hv = 0.0f, lv = 0.0f;
-  const int t0 = sp * a.tiles_per_split;
-  const int t1 = min(t0 + a.tiles_per_split, a.ntiles);
-  for (int t = t0; t < t1; ++t) {
+  // this split's 32-source blocks [b0, b1), staged PAN_TILE sources at a time
+  const int b0 = sp * a.blks_per_split;
+  const int b1 = min(b0 + a.blks_per_split, a.nblk);
+  for (int base = b0; base < b1; base += PAN_TILE / PAN_COMP_BLOCK) {
+    const int ns = min(PAN_TILE, (b1 - base) * PAN_COMP_BLOCK);
     __syncthreads();
-    for (int k = threadIdx.x; k < PAN_TILE; k += PAN_THREADS) {
-      const int j = t * PAN_TILE + k;
+    for (int k = threadIdx.x; k < ns; k += PAN_THREADS) {
+      const int j = base * PAN_COMP_BLOCK + k;
       if (a.mode == 0) {
         const float4 P = a.P[j], Q = a.Q[j];
         sP[k] = P;
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
       }
     }
     __syncthreads();
-    for (int b = 0; b < PAN_TILE; b += PAN_COMP_BLOCK) {
+    for (int b = 0; b < ns; b += PAN_COMP_BLOCK) {
       if (a.mode == 0) {
 #pragma unroll 4
         for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
@@ -282,6 +284,37 @@ __global__ void pan_reduce_kernel(const PanArgs a) {
     sv = fv;
   }
   pan_store(a, i, su, sv);
+}
+
+// The same reduction with one warp per target, for many splits: lanes take every 32nd split,
+// then a shuffle tree (FP64 adds are slow on this GPU, so the serial chain is kept short)
+template <bool COMP>
+__global__ void pan_reduce_warp_kernel(const PanArgs a) {
+  const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= a.nt) return;
+  double su = 0.0, sv = 0.0;
+  if (COMP) {
+    const double* p = static_cast<const double*>(a.part);
+    for (int k = lane; k < a.nsplit; k += 32) {
+      su += p[(size_t)k * a.nt + i];
+      sv += p[((size_t)a.nsplit + k) * a.nt + i];
+    }
+  } else {
+    const float* p = static_cast<const float*>(a.part);
+    float fu = 0.0f, fv = 0.0f;
+    for (int k = lane; k < a.nsplit; k += 32) {
+      fu += p[(size_t)k * a.nt + i];
+      fv += p[((size_t)a.nsplit + k) * a.nt + i];
+    }
+    su = fu;
+    sv = fv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    su += __shfl_xor_sync(0xffffffffu, su, o);
+    sv += __shfl_xor_sync(0xffffffffu, sv, o);
+  }
+  if (lane == 0) pan_store(a, i, su, sv);
 }
 
 // Particles -> float4 (x, y, 0, strength), padded with zero-strength particles far away.
@@ -385,21 +418,22 @@ int pack_panels(obs_context* ctx, const PanelSet& ps, const float* vs, const flo
 
 namespace {
 
-int plan_splits(obs_context* ctx, int ntarg, int ntiles, int nblocks_per_split) {
-  const int want = 8 * 4 * ctx->num_sms;   // ~32 blocks per SM worth of (target, split) blocks
-  int nsplit = std::max(1, (want + nblocks_per_split - 1) / nblocks_per_split);
-  nsplit = std::min(nsplit, std::max(1, ntiles / 2));
-  (void)ntarg;
-  return nsplit;
+// source splits: enough (target block, split) blocks for ~32 per SM, each split at least one
+// 32-source block (small problems -- a few thousand panels -- need the fine splits to fill the
+// GPU at all)
+int plan_splits(obs_context* ctx, int nblk, int tblocks) {
+  const int want = 8 * 4 * ctx->num_sms;
+  const int nsplit = std::max(1, (want + tblocks - 1) / tblocks);
+  return std::min(nsplit, std::max(1, nblk));
 }
 
 int run_pan(obs_context* ctx, PanArgs& a, bool comp, size_t scratch_off) {
   const int tblocks = (a.nt + PAN_THREADS - 1) / PAN_THREADS;
-  int nsplit = plan_splits(ctx, a.nt, a.ntiles, tblocks);
-  const int tps = (a.ntiles + nsplit - 1) / nsplit;
-  nsplit = (a.ntiles + tps - 1) / tps;
+  int nsplit = plan_splits(ctx, a.nblk, tblocks);
+  const int bps = (a.nblk + nsplit - 1) / nsplit;
+  nsplit = (a.nblk + bps - 1) / bps;
   a.nsplit = nsplit;
-  a.tiles_per_split = tps;
+  a.blks_per_split = bps;
   if (nsplit > 1) {
     const size_t bytes = (size_t)2 * nsplit * a.nt * (comp ? sizeof(double) : sizeof(float));
     int s = ctx->work.ensure(scratch_off + bytes, ctx->stream);
@@ -421,7 +455,13 @@ int launch_pan(obs_context* ctx, PanArgs& a, bool comp) {
   ctx->launches++;
   timing_main_end(ctx);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && a.nsplit > 1) {
+  if (e == cudaSuccess && a.nsplit > 16) {
+    const unsigned blocks = (unsigned)(((size_t)a.nt * 32 + 255) / 256);
+    if (comp) pan_reduce_warp_kernel<true><<<blocks, 256, 0, ctx->stream>>>(a);
+    else pan_reduce_warp_kernel<false><<<blocks, 256, 0, ctx->stream>>>(a);
+    ctx->launches++;
+    e = cudaGetLastError();
+  } else if (e == cudaSuccess && a.nsplit > 1) {
     if (comp) pan_reduce_kernel<true><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
     else pan_reduce_kernel<false><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
     ctx->launches++;
@@ -442,7 +482,7 @@ int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* 
   const size_t off_part = hdr + 2 * pbytes;
   PanArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.nsrc = np_pad; a.ntiles = ntiles;
+  a.nsrc = np_pad; a.nblk = np_pad / PAN_COMP_BLOCK;
   a.tx = tx; a.ty = ty; a.nt = nt;
   a.out_u = tu; a.out_v = tv;
   a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
@@ -478,7 +518,7 @@ int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const fl
   const size_t off_part = off_pts + (size_t)ns_pad * sizeof(float4);
   PanArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.nsrc = ns_pad; a.ntiles = ntiles;
+  a.nsrc = ns_pad; a.nblk = ns_pad / PAN_COMP_BLOCK;
   a.nt = np;
   a.out_u = pu; a.out_v = pv;
   a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;

@@ -7,8 +7,8 @@
 // from node 0 to node 1, pushed 1e-4 along the panel normal into the fluid (the bases of
 // compute_bases, src/Surfaces.h:682-724); panels_affect_points then runs on those points and
 // the first npan point velocities are added to the npan panel velocities, index by index.
-// Here one block builds the first npan points (a block-wide scan of the per-panel counts) and
-// the panel kernel of panels.cu accumulates straight into the panel velocities.
+// Here the first npan points are built on the device (per-panel counts, one scan, per-panel
+// emission) and the panel kernel of panels.cu accumulates straight into the panel velocities.
 #include <cmath>
 
 #include "obs_context.h"
@@ -48,18 +48,30 @@ __device__ __forceinline__ long long shed_count(float len, float len0) {
   return 1 + c;
 }
 
-__global__ void __launch_bounds__(1024) collocation_kernel(const float* __restrict__ nx, const float* __restrict__ ny,
-                                                           int nnodes, const unsigned* __restrict__ idx, int npan,
-                                                           float* __restrict__ px, float* __restrict__ py,
-                                                           int* status) {
+// Collocation points in three grid-wide steps (FP64 runs slowly on this GPU, so each panel's
+// FP64 divisions happen once, on many SMs): per-panel geometry and shed count; a one-block
+// exclusive scan of the counts; per-panel emission of its points below index npan.
+__global__ void shed_kernel(const float* __restrict__ nx, const float* __restrict__ ny, int nnodes,
+                            const unsigned* __restrict__ idx, int npan, float4* __restrict__ geo,
+                            float2* __restrict__ nrm, long long* __restrict__ cnt, int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npan) return;
+  const float len0 = panel_geom(nx, ny, idx, nnodes, 0, status).len;
+  const PanelGeom g = panel_geom(nx, ny, idx, nnodes, i, status);
+  geo[i] = make_float4(g.x0, g.y0, g.x1, g.y1);
+  nrm[i] = make_float2(g.nx, g.ny);
+  cnt[i] = shed_count(g.len, len0);
+}
+
+__global__ void __launch_bounds__(1024) shed_scan_kernel(const long long* __restrict__ cnt, int npan,
+                                                         long long* __restrict__ off) {
   __shared__ long long wsum[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int per = (npan + 1023) / 1024;
   const int lo = min(npan, t * per), hi = min(npan, lo + per);
-  const float len0 = panel_geom(nx, ny, idx, nnodes, 0, status).len;
-  long long cnt = 0;
-  for (int i = lo; i < hi; ++i) cnt += shed_count(panel_geom(nx, ny, idx, nnodes, i, status).len, len0);
-  long long incl = cnt;
+  long long c = 0;
+  for (int i = lo; i < hi; ++i) c += cnt[i];
+  long long incl = c;
   for (int o = 1; o < 32; o <<= 1) {
     const long long q = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += q;
@@ -75,16 +87,29 @@ __global__ void __launch_bounds__(1024) collocation_kernel(const float* __restri
     wsum[lane] = x;
   }
   __syncthreads();
-  long long m = incl - cnt + (w ? wsum[w - 1] : 0);
-  const float off = 0.0001f;
-  for (int i = lo; i < hi && m < npan; ++i) {
-    const PanelGeom g = panel_geom(nx, ny, idx, nnodes, i, status);
-    const long long ns = shed_count(g.len, len0);
-    for (long long j = 0; j < ns && m < npan; ++j, ++m) {
-      const float wt = (float)(1 + 2 * j) / (float)(2 * ns);
-      px[m] = (float)((double)(wt * g.x1) + (1.0 - (double)wt) * (double)g.x0 + (double)(off * g.nx));
-      py[m] = (float)((double)(wt * g.y1) + (1.0 - (double)wt) * (double)g.y0 + (double)(off * g.ny));
-    }
+  long long m = incl - c + (w ? wsum[w - 1] : 0);
+  for (int i = lo; i < hi; ++i) {
+    off[i] = m;
+    m += cnt[i];
+  }
+}
+
+// nshed points per panel at weights (1+2j)/(2 nshed) from node 0, pushed 1e-4 along the normal
+__global__ void emit_kernel(const float4* __restrict__ geo, const float2* __restrict__ nrm,
+                            const long long* __restrict__ cnt, const long long* __restrict__ off, int npan,
+                            float* __restrict__ px, float* __restrict__ py) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npan) return;
+  long long m = off[i];
+  const long long ns = cnt[i];
+  if (m >= npan) return;
+  const float4 g = geo[i];
+  const float2 n = nrm[i];
+  const float offd = 0.0001f;
+  for (long long j = 0; j < ns && m < npan; ++j, ++m) {
+    const float wt = (float)(1 + 2 * j) / (float)(2 * ns);
+    px[m] = (float)((double)(wt * g.z) + (1.0 - (double)wt) * (double)g.x + (double)(offd * n.x));
+    py[m] = (float)((double)(wt * g.w) + (1.0 - (double)wt) * (double)g.y + (double)(offd * n.y));
   }
 }
 
@@ -137,6 +162,10 @@ __global__ void augment_kernel(const double* __restrict__ An, int n, int nunk, c
 
 }  // namespace
 
+// state layout of panels_affect_panels: px, py (T floats each) | geo (T float4) | nrm (T float2)
+// | cnt, off (T long long each)
+size_t pap_scratch_bytes(int T) { return (size_t)T * (2 * 4 + 16 + 8 + 2 * 8) + 256; }
+
 // Surfaces::set_geom_center (src/Surfaces.h:623-678) on the host: signed triangle areas from the
 // origin accumulated in double; returns the enclosed area and its centroid
 void geom_center_host(int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, double* vol,
@@ -167,10 +196,12 @@ int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, i
   const int n = ps.npan * nunk;
   const size_t N = (size_t)ps.npan;
   const size_t nn = (size_t)n * n;
-  // state: An (n^2 doubles) | unit strengths vs, ss | induced pu, pv
-  int s = ctx->state.ensure(nn * 8 + 4 * N * 4 + 1024, ctx->stream);
+  // state: the collocation scratch of panels_affect_panels | An (n^2 doubles) | unit strengths
+  // vs, ss | induced pu, pv
+  const size_t base = (pap_scratch_bytes(ps.npan) + 255) & ~(size_t)255;
+  int s = ctx->state.ensure(base + nn * 8 + 4 * N * 4 + 1024, ctx->stream);
   if (s) return s;
-  double* An = ctx->state.as<double>();
+  double* An = reinterpret_cast<double*>(ctx->state.as<char>() + base);
   float* vs = reinterpret_cast<float*>(An + nn);
   float* ss = vs + N;
   float* pu = ss + N;
@@ -193,17 +224,23 @@ int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, i
 int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
                              int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv) {
   if (src.npan == 0 || targ.npan == 0) return OBS_OK;
-  const size_t T = (size_t)targ.npan;
-  int s = ctx->state.ensure(2 * T * sizeof(float) + 256, ctx->stream);
+  const int T = targ.npan;
+  int s = ctx->state.ensure(pap_scratch_bytes(T), ctx->stream);
   if (s) return s;
   float* px = ctx->state.as<float>();
   float* py = px + T;
-  collocation_kernel<<<1, 1024, 0, ctx->stream>>>(targ.nx, targ.ny, targ.nnodes, targ.idx, targ.npan, px, py,
-                                                  ctx->d_status);
-  ctx->launches++;
+  float4* geo = reinterpret_cast<float4*>(ctx->state.as<char>() + (((size_t)T * 8 + 15) & ~(size_t)15));
+  float2* nrm = reinterpret_cast<float2*>(geo + T);
+  long long* cnt = reinterpret_cast<long long*>(nrm + T);
+  long long* off = cnt + T;
+  const int nb = (T + 255) / 256;
+  shed_kernel<<<nb, 256, 0, ctx->stream>>>(targ.nx, targ.ny, targ.nnodes, targ.idx, T, geo, nrm, cnt, ctx->d_status);
+  shed_scan_kernel<<<1, 1024, 0, ctx->stream>>>(cnt, T, off);
+  emit_kernel<<<nb, 256, 0, ctx->stream>>>(geo, nrm, cnt, off, T, px, py);
+  ctx->launches += 3;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e);
-  return run_panels_affect_points(ctx, src, vs, ss, accum, flags, fsx, fsy, targ.npan, px, py, pu, pv);
+  return run_panels_affect_points(ctx, src, vs, ss, accum, flags, fsx, fsy, T, px, py, pu, pv);
 }
 
 }  // namespace obs
