@@ -144,7 +144,8 @@ def time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args):
     n = X.numel()
     U, V = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
     G = [torch.zeros(n, device=dev) for _ in range(4)]
-    out = {"kernel": "p2p_kernel<GAUSS, thick, VELANDGRAD> (generic)", "flops_per_interaction": 41}
+    out = {"kernel": "p2p_packed_res_kernel<thick, compensated, GRAD> (Morton-ordered; far blocks d^2/s^2 > 25 "
+                     "without the exponential)", "flops_per_interaction": 41}
     for name, accum in (("compensated", og.COMPENSATED), ("plain", og.PLAIN_F32)):
         def call():
             for t in (U, V, *G):
@@ -424,7 +425,7 @@ def run_engine(args):
                 "ms_per_step": float(np.mean(e2e_ms))},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "kernel": "p2p_packed_kernel<GAUSS,thick,compensated,2> (Morton-ordered targets and sources)",
+                     "kernel": "p2p_packed_kernel<GAUSS,thick,compensated,4> (Morton-ordered targets and sources)",
                      "flops_per_interaction": FLOPS_PER_PAIR,
                      "flops_note": "the reference's count for the Gaussian thick-target velocity kernel; far "
                                    "(warp, block) pairs execute 7 FP32 lane-ops + 1 MUFU.RCP per interaction",

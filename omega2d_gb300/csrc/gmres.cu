@@ -120,6 +120,13 @@ __global__ void __launch_bounds__(1024) norm_kernel(const double* __restrict__ w
   if (threadIdx.x == 0) *out = sqrt(s);
 }
 
+// *flag = 1 when any x[i] != 0
+__global__ void nonzero_kernel(const double* __restrict__ x, int n, int* flag) {
+  int nz = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) nz |= (x[i] != 0.0);
+  if (__syncthreads_or(nz) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 // v = w / *nrm
 __global__ void scale_kernel(const double* __restrict__ w, int n, const double* nrm, double* __restrict__ v,
                              const GmState* st) {
@@ -586,7 +593,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   double* nrm = ctx->work.as<double>(o_n);
   double* gpart = ctx->work.as<double>(o_gp);
   float2* gvs = ctx->work.as<float2>(o_gv);
-  unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag
+  unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag, [2] x != 0
   float2* AP = fused ? ctx->work.as<float2>(o_ap) : nullptr;
   cudaStream_t strm = ctx->stream;
   const int gb = (n + GM_THREADS - 1) / GM_THREADS;
@@ -596,15 +603,18 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   diag_inv_kernel<<<gb, GM_THREADS, 0, strm>>>(A, n, dinv);
   norm_kernel<<<1, 1024, 0, strm>>>(b, n, nrm, nullptr);
   launched(2);
-  if ((e = cudaMemsetAsync(gbar, 0, 2 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
+  if ((e = cudaMemsetAsync(gbar, 0, 3 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
+  nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
+  launched(1);
   if (fused) {
     split_planes_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, N * N, AP, reinterpret_cast<int*>(gbar + 1));
     launched(1);
   }
   double bnorm = 0.0;
-  int range_bad = 0;
+  int range_bad = 0, x_nonzero = 0;
   e = cudaMemcpyAsync(&bnorm, nrm, 8, cudaMemcpyDeviceToHost, strm);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&range_bad, gbar + 1, 4, cudaMemcpyDeviceToHost, strm);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&x_nonzero, gbar + 2, 4, cudaMemcpyDeviceToHost, strm);
   if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
   if (e != cudaSuccess) return cuda_status(e);
   if (range_bad) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
@@ -619,7 +629,11 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     norm_kernel<<<1, 1024, 0, strm>>>(w, n, nrm, nullptr);
     launched(3);
   };
-  residual();
+  if (x_nonzero) {
+    residual();
+  } else {   // zero initial guess: r = b, and nrm already holds ||b||
+    if ((e = cudaMemcpyAsync(w, b, N * 8, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess) return cuda_status(e);
+  }
   int total_it = 0;
   double rel = 0.0;
   for (;;) {
