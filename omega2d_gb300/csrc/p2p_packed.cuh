@@ -32,20 +32,6 @@ constexpr int PK_ELEM = 3;   // float4 per staged source: (x,x,y,y) (G,G,-G,-G) 
 constexpr int PK_BLK = 32;   // sources per near-mask bit word / compensated block
 constexpr int PK_NB = SRC_TILE / PK_BLK;
 
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-
-// packed two-sum: hi + lo accumulates b
-__device__ __forceinline__ void two_sum2(float2& hi, float2& lo, float2 b) {
-  const float2 m1 = f2(-1.0f, -1.0f);
-  const float2 s = __fadd2_rn(hi, b);
-  const float2 bp = __ffma2_rn(hi, m1, s);        // s - hi
-  const float2 ap = __ffma2_rn(bp, m1, s);        // s - bp
-  const float2 da = __ffma2_rn(ap, m1, hi);       // hi - ap
-  const float2 db = __ffma2_rn(bp, m1, b);        // b - bp
-  lo = __fadd2_rn(lo, __fadd2_rn(da, db));
-  hi = s;
-}
-
 struct PackedUni {
   float us2, ucf, cfl, thr_small, thr_far;
   float2 cfl2, s22;

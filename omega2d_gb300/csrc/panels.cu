@@ -25,6 +25,7 @@ namespace {
 constexpr int PAN_THREADS = 128;
 constexpr int PAN_TILE = 128;           // panels (or particles) per shared-memory tile
 constexpr int PAN_COMP_BLOCK = 32;
+constexpr int PAN_TPB = 2 * PAN_THREADS;   // targets per block: two per thread
 
 // Per panel: P = (x0, y0, x1, y1), Q = (ux, uy, vortex strength, source strength), where
 // (ux, uy) is the unit tangent node0 -> node1 formed as the reference does (px * rsqrt(panl),
@@ -88,51 +89,58 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
-// atan(r), r in [0, 1], as r * P(r^2): P of degree 8 fitted to atan(r)/r for minimum maximum
-// relative error (omega2d_gb300/poly_fit.py); 1.5e-7 relative error in FP32
-__device__ __forceinline__ float atan_unit(float r) {
-  const float t = r * r;
-  float p = 2.849889686e-03f;
-  p = fmaf(p, t, -1.606862992e-02f);
-  p = fmaf(p, t, 4.269152135e-02f);
-  p = fmaf(p, t, -7.504294813e-02f);
-  p = fmaf(p, t, 1.064093411e-01f);
-  p = fmaf(p, t, -1.420364380e-01f);
-  p = fmaf(p, t, 1.999261975e-01f);
-  p = fmaf(p, t, -3.333307207e-01f);
-  p = fmaf(p, t, 1.0f);
-  return r * p;
-}
+// u* and v* of a panel seen from a target, for two (panel, target) pairs at once in f32x2
+// register pairs (FADD2 / FMUL2 / FFMA2 for the arithmetic; per-lane reciprocals, selects and
+// the rare near-panel fix-up).  atan on [0, 1] is r * P(r^2) with P of degree 8 fitted to
+// atan(r)/r for minimum maximum relative error (omega2d_gb300/poly_fit.py; 1.5e-7 relative in
+// FP32), reflected into the octant of (cross, dot).
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f, -1.0f), a); }
 
-// atan2(y, x) over the whole circle: atan_unit of min/max, reflected into the octant
-__device__ __forceinline__ float atan2_poly(float y, float x) {
-  const float ax = fabsf(x), ay = fabsf(y);
-  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-  const float r = (mx > 0.0f) ? mn * rcp_approx(mx) : 0.0f;
-  float p = atan_unit(r);
+__device__ __forceinline__ float atan2_fix(float p, float y, float x, float ay, float ax) {
   p = (ay > ax) ? 1.57079632679f - p : p;
   p = (x < 0.0f) ? 3.14159265359f - p : p;
   return copysignf(p, y);
 }
 
-// u* and v* of the panel (x0, y0)-(x1, y1), px = x1 - x0, py = y1 - y0, seen from (tx, ty)
-__device__ __forceinline__ void panel_uv_star_fast(float x0, float y0, float x1, float y1, float px, float py,
-                                                   float tx, float ty, float& us, float& vs) {
-  const float dx0 = tx - x0, dy0 = ty - y0;
-  const float dx1 = tx - x1, dy1 = ty - y1;
-  us = atan2_poly(dx0 * py - dy0 * px, dx0 * dx1 + dy0 * dy1);   // cross product as in panel_uv_star
-  const float r1 = dx1 * dx1 + dy1 * dy1;
-  const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
-  const float sv = diff * rcp_approx(fmaf(2.0f, r1, diff));  // (rho - 1) / (rho + 1)
-  const float t = sv * sv;
-  float p = fmaf(t, 1.0f / 9.0f, 1.0f / 7.0f);
-  p = fmaf(p, t, 1.0f / 5.0f);
-  p = fmaf(p, t, 1.0f / 3.0f);
-  vs = fmaf(sv * t, p, sv);                                  // atanh(s), truncation < 1e-9
-  if (!(fabsf(sv) <= 0.2f)) {
-    const float q = diff / r1;
-    vs = (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
-  }
+__device__ __forceinline__ float half_log_near(float dx0, float dy0, float r1, float diff) {
+  const float q = diff / r1;
+  return (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
+}
+
+__device__ __forceinline__ void panel_uv_star_fast2(float2 x0, float2 y0, float2 x1, float2 y1, float2 px, float2 py,
+                                                    float2 tx, float2 ty, float2& us, float2& vs) {
+  const float2 dx0 = sub2(tx, x0), dy0 = sub2(ty, y0);
+  const float2 dx1 = sub2(tx, x1), dy1 = sub2(ty, y1);
+  const float2 cr = sub2(__fmul2_rn(dx0, py), __fmul2_rn(dy0, px));     // (t - p0) x (p1 - p0)
+  const float2 dt = __ffma2_rn(dx0, dx1, __fmul2_rn(dy0, dy1));
+  // arctangent: |min|/|max| per lane, the polynomial packed
+  const float ax0 = fabsf(dt.x), ay0 = fabsf(cr.x), ax1 = fabsf(dt.y), ay1 = fabsf(cr.y);
+  const float mx0 = fmaxf(ax0, ay0), mx1 = fmaxf(ax1, ay1);
+  const float2 r = f2((mx0 > 0.0f) ? fminf(ax0, ay0) * rcp_approx(mx0) : 0.0f,
+                      (mx1 > 0.0f) ? fminf(ax1, ay1) * rcp_approx(mx1) : 0.0f);
+  const float2 t = __fmul2_rn(r, r);
+  float2 p = __ffma2_rn(f2(2.849889686e-03f, 2.849889686e-03f), t, f2(-1.606862992e-02f, -1.606862992e-02f));
+  p = __ffma2_rn(p, t, f2(4.269152135e-02f, 4.269152135e-02f));
+  p = __ffma2_rn(p, t, f2(-7.504294813e-02f, -7.504294813e-02f));
+  p = __ffma2_rn(p, t, f2(1.064093411e-01f, 1.064093411e-01f));
+  p = __ffma2_rn(p, t, f2(-1.420364380e-01f, -1.420364380e-01f));
+  p = __ffma2_rn(p, t, f2(1.999261975e-01f, 1.999261975e-01f));
+  p = __ffma2_rn(p, t, f2(-3.333307207e-01f, -3.333307207e-01f));
+  p = __ffma2_rn(p, t, f2(1.0f, 1.0f));
+  p = __fmul2_rn(r, p);
+  us = f2(atan2_fix(p.x, cr.x, dt.x, ay0, ax0), atan2_fix(p.y, cr.y, dt.y, ay1, ax1));
+  // half-log: atanh series of (rho - 1)/(rho + 1)
+  const float2 r1 = __ffma2_rn(dx1, dx1, __fmul2_rn(dy1, dy1));
+  const float2 diff = __ffma2_rn(px, __fadd2_rn(dx0, dx1), __fmul2_rn(py, __fadd2_rn(dy0, dy1)));
+  const float2 den = __ffma2_rn(f2(2.0f, 2.0f), r1, diff);
+  const float2 sv = __fmul2_rn(diff, f2(rcp_approx(den.x), rcp_approx(den.y)));
+  const float2 ts = __fmul2_rn(sv, sv);
+  float2 q = __ffma2_rn(ts, f2(1.0f / 9.0f, 1.0f / 9.0f), f2(1.0f / 7.0f, 1.0f / 7.0f));
+  q = __ffma2_rn(q, ts, f2(1.0f / 5.0f, 1.0f / 5.0f));
+  q = __ffma2_rn(q, ts, f2(1.0f / 3.0f, 1.0f / 3.0f));
+  vs = __ffma2_rn(__fmul2_rn(sv, ts), q, sv);
+  if (!(fabsf(sv.x) <= 0.2f)) vs.x = half_log_near(dx0.x, dy0.x, r1.x, diff.x);
+  if (!(fabsf(sv.y) <= 0.2f)) vs.y = half_log_near(dx0.y, dy0.y, r1.y, diff.y);
 }
 
 struct PanArgs {
@@ -162,9 +170,10 @@ __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, do
   a.out_v[i] = (float)(((double)a.out_v[i] + sv) * f + fy);
 }
 
-// One thread per target, sources (panels or particles) staged through shared memory in tiles;
-// grid = (target blocks, source splits).  Compensated: FP32 partials over 32 sources folded
-// into two-sum pairs, FP64 out; plain: FP32 throughout.
+// Two targets per thread (h = 0, 1: targets blockIdx.x PAN_TPB + h PAN_THREADS + tid) in
+// f32x2 register pairs; sources (panels or particles) staged through shared memory; grid =
+// (target blocks, source splits).  Compensated: FP32 partials over 32 sources folded into
+// two-sum pairs, FP64 out; plain: FP32 throughout.
 //   panels -> points: with the panel's unit tangent (tx, ty) and strengths (g, s), the sheet
 //     velocity (kernelu_1vs_0p) is u = u* A + v* B, v = v* A - u* B with A = g tx + s ty,
 //     B = s tx - g ty, formed once per panel when the tile is staged;
@@ -172,26 +181,33 @@ __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, do
 //     are of w u* and w v* and the tangent is applied once at the end.
 template <bool COMP>
 __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
-  __shared__ float4 sP[PAN_TILE];
-  __shared__ float4 sQ[PAN_TILE];
-  const int i = blockIdx.x * PAN_THREADS + threadIdx.x;
+  // sources pre-duplicated for the packed operands: panels (x0,x0,y0,y0) (x1,x1,y1,y1)
+  // (px,px,py,py) (A,A,B,B); particles (x,x,y,y) (w,w,0,0)
+  __shared__ float4 sE[PAN_TILE][4];
   const int sp = blockIdx.y;
-  const int ic = i < a.nt ? i : a.nt - 1;
-  // this thread's target: a point, or a panel (its geometry and inverse length)
-  float tx = 0.0f, ty = 0.0f;
-  float4 TP = make_float4(0, 0, 0, 0), TQ = make_float4(0, 0, 0, 0);
-  float tinv = 0.0f, tpx = 0.0f, tpy = 0.0f;
-  if (a.mode == 0) {
-    tx = a.tx[ic];
-    ty = a.ty[ic];
-  } else {
-    TP = a.P[ic];
-    TQ = a.Q[ic];
-    tinv = 1.0f / a.plen[ic];
-    tpx = TP.z - TP.x;
-    tpy = TP.w - TP.y;
+  int ti[2];
+  float tx[2] = {0.0f, 0.0f}, ty[2] = {0.0f, 0.0f}, tinv[2] = {0.0f, 0.0f};
+  float4 TP[2], TQ[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    ti[h] = blockIdx.x * PAN_TPB + h * PAN_THREADS + threadIdx.x;
+    const int ic = ti[h] < a.nt ? ti[h] : a.nt - 1;
+    TP[h] = TQ[h] = make_float4(0, 0, 0, 0);
+    if (a.mode == 0) {
+      tx[h] = a.tx[ic];
+      ty[h] = a.ty[ic];
+    } else {
+      TP[h] = a.P[ic];
+      TQ[h] = a.Q[ic];
+      tinv[h] = 1.0f / a.plen[ic];
+    }
   }
-  float au = 0.0f, av = 0.0f, hu = 0.0f, lu = 0.0f, hv = 0.0f, lv = 0.0f;
+  const float2 T2x = f2(tx[0], tx[1]), T2y = f2(ty[0], ty[1]);
+  const float2 X0 = f2(TP[0].x, TP[1].x), Y0 = f2(TP[0].y, TP[1].y);
+  const float2 X1 = f2(TP[0].z, TP[1].z), Y1 = f2(TP[0].w, TP[1].w);
+  const float2 PX = sub2(X1, X0), PY = sub2(Y1, Y0);
+  const float2 z2 = f2(0.0f, 0.0f);
+  float2 au = z2, av = z2, hu = z2, lu = z2, hv = z2, lv = z2;
   // this split's 32-source blocks [b0, b1), staged PAN_TILE sources at a time
   const int b0 = sp * a.blks_per_split;
   const int b1 = min(b0 + a.blks_per_split, a.nblk);
@@ -202,63 +218,76 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
       const int j = base * PAN_COMP_BLOCK + k;
       if (a.mode == 0) {
         const float4 P = a.P[j], Q = a.Q[j];
-        sP[k] = P;
-        sQ[k] = make_float4(P.z - P.x, P.w - P.y, Q.z * Q.x + Q.w * Q.y, Q.w * Q.x - Q.z * Q.y);
+        const float px = P.z - P.x, py = P.w - P.y;
+        const float A = Q.z * Q.x + Q.w * Q.y, B = Q.w * Q.x - Q.z * Q.y;
+        sE[k][0] = make_float4(P.x, P.x, P.y, P.y);
+        sE[k][1] = make_float4(P.z, P.z, P.w, P.w);
+        sE[k][2] = make_float4(px, px, py, py);
+        sE[k][3] = make_float4(A, A, B, B);
       } else {
-        sP[k] = a.pts[j];
+        const float4 q = a.pts[j];
+        sE[k][0] = make_float4(q.x, q.x, q.y, q.y);
+        sE[k][1] = make_float4(q.w, q.w, 0.0f, 0.0f);
       }
     }
     __syncthreads();
     for (int b = 0; b < ns; b += PAN_COMP_BLOCK) {
       if (a.mode == 0) {
-#pragma unroll 4
+#pragma unroll 2
         for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
-          const float4 P = sP[b + k], Q = sQ[b + k];
-          float us, vs;
-          panel_uv_star_fast(P.x, P.y, P.z, P.w, Q.x, Q.y, tx, ty, us, vs);
-          au = fmaf(us, Q.z, fmaf(vs, Q.w, au));
-          av = fmaf(vs, Q.z, fmaf(-us, Q.w, av));
+          const float4 E0 = sE[b + k][0], E1 = sE[b + k][1], E2 = sE[b + k][2], E3 = sE[b + k][3];
+          float2 us, vs;
+          panel_uv_star_fast2(f2(E0.x, E0.y), f2(E0.z, E0.w), f2(E1.x, E1.y), f2(E1.z, E1.w), f2(E2.x, E2.y),
+                              f2(E2.z, E2.w), T2x, T2y, us, vs);
+          const float2 A = f2(E3.x, E3.y), B = f2(E3.z, E3.w);
+          au = __ffma2_rn(us, A, __ffma2_rn(vs, B, au));
+          av = __ffma2_rn(vs, A, sub2(av, __fmul2_rn(us, B)));
         }
       } else {
         // the panel is the "source" of kernelu_1v_0p with the particle strength, the particle
         // the "target"; the sum is used with a minus sign (src/Influence.h:737-759)
-#pragma unroll 4
+#pragma unroll 2
         for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
-          const float4 q = sP[b + k];
-          float us, vs;
-          panel_uv_star_fast(TP.x, TP.y, TP.z, TP.w, tpx, tpy, q.x, q.y, us, vs);
-          au = fmaf(q.w, us, au);
-          av = fmaf(q.w, vs, av);
+          const float4 E0 = sE[b + k][0], E1 = sE[b + k][1];
+          float2 us, vs;
+          panel_uv_star_fast2(X0, Y0, X1, Y1, PX, PY, f2(E0.x, E0.y), f2(E0.z, E0.w), us, vs);
+          const float2 w = f2(E1.x, E1.y);
+          au = __ffma2_rn(w, us, au);
+          av = __ffma2_rn(w, vs, av);
         }
       }
       if (COMP) {
-        two_sum_acc(hu, lu, au);
-        two_sum_acc(hv, lv, av);
-        au = 0.0f;
-        av = 0.0f;
+        two_sum2(hu, lu, au);
+        two_sum2(hv, lv, av);
+        au = z2;
+        av = z2;
       }
     }
   }
-  if (i >= a.nt) return;
-  double su = COMP ? (double)hu + (double)lu : (double)au;
-  double sv = COMP ? (double)hv + (double)lv : (double)av;
-  if (a.mode == 1) {
-    // (sum w u*, sum w v*) -> velocity along the fixed tangent, times -1/len
-    const double ux = TQ.x, uy = TQ.y;
-    const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
-    su = -vu * (double)tinv;
-    sv = -vv * (double)tinv;
-  }
-  if (a.nsplit == 1) {
-    pan_store(a, i, su, sv);
-  } else if (COMP) {
-    double* p = static_cast<double*>(a.part);
-    p[(size_t)sp * a.nt + i] = su;
-    p[((size_t)a.nsplit + sp) * a.nt + i] = sv;
-  } else {
-    float* p = static_cast<float*>(a.part);
-    p[(size_t)sp * a.nt + i] = (float)su;
-    p[((size_t)a.nsplit + sp) * a.nt + i] = (float)sv;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int i = ti[h];
+    if (i >= a.nt) continue;
+    double su = COMP ? (double)(h ? hu.y : hu.x) + (double)(h ? lu.y : lu.x) : (double)(h ? au.y : au.x);
+    double sv = COMP ? (double)(h ? hv.y : hv.x) + (double)(h ? lv.y : lv.x) : (double)(h ? av.y : av.x);
+    if (a.mode == 1) {
+      // (sum w u*, sum w v*) -> velocity along the fixed tangent, times -1/len
+      const double ux = TQ[h].x, uy = TQ[h].y;
+      const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
+      su = -vu * (double)tinv[h];
+      sv = -vv * (double)tinv[h];
+    }
+    if (a.nsplit == 1) {
+      pan_store(a, i, su, sv);
+    } else if (COMP) {
+      double* p = static_cast<double*>(a.part);
+      p[(size_t)sp * a.nt + i] = su;
+      p[((size_t)a.nsplit + sp) * a.nt + i] = sv;
+    } else {
+      float* p = static_cast<float*>(a.part);
+      p[(size_t)sp * a.nt + i] = (float)su;
+      p[((size_t)a.nsplit + sp) * a.nt + i] = (float)sv;
+    }
   }
 }
 
@@ -428,7 +457,7 @@ int plan_splits(obs_context* ctx, int nblk, int tblocks) {
 }
 
 int run_pan(obs_context* ctx, PanArgs& a, bool comp, size_t scratch_off) {
-  const int tblocks = (a.nt + PAN_THREADS - 1) / PAN_THREADS;
+  const int tblocks = (a.nt + PAN_TPB - 1) / PAN_TPB;
   int nsplit = plan_splits(ctx, a.nblk, tblocks);
   const int bps = (a.nblk + nsplit - 1) / nsplit;
   nsplit = (a.nblk + bps - 1) / bps;
@@ -447,7 +476,7 @@ int run_pan(obs_context* ctx, PanArgs& a, bool comp, size_t scratch_off) {
 }  // namespace
 
 int launch_pan(obs_context* ctx, PanArgs& a, bool comp) {
-  const int tblocks = (a.nt + PAN_THREADS - 1) / PAN_THREADS;
+  const int tblocks = (a.nt + PAN_TPB - 1) / PAN_TPB;
   dim3 grid(tblocks, a.nsplit);
   timing_main_begin(ctx);
   if (comp) pan_kernel<true><<<grid, PAN_THREADS, 0, ctx->stream>>>(a);
