@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
       float S0 = 0.f, s0 = 0.f, S1 = 0.f, s1 = 0.f;
       const float2* col = a.AP + (size_t)c0 * a.n + ic;
       int c = c0;
-#pragma unroll 4
+#pragma unroll 8
       for (; c + 1 < c1; c += 2, col += 2 * (size_t)a.n) {
         df_fma(__ldg(col), a.vs[c], S0, s0);
         df_fma(__ldg(col + a.n), a.vs[c + 1], S1, s1);
