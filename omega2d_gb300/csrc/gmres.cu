@@ -205,19 +205,31 @@ constexpr int GC_THREADS = 1024;
 constexpr int GC_WARPS = GC_THREADS / 32;
 constexpr int GC_MAXM = 64;                     // restart length supported by the fused kernel
 
-// hi/lo planes of A; flags entries outside 2^+-99 (other than 0), where the planes would lose
-// precision or overflow
+// hi/lo planes of A, split from the bits of each double without FP64 arithmetic (double <->
+// float conversions run on the slow FP64 path of this GPU): hi keeps the sign, the exponent and
+// the top 23 stored significand bits (truncated), lo is the remaining 29 bits as an integer
+// converted to FP32 (rounded to 24 bits) and scaled by 2^(e-1075) in two normal steps; hi + lo
+// carries 48 significand bits.  Flags entries outside 2^+-99 (other than 0), where the planes
+// would lose precision or overflow.
+__device__ __forceinline__ float2 split_bits(double a, int& bad) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(a);
+  const int e = (int)((u >> 52) & 0x7ff);
+  const unsigned long long mant = u & ((1ull << 52) - 1);
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  bad |= (e != 0 && (e < 1023 - 99 || e > 1023 + 99)) || (e == 0 && mant != 0);
+  if (e == 0) return make_float2(__uint_as_float(sign), 0.0f);
+  const unsigned hib = sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29);
+  const int sh = e - 1075, s1 = sh / 2, s2 = sh - s1;            // each in [-76, 24] when not flagged
+  const float p1 = __uint_as_float((unsigned)(s1 + 127) << 23), p2 = __uint_as_float((unsigned)(s2 + 127) << 23);
+  const float lo = __int2float_rn((int)(mant & ((1ull << 29) - 1))) * p1 * p2;
+  return make_float2(__uint_as_float(hib), __uint_as_float(__float_as_uint(lo) | sign));
+}
+
 __global__ void split_planes_kernel(const double* __restrict__ A, size_t nn, float2* __restrict__ AP,
                                     int* __restrict__ range_flag) {
   int bad = 0;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x) {
-    const double a = A[k];
-    const float hi = __double2float_rn(a);
-    const float lo = __double2float_rn(a - (double)hi);
-    const int ex = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
-    bad |= (ex != 0 && (ex < 1023 - 99 || ex > 1023 + 99)) || (ex == 0 && (__double_as_longlong(a) << 1) != 0);
-    AP[k] = make_float2(hi, lo);
-  }
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x)
+    AP[k] = split_bits(A[k], bad);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(range_flag, 1);
 }
 
