@@ -60,28 +60,13 @@ __global__ void pack_panels_kernel(const float* __restrict__ nx, const float* __
   if (len) len[i] = sqrtf(panl);
 }
 
-// Subtended angle u* and log ratio v* of one panel seen from (tx, ty)
-// (get_ustar and my_halflog(rij2/rij12) of src/Kernels.h:256-268, 330-338).
-__device__ __forceinline__ void panel_uv_star(float4 P, float tx, float ty, float& us, float& vs) {
-  const float dx0 = tx - P.x, dy0 = ty - P.y;
-  const float dx1 = tx - P.z, dy1 = ty - P.w;
-  const float px = P.z - P.x, py = P.w - P.y;
-  // (t - p0) x (t - p1) = (t - p0) x (p1 - p0): the second form has no cancellation at distant
-  // targets, where the first differences two products of size d^2 to get one of size d L
-  us = atan2f(dx0 * py - dy0 * px, dx0 * dx1 + dy0 * dy1);
-  const float r1 = dx1 * dx1 + dy1 * dy1;
-  const float diff = px * (dx0 + dx1) + py * (dy0 + dy1);   // r0^2 - r1^2
-  // log(r0^2 / r1^2) in whichever form is well conditioned: log1p of the difference quotient
-  // when the ratio is near 1 (far from the panel), the ratio itself when the target is much
-  // closer to node 0 than to node 1 (there 1 + diff/r1 would cancel)
-  const float q = diff / r1;
-  vs = (q > -0.5f) ? 0.5f * log1pf(q) : 0.5f * logf((dx0 * dx0 + dy0 * dy0) / r1);
-}
-
-// ---- the same two quantities with fewer instructions, for the panel <-> particle sums, which
-// are issue-bound: a polynomial arctangent, and the half-log as atanh of s = (rho-1)/(rho+1),
-// rho = r0^2/r1^2, from its odd series where |s| <= 0.2 (every target more than a few panel
-// lengths from the panel).  Both keep full relative accuracy at small angles and logs.
+// ---- the subtended angle u* and log ratio v* of a panel seen from a target (get_ustar and
+// my_halflog(rij2/rij12) of src/Kernels.h:256-268, 330-338), in forms that need few
+// instructions: a polynomial arctangent of (cross, dot) with the cross product taken against
+// the panel vector, and the half-log as atanh of s = (rho-1)/(rho+1), rho = r0^2/r1^2, from its
+// odd series where |s| <= 0.2 (every target more than a few panel lengths from the panel),
+// else log1p of the exactly formed (r0^2 - r1^2)/r1^2 or the ratio itself near node 0.  Both
+// keep full relative accuracy at small angles and logs.
 
 __device__ __forceinline__ float rcp_approx(float x) {
   float y;
@@ -354,6 +339,20 @@ __global__ void pack_points_kernel(const float* __restrict__ x, const float* __r
   out[i] = i < n ? make_float4(x[i], y[i], 0.0f, s[i]) : make_float4(1.0e6f, 1.0e6f, 0.0f, 0.0f);
 }
 
+// float -> double from the bits (exact): float->double conversions run on the slow FP64 path of
+// this GPU; zero and normal values are rebiased with integer operations, anything else (a
+// subnormal, infinity or NaN) takes the hardware conversion
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xff;
+  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  if ((b & 0x7fffffffu) == 0) return __longlong_as_double((long long)sign);
+  if (e == 0 || e == 0xff) return (double)f;
+  const unsigned long long d = sign | ((unsigned long long)(e - 127 + 1023) << 52) |
+                               ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
 // panels_on_panels_coeff: one thread per (target panel i, source panel j); column-major output
 // with targets as rows (src/Coefficients.h:155-427).  Unit-strength influence of source j at
 // the midpoint of target i, dotted with target i's tangent and normal, averaged with the
@@ -372,8 +371,12 @@ __global__ void coeff_kernel(const float4* __restrict__ SP, const float4* __rest
   const float tnx = -tq.y, tny = tq.x;       // target normal (left of node0 -> node1)
   const float xi = 0.5f * (tp.z + tp.x), yi = 0.5f * (tp.w + tp.y);
   const float xj = 0.5f * (sp.x + sp.z), yj = 0.5f * (sp.y + sp.w);
-  float us, vs;
-  panel_uv_star(sp, xi, yi, us, vs);
+  // both evaluations in one packed call: lane x = source panel j at the midpoint of i, lane y =
+  // target panel i at the midpoint of j (the reversed roles below)
+  float2 us2, vs2;
+  panel_uv_star_fast2(f2(sp.x, tp.x), f2(sp.y, tp.y), f2(sp.z, tp.z), f2(sp.w, tp.w), f2(sp.z - sp.x, tp.z - tp.x),
+                      f2(sp.w - sp.y, tp.w - tp.y), f2(xi, xj), f2(yi, yj), us2, vs2);
+  float us = us2.x, vs = vs2.x;
   float vu = us * sq.x - vs * sq.y, vv = us * sq.y + vs * sq.x;
   float c11 = vu * ttx + vv * tty, c12 = vu * tnx + vv * tny;
   float c21 = 0.0f, c22 = 0.0f;
@@ -383,7 +386,8 @@ __global__ void coeff_kernel(const float4* __restrict__ SP, const float4* __rest
     c22 = su * tnx + sv * tny;
   }
   // reversed roles: target panel as source, evaluated at the source midpoint
-  panel_uv_star(tp, xj, yj, us, vs);
+  us = us2.y;
+  vs = vs2.y;
   const float fact = SL[j] / TL[i];
   vu = us * tq.x - vs * tq.y;
   vv = us * tq.y + vs * tq.x;
@@ -406,11 +410,16 @@ __global__ void coeff_kernel(const float4* __restrict__ SP, const float4* __rest
   if (nunk == 2) {
     const size_t c0 = (size_t)(2 * j) * nrows + 2 * i, c1 = (size_t)(2 * j + 1) * nrows + 2 * i;
     if (A32) { A32[c0] = c11; A32[c0 + 1] = c12; A32[c1] = c21; A32[c1 + 1] = c22; }
-    if (A64) { A64[c0] = c11; A64[c0 + 1] = c12; A64[c1] = c21; A64[c1 + 1] = c22; }
+    if (A64) {
+      A64[c0] = f2d_bits(c11);
+      A64[c0 + 1] = f2d_bits(c12);
+      A64[c1] = f2d_bits(c21);
+      A64[c1 + 1] = f2d_bits(c22);
+    }
   } else {
     const size_t c0 = (size_t)j * nrows + i;
     if (A32) A32[c0] = c11;
-    if (A64) A64[c0] = c11;
+    if (A64) A64[c0] = f2d_bits(c11);
   }
 }
 
