@@ -254,6 +254,20 @@ def test_gmres_fused_cycle_matches_per_step_kernels(n):
     assert np.max(np.abs(xf - xg)) < 1e-9 * np.max(np.abs(xt))
 
 
+@pytest.mark.parametrize("scale", [1e-35, 1e-20, 1.0, 1e20, 1e35])
+def test_gmres_matrix_scales(scale):
+    """Entries beyond 2^+-99 cannot be carried by the FP32 planes of the fused cycle: such a
+    matrix takes the FP64 per-step kernels; every scale converges to the same solution."""
+    rng = np.random.default_rng(7)
+    n = 300
+    A = (np.eye(n) * 3.0 + rng.normal(0, 1.0 / np.sqrt(n), (n, n))) * scale
+    xt = rng.normal(size=n)
+    b = A @ xt
+    x, it, rel = og.solve_gmres_f64(A, b, tol=1e-12, restart=40, maxiter=400, context=og.Context())
+    assert rel < 1e-12
+    assert np.max(np.abs(x - xt)) < 1e-9 * np.max(np.abs(xt))
+
+
 @pytest.mark.parametrize("shape", ["circle", "poly"])
 def test_augmented_block_matches_reference(ctx, golden, shape):
     g = golden("augment")
