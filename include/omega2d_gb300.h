@@ -76,7 +76,8 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
 /* Kernel variant for particle-on-particle sums.  AUTO uses the packed-FP32 kernels (two
  * targets per f32x2 register pair) where they exist -- velocity for every core, with 4 target
- * pairs per thread (2 for Vatistas n=3 and the singular core); velocity gradient, vorticity
+ * pairs per thread (2 for Vatistas n=3, the singular core and sums with fewer than 49,152
+ * targets, 98,304 for the compact exponential); velocity gradient, vorticity
  * and shear for the Gaussian core -- and the generic kernels elsewhere.  GENERIC forces the
  * generic kernels (and the one-kernel-per-step GMRES); PACKED2 / PACKED3 / PACKED4 pick 2, 3
  * (Gaussian only; 2 for the other cores) or 4 target pairs per thread for the packed velocity
@@ -97,7 +98,7 @@ int obs_set_kernel_variant(obs_context* ctx, int variant);
  *   BINNED_TARGETS : binned targets; results are bit-identical to INPUT;
  *   BINNED         : binned targets and sources; sources are summed in the binned order, so
  *                    results differ from INPUT by rounding only (and are reproducible);
- *   AUTO           : BINNED when the sum has at least 2e9 pairs and 4096 targets and sources,
+ *   AUTO           : BINNED when the sum has at least 3e8 pairs and 4096 targets and sources,
  *                    else INPUT. */
 #define OBS_ORDER_AUTO 0
 #define OBS_ORDER_INPUT 1

@@ -107,8 +107,8 @@ int p2p_ncomp(int res);
 
 // packed-FP32 velocity kernels (p2p_packed.cu)
 bool packed_supported(int core, int res);
-// target pairs per thread of the packed velocity kernel for a core and OBS_VARIANT_*
-int packed_np(int core, int variant);
+// target pairs per thread of the packed velocity kernel for a core, OBS_VARIANT_* and target count
+int packed_np(int core, int variant, int nt);
 cudaError_t packed_dispatch(int core, int np, bool thick, bool comp, const P2PArgs* a, int grid, cudaStream_t st,
                             int* occ);
 // packed Gaussian kernels for the gradient, vorticity and shear results (p2p_packed_res.cu):

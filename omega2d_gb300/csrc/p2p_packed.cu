@@ -60,14 +60,19 @@ bool packed_supported(int core, int res) {
   return core == CORE_GAUSS && (res == RES_GRAD || res == RES_VORT || res == RES_SHEAR);
 }
 
-int packed_np(int core, int variant) {
+int packed_np(int core, int variant, int nt) {
   if (variant == OBS_VARIANT_PACKED2) return 2;
   if (variant == OBS_VARIANT_PACKED3) return core == CORE_GAUSS ? 3 : 2;
   if (variant == OBS_VARIANT_PACKED4) return 4;
   // AUTO, from the 1M Gaussian patch (compensated, Ginter/s with 4 vs 2 target pairs):
   // Gaussian 4111 vs 3785 (Morton order), RM 4116 vs 4017, Vatistas-2 3810 vs 3776,
-  // Winckelmans-Leonard 2996 vs 2762; the singular core 3694 vs 3732 and Vatistas-3 keep 2
-  return (core == CORE_V3 || core == CORE_SING) ? 2 : 4;
+  // Winckelmans-Leonard 2996 vs 2762; the singular core 3694 vs 3732 and Vatistas-3 keep 2.
+  // Fewer targets need the smaller target blocks to fill the GPU (uniform [-1,1]^2 clouds:
+  // 20k RM 2391 vs 2136; 65k compact exponential, Morton order, 3383 vs 3190, Gaussian 3305
+  // vs 3439)
+  if (core == CORE_V3 || core == CORE_SING) return 2;
+  if (nt < (core == CORE_CEXP ? 98304 : 49152)) return 2;
+  return 4;
 }
 
 // np must come from packed_np: the host sizes the target blocks with it
