@@ -74,6 +74,13 @@ int obs_last_timing(obs_context* ctx, float* main_kernel_ms, float* call_ms);
 /* Device-side failure record seen by the last synchronizing call that reported one: DEV_ERR
  * bits (1 = bounded wait timed out, 4 = bounds check), the check code, and two values. */
 int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2);
+/* Failure-path self-test: runs, on the context's stream, a bounded wait that nothing
+ * completes -- which 0: an mbarrier phase with no arrival (the wait of the tile pipelines),
+ * which 1: a grid barrier expecting one block more than the grid (the fused GMRES cycle) --
+ * which gives up after max_polls polls, records its location (codes 901 / 700) and returns.
+ * Returns the status the next synchronizing call reads: OBS_ERR_TIMEOUT when the wait gave up
+ * as designed; the context stays usable. */
+int obs_selftest_bounded_wait(obs_context* ctx, int which, int max_polls);
 /* Kernel variant for particle-on-particle sums.  AUTO uses the packed-FP32 kernels (two
  * targets per f32x2 register pair) where they exist -- velocity for every core, with 4 target
  * pairs per thread (2 for Vatistas n=3, the singular core and sums with fewer than 49,152

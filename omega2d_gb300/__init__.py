@@ -146,6 +146,17 @@ class Context:
     def launches(self) -> int:
         return int(lib().obs_launch_count(self._h))
 
+    def last_failure(self):
+        """(bits, code, v1, v2) of the last device-side failure record a synchronizing call read."""
+        w = [ctypes.c_int() for _ in range(4)]
+        _check(lib().obs_last_failure(self._h, *[ctypes.byref(v) for v in w]), "obs_last_failure")
+        return tuple(v.value for v in w)
+
+    def selftest_bounded_wait(self, which: int, max_polls: int = 64) -> int:
+        """Run a bounded wait that nothing completes (0: mbarrier, 1: grid barrier) and return the
+        status the host reads afterwards (OBS_ERR_TIMEOUT when it gave up as designed)."""
+        return int(lib().obs_selftest_bounded_wait(self._h, ctypes.c_int(which), ctypes.c_int(max_polls)))
+
 
 _default_ctx: Context | None = None
 

@@ -230,6 +230,13 @@ int obs_last_failure(obs_context* ctx, int* bits, int* code, int* v1, int* v2) {
   return OBS_OK;
 }
 
+int obs_selftest_bounded_wait(obs_context* ctx, int which, int max_polls) {
+  if (!ctx) return OBS_ERR_ARG;
+  int s = obs::bind(ctx);
+  if (s) return s;
+  return obs::selftest_bounded_wait(ctx, which, max_polls);
+}
+
 int obs_set_kernel_variant(obs_context* ctx, int variant) {
   if (!ctx) return OBS_ERR_ARG;
   if (variant != OBS_VARIANT_AUTO && variant != OBS_VARIANT_GENERIC && variant != OBS_VARIANT_PACKED2 &&

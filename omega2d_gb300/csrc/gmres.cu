@@ -257,17 +257,19 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 }
 
 // grid barrier number `nb` (0, 1, 2, ...) over co-resident blocks: a monotone arrival counter
-// with release adds and acquire polls; the poll is bounded (about a second), after which the
-// block records where it gave up and every block returns false
-__device__ bool gc_barrier(unsigned* bar, int* status, unsigned nb) {
+// with release adds and acquire polls; the poll is bounded (about a second by default), after
+// which the block records where it gave up and every block returns false.  `arrivals` is the
+// count one barrier waits for (the grid size; the bounded-wait self-test asks for one more).
+__device__ bool gc_barrier(unsigned* bar, int* status, unsigned nb, unsigned arrivals = 0,
+                           unsigned max_polls = 1u << 21) {
   __syncthreads();
   int ok = 1;
   if (threadIdx.x == 0) {
-    const unsigned target = (nb + 1) * gridDim.x;
+    const unsigned target = (nb + 1) * (arrivals ? arrivals : gridDim.x);
     red_release_gpu(bar, 1u);
     unsigned it = 0;
     while (ld_acquire_gpu(bar) < target) {
-      if (++it > (1u << 21)) {
+      if (++it > max_polls) {
         record_failure(status, DEV_ERR_TIMEOUT, 700, (int)blockIdx.x, (int)nb);
         ok = 0;
         break;
@@ -534,7 +536,48 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     }
 }
 
+// Bounded-wait self-tests: waits that nothing completes, so each gives up after max_polls,
+// records DEV_ERR_TIMEOUT in the status block and returns (no fault, no hang).
+//   which 0: an mbarrier phase with no arrival (the wait of the TMA tile pipelines)
+//   which 1: a grid barrier that waits for one block more than the grid (the fused GMRES cycle)
+__global__ void selftest_mbar_kernel(int* status, unsigned max_polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0u, max_polls);
+  if (!ok && threadIdx.x == 0) record_failure(status, DEV_ERR_TIMEOUT, 901, (int)blockIdx.x, 0);
+}
+
+__global__ void selftest_grid_barrier_kernel(unsigned* bar, int* status, unsigned max_polls) {
+  (void)gc_barrier(bar, status, 0, gridDim.x + 1, max_polls);
+}
+
 }  // namespace
+
+int selftest_bounded_wait(obs_context* ctx, int which, int max_polls) {
+  if (max_polls <= 0 || (which != 0 && which != 1)) return OBS_ERR_ARG;
+  cudaStream_t st = ctx->stream;
+  cudaError_t e;
+  if (which == 0) {
+    selftest_mbar_kernel<<<1, 32, 0, st>>>(ctx->d_status, (unsigned)max_polls);
+    e = cudaGetLastError();
+  } else {
+    int s = ctx->work.ensure(256, st);
+    if (s) return s;
+    unsigned* bar = ctx->work.as<unsigned>();
+    if ((e = cudaMemsetAsync(bar, 0, sizeof(unsigned), st)) != cudaSuccess) return cuda_status(e);
+    const int grid = std::max(1, std::min(ctx->num_sms, 64));
+    unsigned polls = (unsigned)max_polls;
+    void* args[] = {&bar, &ctx->d_status, &polls};
+    e = cudaLaunchCooperativeKernel((const void*)selftest_grid_barrier_kernel, dim3(grid), dim3(32), args, 0, st);
+  }
+  ctx->launches++;
+  if (e != cudaSuccess) return cuda_status(e);
+  return take_device_status(ctx);
+}
 
 int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double* x, double tol, int restart,
               int maxiter, int* iters_out, double* rel_residual) {

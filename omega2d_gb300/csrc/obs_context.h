@@ -76,6 +76,9 @@ int cuda_status(cudaError_t e);
 int bind(obs_context* ctx);
 // Read and clear the device error bits (synchronizes the stream).
 int take_device_status(obs_context* ctx);
+// runs a wait that nothing completes (which 0: mbarrier, 1: grid barrier) and returns the
+// status the host reads afterwards (OBS_ERR_TIMEOUT when the bounded wait gave up as designed)
+int selftest_bounded_wait(obs_context* ctx, int which, int max_polls);
 // Event helpers around the main kernel of a call.
 void timing_begin(obs_context* ctx);
 void timing_main_begin(obs_context* ctx);

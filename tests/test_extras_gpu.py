@@ -183,3 +183,24 @@ def test_tape_required(ctx):
     with pytest.raises(og.EngineError):
         og.advect_vjp_tape_dev(other, z, z, z, z, z)
     other.close()
+
+
+@pytest.mark.parametrize("which,code", [(0, 901), (1, 700)])
+def test_bounded_wait_gives_up_and_context_stays_usable(restatement, which, code):
+    """Failure path of the device waits, made without a fault: an mbarrier phase with no
+    arrival (0) and a grid barrier waiting for one block more than the grid (1) give up after
+    their poll limit, record where, and the host reads OBS_ERR_TIMEOUT; the same context then
+    computes a correct sum."""
+    ctx = og.Context()
+    assert ctx.selftest_bounded_wait(which, 64 if which == 0 else 2000) == -4   # OBS_ERR_TIMEOUT
+    bits, got_code, _, _ = ctx.last_failure()
+    assert bits & 1 and got_code == code
+    rng = np.random.default_rng(3)
+    sx, sy = rng.uniform(-1, 1, (2, 2000)).astype(np.float32)
+    sr = np.full(2000, 0.02, np.float32)
+    ss = rng.normal(0, 1e-3, 2000).astype(np.float32)
+    t = og.Points(sx, sy, sr, None)
+    og.points_affect_points(og.Points(sx, sy, sr, ss), t, og.VELONLY, og.ExecEnv(og.CORE_GAUSSIAN, og.COMPENSATED, ctx))
+    u64, v64, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, sx, sy, sr, fp64=True)
+    assert rel_err(u64, t.u) < 2e-6 and rel_err(v64, t.v) < 2e-6
+    assert ctx.selftest_bounded_wait(which, 0) == -1                            # OBS_ERR_ARG
