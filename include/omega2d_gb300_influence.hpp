@@ -63,4 +63,41 @@ float points_affect_points(const SrcPoints& src, TargPoints& targ, int result,
   return (float)flops;
 }
 
+// Mirror of panels_affect_points<float,A>(src, targ, restype, env) (src/Influence.h:422-614):
+// accumulates the unscaled velocity of the panels' vortex sheets (and source sheets, when the
+// surface has source strengths) at the points.  Surfaces accessors: get_pos() (nodes),
+// get_idx() (two 32-bit node indices per panel), get_npanels(), get_str(), have_src_str(),
+// get_src_str() (src/Surfaces.h:231-252).
+template <class SrcSurfaces, class TargPoints>
+void panels_affect_points(const SrcSurfaces& src, TargPoints& targ, int accum = OBS_COMPENSATED) {
+  const auto& nx = src.get_pos();
+  const auto& idx = src.get_idx();
+  static_assert(sizeof(idx[0]) == sizeof(unsigned), "panel node indices must be 32-bit");
+  const float* ss = src.have_src_str() ? src.get_src_str().data() : nullptr;
+  const auto& tx = targ.get_pos();
+  auto& tu = targ.get_vel();
+  const int s = obs_panels_affect_points(context(), accum, 0, 0.0, 0.0, (int)nx[0].size(), nx[0].data(), nx[1].data(),
+                                         (int)src.get_npanels(), reinterpret_cast<const unsigned*>(idx.data()),
+                                         src.get_str().data(), ss, (int)targ.get_n(), tx[0].data(), tx[1].data(),
+                                         tu[0].data(), tu[1].data());
+  if (s != OBS_OK) throw std::runtime_error(std::string("obs_panels_affect_points: ") + obs_status_string(s));
+}
+
+// Mirror of points_affect_panels<float,A>(src, targ, restype, env) (src/Influence.h:633-771):
+// accumulates into each panel's velocity the mean velocity of the point vortices over the
+// panel (the BEM right-hand-side input; the points' core radii are ignored, as there).
+template <class SrcPoints, class TargSurfaces>
+void points_affect_panels(const SrcPoints& src, TargSurfaces& targ, int accum = OBS_COMPENSATED) {
+  const auto& sx = src.get_pos();
+  const auto& nx = targ.get_pos();
+  const auto& idx = targ.get_idx();
+  static_assert(sizeof(idx[0]) == sizeof(unsigned), "panel node indices must be 32-bit");
+  auto& pu = targ.get_vel();
+  const int s = obs_points_affect_panels(context(), accum, 0, 0.0, 0.0, (int)src.get_n(), sx[0].data(), sx[1].data(),
+                                         src.get_str().data(), (int)nx[0].size(), nx[0].data(), nx[1].data(),
+                                         (int)targ.get_npanels(), reinterpret_cast<const unsigned*>(idx.data()),
+                                         pu[0].data(), pu[1].data());
+  if (s != OBS_OK) throw std::runtime_error(std::string("obs_points_affect_panels: ") + obs_status_string(s));
+}
+
 }  // namespace omega2d_gb300
