@@ -98,22 +98,34 @@ __device__ __forceinline__ void panel_uv_star_fast2(float2 x0, float2 y0, float2
   const float2 dx1 = sub2(tx, x1), dy1 = sub2(ty, y1);
   const float2 cr = sub2(__fmul2_rn(dx0, py), __fmul2_rn(dy0, px));     // (t - p0) x (p1 - p0)
   const float2 dt = __ffma2_rn(dx0, dx1, __fmul2_rn(dy0, dy1));
-  // arctangent: |min|/|max| per lane, the polynomial packed
-  const float ax0 = fabsf(dt.x), ay0 = fabsf(cr.x), ax1 = fabsf(dt.y), ay1 = fabsf(cr.y);
-  const float mx0 = fmaxf(ax0, ay0), mx1 = fmaxf(ax1, ay1);
-  const float2 r = f2((mx0 > 0.0f) ? fminf(ax0, ay0) * rcp_approx(mx0) : 0.0f,
-                      (mx1 > 0.0f) ? fminf(ax1, ay1) * rcp_approx(mx1) : 0.0f);
-  const float2 t = __fmul2_rn(r, r);
-  float2 p = __ffma2_rn(f2(2.849889686e-03f, 2.849889686e-03f), t, f2(-1.606862992e-02f, -1.606862992e-02f));
-  p = __ffma2_rn(p, t, f2(4.269152135e-02f, 4.269152135e-02f));
-  p = __ffma2_rn(p, t, f2(-7.504294813e-02f, -7.504294813e-02f));
-  p = __ffma2_rn(p, t, f2(1.064093411e-01f, 1.064093411e-01f));
-  p = __ffma2_rn(p, t, f2(-1.420364380e-01f, -1.420364380e-01f));
-  p = __ffma2_rn(p, t, f2(1.999261975e-01f, 1.999261975e-01f));
-  p = __ffma2_rn(p, t, f2(-3.333307207e-01f, -3.333307207e-01f));
-  p = __ffma2_rn(p, t, f2(1.0f, 1.0f));
-  p = __fmul2_rn(r, p);
-  us = f2(atan2_fix(p.x, cr.x, dt.x, ay0, ax0), atan2_fix(p.y, cr.y, dt.y, ay1, ax1));
+  if (fabsf(cr.x) < 0.2f * dt.x && fabsf(cr.y) < 0.2f * dt.y) {
+    // both targets see the panel under less than atan(0.2) from in front (every target more
+    // than a few panel lengths away): atan of the signed ratio by its odd Taylor series to
+    // r^9 (truncation below 1e-8 relative), no octant reflection
+    const float2 r = __fmul2_rn(cr, f2(rcp_approx(dt.x), rcp_approx(dt.y)));
+    const float2 t = __fmul2_rn(r, r);
+    float2 p = __ffma2_rn(t, f2(1.0f / 9.0f, 1.0f / 9.0f), f2(-1.0f / 7.0f, -1.0f / 7.0f));
+    p = __ffma2_rn(p, t, f2(1.0f / 5.0f, 1.0f / 5.0f));
+    p = __ffma2_rn(p, t, f2(-1.0f / 3.0f, -1.0f / 3.0f));
+    us = __ffma2_rn(__fmul2_rn(r, t), p, r);
+  } else {
+    // arctangent: |min|/|max| per lane, the polynomial packed
+    const float ax0 = fabsf(dt.x), ay0 = fabsf(cr.x), ax1 = fabsf(dt.y), ay1 = fabsf(cr.y);
+    const float mx0 = fmaxf(ax0, ay0), mx1 = fmaxf(ax1, ay1);
+    const float2 r = f2((mx0 > 0.0f) ? fminf(ax0, ay0) * rcp_approx(mx0) : 0.0f,
+                        (mx1 > 0.0f) ? fminf(ax1, ay1) * rcp_approx(mx1) : 0.0f);
+    const float2 t = __fmul2_rn(r, r);
+    float2 p = __ffma2_rn(f2(2.849889686e-03f, 2.849889686e-03f), t, f2(-1.606862992e-02f, -1.606862992e-02f));
+    p = __ffma2_rn(p, t, f2(4.269152135e-02f, 4.269152135e-02f));
+    p = __ffma2_rn(p, t, f2(-7.504294813e-02f, -7.504294813e-02f));
+    p = __ffma2_rn(p, t, f2(1.064093411e-01f, 1.064093411e-01f));
+    p = __ffma2_rn(p, t, f2(-1.420364380e-01f, -1.420364380e-01f));
+    p = __ffma2_rn(p, t, f2(1.999261975e-01f, 1.999261975e-01f));
+    p = __ffma2_rn(p, t, f2(-3.333307207e-01f, -3.333307207e-01f));
+    p = __ffma2_rn(p, t, f2(1.0f, 1.0f));
+    p = __fmul2_rn(r, p);
+    us = f2(atan2_fix(p.x, cr.x, dt.x, ay0, ax0), atan2_fix(p.y, cr.y, dt.y, ay1, ax1));
+  }
   // half-log: atanh series of (rho - 1)/(rho + 1)
   const float2 r1 = __ffma2_rn(dx1, dx1, __fmul2_rn(dy1, dy1));
   const float2 diff = __ffma2_rn(px, __fadd2_rn(dx0, dx1), __fmul2_rn(py, __fadd2_rn(dy0, dy1)));
