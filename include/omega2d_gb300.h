@@ -197,6 +197,17 @@ int obs_panels_affect_panels_dev(obs_context* ctx, int accum, int flags, double 
 /* points_affect_panels -- replaces src/Influence.h:633-771: mean velocity over each panel due
  * to point vortices of strength ss (the particle core is not used, as in the reference),
  * accumulated into the panel-centre velocities pu, pv. */
+/* Reverse mode of obs_panels_affect_points with respect to the panel strengths (no counterpart
+ * in the reference): for cotangents (lu, lv) of the finalized velocities at the nt points
+ * (tx, ty) -- L depends on u = fs + (panel sum)/(2 pi) -- accumulates gvs[p] += dL/d(vortex
+ * strength p) and, when gss is not null, gss[p] += dL/d(source strength p).  Both panel
+ * strength sets enter the forward sum linearly, so these are exact gradients. */
+int obs_panels_affect_points_vjp(obs_context* ctx, int accum, int nnodes, const float* nx, const float* ny,
+                                 int npan, const unsigned* idx, int nt, const float* tx, const float* ty,
+                                 const float* lu, const float* lv, float* gvs, float* gss);
+int obs_panels_affect_points_vjp_dev(obs_context* ctx, int accum, int nnodes, const float* nx, const float* ny,
+                                     int npan, const unsigned* idx, int nt, const float* tx, const float* ty,
+                                     const float* lu, const float* lv, float* gvs, float* gss);
 int obs_points_affect_panels(obs_context* ctx, int accum, int flags, double fsx, double fsy,
                              int ns, const float* sx, const float* sy, const float* ss,
                              int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,

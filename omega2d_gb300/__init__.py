@@ -426,6 +426,29 @@ def panels_affect_points(src: Surfaces, targ: Points, env: ExecEnv | None = None
     _check(st, "obs_panels_affect_points")
 
 
+def panels_affect_points_vjp(src: Surfaces, targ: Points, lu, lv, env: ExecEnv | None = None):
+    """Reverse mode of panels_affect_points with respect to the panel strengths: for cotangents
+    (lu, lv) of the finalized point velocities returns (dL/d vortex strengths, dL/d source
+    strengths), one value per panel (no counterpart in the reference)."""
+    env = env or ExecEnv()
+    gv = np.zeros(src.npan, np.float32)
+    gs = np.zeros(src.npan, np.float32)
+    lu, lv = _own32(lu), _own32(lv)
+    st = lib().obs_panels_affect_points_vjp(env.ctx().handle, ctypes.c_int(env.accum), *src._geo(),
+                                            ctypes.c_int(targ.n), _ptr(targ.x), _ptr(targ.y), _ptr(lu), _ptr(lv),
+                                            _ptr(gv), _ptr(gs))
+    _check(st, "obs_panels_affect_points_vjp")
+    return gv, gs
+
+
+def panels_affect_points_vjp_dev(ctx: Context, accum: int, nx, ny, idx, tx, ty, lu, lv, gvs, gss=None):
+    """Device-resident panel-strength VJP (CUDA tensors), asynchronous; gvs, gss accumulate."""
+    _check(lib().obs_panels_affect_points_vjp_dev(ctx.handle, ctypes.c_int(accum), ctypes.c_int(nx.numel()), _ptr(nx),
+                                                  _ptr(ny), ctypes.c_int(idx.numel() // 2), _ptr(idx),
+                                                  ctypes.c_int(tx.numel()), _ptr(tx), _ptr(ty), _ptr(lu), _ptr(lv),
+                                                  _ptr(gvs), _ptr(gss)), "obs_panels_affect_points_vjp_dev")
+
+
 def points_affect_panels(src: Points, targ: Surfaces, env: ExecEnv | None = None,
                          finalize: bool = False, fs=(0.0, 0.0)):
     """points_affect_panels (src/Influence.h:633-771): mean velocity over each panel due to the

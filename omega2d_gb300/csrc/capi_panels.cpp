@@ -233,6 +233,55 @@ int obs_points_affect_panels(obs_context* ctx, int accum, int flags, double fsx,
   return copy_back(ctx, {{pu, {dpu, (size_t)npan * 4}}, {pv, {dpv, (size_t)npan * 4}}});
 }
 
+// ---- reverse mode of panels_affect_points w.r.t. the panel strengths
+int obs_panels_affect_points_vjp_dev(obs_context* ctx, int accum, int nnodes, const float* nx, const float* ny,
+                                     int npan, const unsigned* idx, int nt, const float* tx, const float* ty,
+                                     const float* lu, const float* lv, float* gvs, float* gss) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (nt < 0 || (nt > 0 && (!tx || !ty || !lu || !lv)) || (npan > 0 && !gvs)) return OBS_ERR_ARG;
+  if ((s = obs::bind(ctx))) return s;
+  PanelSet ps{nnodes, nx, ny, npan, idx};
+  return obs::run_panels_affect_points_vjp(ctx, ps, nt, tx, ty, lu, lv, accum, gvs, gss);
+}
+
+int obs_panels_affect_points_vjp(obs_context* ctx, int accum, int nnodes, const float* nx, const float* ny,
+                                 int npan, const unsigned* idx, int nt, const float* tx, const float* ty,
+                                 const float* lu, const float* lv, float* gvs, float* gss) {
+  if (!ctx) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if (nt < 0 || (nt > 0 && (!tx || !ty || !lu || !lv)) || (npan > 0 && !gvs)) return OBS_ERR_ARG;
+  if (npan == 0) return OBS_OK;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  Stage g(ctx);
+  for (int k = 0; k < 4; ++k) g.reserve((size_t)nt * 4);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)npan * 4);
+  if ((s = g.commit())) return s;
+  const float* dtx = g.take(tx, nt);
+  const float* dty = g.take(ty, nt);
+  const float* dlu = g.take(lu, nt);
+  const float* dlv = g.take(lv, nt);
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  float* dgv = g.take(gvs, npan);
+  float* dgs = gss ? g.take(gss, npan) : g.take<float>(nullptr, npan);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  s = obs::run_panels_affect_points_vjp(ctx, ps, nt, dtx, dty, dlu, dlv, accum, dgv, gss ? dgs : nullptr);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  if (gss) return copy_back(ctx, {{gvs, {dgv, (size_t)npan * 4}}, {gss, {dgs, (size_t)npan * 4}}});
+  return copy_back(ctx, {{gvs, {dgv, (size_t)npan * 4}}});
+}
+
 // ---- panels_on_panels_coeff (src/Coefficients.h:155-427)
 int obs_panels_on_panels_coeff_dev(obs_context* ctx, int nunk, int self_block,
                                    int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,

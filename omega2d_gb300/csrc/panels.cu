@@ -157,7 +157,8 @@ struct PanArgs {
   void* part;
   int finalize;
   double fsx, fsy;
-  int mode;             // 0: panels -> points, 1: points -> panels
+  int mode;             // 0: panels -> points, 1: points -> panels, 2: VJP of mode 0 w.r.t. the
+                        //    panel strengths (sources = points with their cotangents)
 };
 
 __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, double sv) {
@@ -222,9 +223,9 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
         sE[k][2] = make_float4(px, px, py, py);
         sE[k][3] = make_float4(A, A, B, B);
       } else {
-        const float4 q = a.pts[j];
+        const float4 q = a.pts[j];   // (x, y, 0, strength) or, mode 2, (x, y, lu, lv)
         sE[k][0] = make_float4(q.x, q.x, q.y, q.y);
-        sE[k][1] = make_float4(q.w, q.w, 0.0f, 0.0f);
+        sE[k][1] = (a.mode == 1) ? make_float4(q.w, q.w, 0.0f, 0.0f) : make_float4(q.z, q.z, q.w, q.w);
       }
     }
     __syncthreads();
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
           au = __ffma2_rn(us, A, __ffma2_rn(vs, B, au));
           av = __ffma2_rn(vs, A, sub2(av, __fmul2_rn(us, B)));
         }
-      } else {
+      } else if (a.mode == 1) {
         // the panel is the "source" of kernelu_1v_0p with the particle strength, the particle
         // the "target"; the sum is used with a minus sign (src/Influence.h:737-759)
 #pragma unroll 2
@@ -251,6 +252,18 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
           const float2 w = f2(E1.x, E1.y);
           au = __ffma2_rn(w, us, au);
           av = __ffma2_rn(w, vs, av);
+        }
+      } else {
+        // VJP of the sheet velocity u = u* A + v* B, v = v* A - u* B at a point with cotangent
+        // (lu, lv): P = sum lu u* + lv v*, Q = sum lv u* - lu v*; dL/dA = P, dL/dB = -Q
+#pragma unroll 2
+        for (int k = 0; k < PAN_COMP_BLOCK; ++k) {
+          const float4 E0 = sE[b + k][0], E1 = sE[b + k][1];
+          float2 us, vs;
+          panel_uv_star_fast2(X0, Y0, X1, Y1, PX, PY, f2(E0.x, E0.y), f2(E0.z, E0.w), us, vs);
+          const float2 lu = f2(E1.x, E1.y), lv = f2(E1.z, E1.w);
+          au = __ffma2_rn(lu, us, __ffma2_rn(lv, vs, au));
+          av = __ffma2_rn(lv, us, sub2(av, __fmul2_rn(lu, vs)));
         }
       }
       if (COMP) {
@@ -273,6 +286,13 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
       const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
       su = -vu * (double)tinv[h];
       sv = -vv * (double)tinv[h];
+    } else if (a.mode == 2) {
+      // A = g tx + s ty, B = s tx - g ty: dL/dg = tx P + ty Q, dL/ds = ty P - tx Q, times the
+      // finalize factor 1/(2 pi) (the gradients are of the finalized velocities)
+      const double ux = TQ[h].x, uy = TQ[h].y;
+      const double gg = (ux * su + uy * sv) * 0.15915494309189535, gs = (uy * su - ux * sv) * 0.15915494309189535;
+      su = gg;
+      sv = gs;
     }
     if (a.nsplit == 1) {
       pan_store(a, i, su, sv);
@@ -341,6 +361,16 @@ __global__ void pan_reduce_warp_kernel(const PanArgs a) {
     sv += __shfl_xor_sync(0xffffffffu, sv, o);
   }
   if (lane == 0) pan_store(a, i, su, sv);
+}
+
+// Points with their velocity cotangents -> float4 (x, y, lu, lv), padded with zero cotangents
+// far away.
+__global__ void pack_cotangents_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                       const float* __restrict__ lu, const float* __restrict__ lv, int n, int n_pad,
+                                       float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pad) return;
+  out[i] = i < n ? make_float4(x[i], y[i], lu[i], lv[i]) : make_float4(1.0e6f, 1.0e6f, 0.0f, 0.0f);
 }
 
 // Particles -> float4 (x, y, 0, strength), padded with zero-strength particles far away.
@@ -587,6 +617,52 @@ int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const fl
   s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, L, np);
   if (!s) {
     pack_points_kernel<<<(ns_pad + 255) / 256, 256, 0, ctx->stream>>>(sx, sy, ss, ns, ns_pad, pts);
+    ctx->launches++;
+    s = cuda_status(cudaGetLastError());
+  }
+  if (!s) s = launch_pan(ctx, a, comp);
+  timing_end(ctx);
+  return s;
+}
+
+// Reverse mode of panels_affect_points with respect to the panel strengths: for cotangents
+// (lu, lv) of the finalized point velocities, gvs[p] += dL/dgamma_p and gss[p] += dL/dsigma_p
+// (gss may be null).  The panels are the targets of the sum, the points its sources.
+int run_panels_affect_points_vjp(obs_context* ctx, const PanelSet& ps, int nt, const float* tx, const float* ty,
+                                 const float* lu, const float* lv, int accum, float* gvs, float* gss) {
+  if (ps.npan == 0 || nt == 0) return OBS_OK;
+  const bool comp = accum == OBS_COMPENSATED;
+  const int ntiles = (nt + PAN_TILE - 1) / PAN_TILE;
+  const int nt_pad = ntiles * PAN_TILE;
+  const int np = ps.npan;
+  const size_t hdr = 256;
+  const size_t pbytes = ((size_t)np * sizeof(float4) + 255) & ~(size_t)255;
+  const size_t lbytes = ((size_t)np * sizeof(float) + 255) & ~(size_t)255;
+  const size_t off_pts = hdr + 2 * pbytes + 2 * lbytes;
+  const size_t off_part = off_pts + (size_t)nt_pad * sizeof(float4);
+  PanArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nsrc = nt_pad; a.nblk = nt_pad / PAN_COMP_BLOCK;
+  a.nt = np;
+  a.finalize = 0;
+  a.mode = 2;
+  int s = ctx->work.ensure(off_part, ctx->stream);
+  if (!s) s = run_pan(ctx, a, comp, off_part);
+  if (s) return s;
+  float4* P = ctx->work.as<float4>(hdr);
+  float4* Q = ctx->work.as<float4>(hdr + pbytes);
+  float* L = ctx->work.as<float>(hdr + 2 * pbytes);
+  float* sink = ctx->work.as<float>(hdr + 2 * pbytes + lbytes);   // dL/dsigma when not wanted
+  float4* pts = ctx->work.as<float4>(off_pts);
+  a.P = P; a.Q = Q; a.plen = L; a.pts = pts;
+  a.out_u = gvs;
+  a.out_v = gss ? gss : sink;
+  if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
+  timing_begin(ctx);
+  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, L, np);
+  if (!s && !gss) s = cuda_status(cudaMemsetAsync(sink, 0, (size_t)np * sizeof(float), ctx->stream));
+  if (!s) {
+    pack_cotangents_kernel<<<(nt_pad + 255) / 256, 256, 0, ctx->stream>>>(tx, ty, lu, lv, nt, nt_pad, pts);
     ctx->launches++;
     s = cuda_status(cudaGetLastError());
   }

@@ -21,6 +21,10 @@ int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* 
 int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const float* sy, const float* ss,
                              const PanelSet& ps, int accum, int flags, double fsx, double fsy,
                              float* pu, float* pv);
+// reverse mode of panels_affect_points w.r.t. the panel strengths (cotangents of the finalized
+// point velocities); gvs, gss (optional) accumulate
+int run_panels_affect_points_vjp(obs_context* ctx, const PanelSet& ps, int nt, const float* tx, const float* ty,
+                                 const float* lu, const float* lv, int accum, float* gvs, float* gss);
 // panels_affect_panels (src/Influence.h:774-795) through the reference's collocation points
 int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
                              int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv);

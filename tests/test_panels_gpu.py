@@ -299,3 +299,53 @@ def test_augmented_solve_circulation_and_rotation(ctx):
     assert rel < 1e-12
     # the bottom row of the system: sum(vs * len) + 2 area * omega = C
     assert abs(np.sum(surf.vs.astype(np.float64) * L) + 2 * vol * om - 0.7) < 1e-4
+
+
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+def test_panel_strength_vjp_vs_fp64(ctx, restatement, accum):
+    """Reverse mode of panels_affect_points w.r.t. the vortex and source strengths against the
+    FP64 restatement's unit-strength responses (the forward is linear in the strengths, so those
+    are the exact gradients), with points far from and close to the body."""
+    rng = np.random.default_rng(12)
+    npan = 64
+    c = og.circle_panels(npan)
+    n = 1500
+    rad = np.concatenate([np.sqrt(rng.uniform(0.55 ** 2, 9.0, n - 100)), 0.5 + rng.choice([-1, 1], 100) * 0.02])
+    th = rng.uniform(0, 2 * np.pi, n)
+    x, y = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    lu, lv = rng.normal(size=(2, n)).astype(np.float32)
+    gv, gs = og.panels_affect_points_vjp(og.Surfaces(c.nx, c.ny, c.idx), og.Points(x, y), lu, lv,
+                                         og.ExecEnv(accum=accum, context=ctx))
+    gv_ref, gs_ref = np.zeros(npan), np.zeros(npan)
+    zero = np.zeros(npan, np.float32)
+    for p in range(npan):
+        e = zero.copy()
+        e[p] = 1.0
+        u, v = restatement.panels_affect_points(c.nx, c.ny, c.idx, e, zero, x, y, fp64=True)
+        gv_ref[p] = (lu @ u + lv @ v) / (2 * np.pi)
+        u, v = restatement.panels_affect_points(c.nx, c.ny, c.idx, zero, e, x, y, fp64=True)
+        gs_ref[p] = (lu @ u + lv @ v) / (2 * np.pi)
+    tol = 5e-6 if accum == og.COMPENSATED else 5e-5
+    assert rel_err(gv_ref, gv) < tol and rel_err(gs_ref, gs) < tol
+
+
+def test_panel_strength_vjp_homogeneity(ctx):
+    """Large case, size-independent check: the forward is linear in the strengths, so
+    sum_p (dL/dg_p g_p + dL/ds_p s_p) equals L = sum_t lambda_t . u_t / (2 pi)."""
+    rng = np.random.default_rng(13)
+    npan, n = 2048, 200_000
+    c = og.circle_panels(npan)
+    surf = og.Surfaces(c.nx, c.ny, c.idx, vs=rng.normal(0, 1, npan).astype(np.float32),
+                       ss=rng.normal(0, 1, npan).astype(np.float32))
+    rad = np.sqrt(rng.uniform(0.55 ** 2, 9.0, n))
+    th = rng.uniform(0, 2 * np.pi, n)
+    x, y = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    lu, lv = rng.normal(size=(2, n)).astype(np.float32)
+    env = og.ExecEnv(accum=og.COMPENSATED, context=ctx)
+    targ = og.Points(x, y)
+    og.panels_affect_points(surf, targ, env, finalize=True)
+    L = float(lu.astype(np.float64) @ targ.u + lv.astype(np.float64) @ targ.v)
+    gv, gs = og.panels_affect_points_vjp(surf, og.Points(x, y), lu, lv, env)
+    lin = float(gv.astype(np.float64) @ surf.vs + gs.astype(np.float64) @ surf.ss)
+    scale = float(np.abs(lu).astype(np.float64) @ np.abs(targ.u) + np.abs(lv).astype(np.float64) @ np.abs(targ.v))
+    assert abs(lin - L) < 1e-5 * scale
