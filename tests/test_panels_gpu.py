@@ -349,3 +349,32 @@ def test_panel_strength_vjp_homogeneity(ctx):
     lin = float(gv.astype(np.float64) @ surf.vs + gs.astype(np.float64) @ surf.ss)
     scale = float(np.abs(lu).astype(np.float64) @ np.abs(targ.u) + np.abs(lv).astype(np.float64) @ np.abs(targ.v))
     assert abs(lin - L) < 1e-5 * scale
+
+
+def test_panel_autograd_wrapper_matches_c_abi(ctx):
+    """torch autograd through the panel forward/backward pair gives the C-ABI VJP for the
+    loss sum(u^2 + v^2)."""
+    torch = pytest.importorskip("torch")
+    from autograd_ops import PanelVelocity
+    rng = np.random.default_rng(14)
+    npan, n = 256, 20_000
+    c = og.circle_panels(npan)
+    vs = rng.normal(0, 1, npan).astype(np.float32)
+    ss = rng.normal(0, 1, npan).astype(np.float32)
+    rad = np.sqrt(rng.uniform(0.55 ** 2, 4.0, n))
+    th = rng.uniform(0, 2 * np.pi, n)
+    x, y = (rad * np.cos(th)).astype(np.float32), (rad * np.sin(th)).astype(np.float32)
+    dev = torch.device("cuda:0")
+    T = lambda a, g=False: torch.tensor(a, device=dev, requires_grad=g)
+    tvs, tss = T(vs, True), T(ss, True)
+    idx = torch.from_numpy(c.idx.astype(np.int32)).to(dev)
+    u, v = PanelVelocity.apply(tvs, tss, T(c.nx), T(c.ny), idx, T(x), T(y), ctx, og.COMPENSATED)
+    (u * u + v * v).sum().backward()
+    ctx.set_stream(None)
+    env = og.ExecEnv(accum=og.COMPENSATED, context=ctx)
+    surf = og.Surfaces(c.nx, c.ny, c.idx, vs=vs, ss=ss)
+    targ = og.Points(x, y)
+    og.panels_affect_points(surf, targ, env, finalize=True)
+    assert rel_err(targ.u, u.detach().cpu().numpy()) < 1e-6
+    gv, gs = og.panels_affect_points_vjp(surf, og.Points(x, y), 2 * targ.u, 2 * targ.v, env)
+    assert rel_err(gv, tvs.grad.cpu().numpy()) < 1e-6 and rel_err(gs, tss.grad.cpu().numpy()) < 1e-6
