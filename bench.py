@@ -680,9 +680,11 @@ def run_rk2adjoint2M(args):
     """Two co-rotating Gaussian patches of 1M particles each (sigma 0.1, centres (+-0.3, 0),
     total circulation 1 each), core 0.004, Gaussian; `--rk-steps` Ralston RK2 steps with
     dt = 0.005; loss L = |X_A - X_B|^2 with X_P = sum_P G^2 x / sum_P G^2; gradient of L with
-    respect to the initial strengths through the trajectory, checkpoints every 8 steps."""
+    respect to the initial strengths through the trajectory, checkpoints every 8 steps
+    (`--checkpoint-every -1`: every step's positions and stage positions kept in HBM, so the
+    backward recomputes nothing)."""
     torch, og, dev, ctx, stream, flush = _engine_setup()
-    n, K, dt, every = 2_000_000, args.rk_steps, 0.005, 8
+    n, K, dt, every = 2_000_000, args.rk_steps, 0.005, args.checkpoint_every
     rng = np.random.default_rng(5)
     lab = (np.arange(n) % 2).astype(np.int64)
     cx = np.where(lab == 0, -0.3, 0.3)
@@ -739,7 +741,8 @@ def run_rk2adjoint2M(args):
            "unit": UNIT, "data": "synthetic (seed 5)", "n": n, "rk2_steps": K, "dt": dt, "checkpoint_every": every,
            "forward_ms": f_ms, "forward_ginter_s": evals / (f_ms * 1e-3) / 1e9,
            "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
-           "adjoint_note": "from the recorded checkpoints: recomputes each segment (about 2K velocity sums) and "
+           "adjoint_note": ("from the full tape: no recomputed velocity sum, " if every == og.TAPE_ALL else
+                            "from the recorded checkpoints: recomputes each segment (about 2K velocity sums) and ") +
                            "runs 2K self-interaction VJP gathers",
            "value": evals / (f_ms * 1e-3) / 1e9, "loss": L, "grad_strength_norm": float(np.linalg.norm(gs)),
            "grad_strength_finite": bool(np.isfinite(gs).all()),
@@ -933,6 +936,8 @@ def main():
     ap.add_argument("--workload", default="patch1M", choices=["patch1M", "euler20k", "bem2048", "rk2adjoint2M", "rows"],
                     help="patch1M is the headline line; the others measure the remaining configurations")
     ap.add_argument("--rk-steps", type=int, default=64, help="RK2 steps of rk2adjoint2M")
+    ap.add_argument("--checkpoint-every", type=int, default=8,
+                    help="rk2adjoint2M checkpoint interval; -1 keeps the whole trajectory (no recompute)")
     args = ap.parse_args()
     globals()["N"] = args.n
     if args.impl == "reference":

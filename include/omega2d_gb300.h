@@ -340,7 +340,12 @@ int obs_advect_dev(obs_context* ctx, int core, int accum, int order, int n, floa
 /* Forward op that also records the checkpoints (every checkpoint_every steps; 0: ceil(sqrt
  * (nsteps))) and copies of r and s in the context, so that obs_advect_vjp_tape_dev can run the
  * backward without repeating the forward sweep.  One recording per context; the next
- * recording (or obs_advect_vjp) replaces it. */
+ * recording (or obs_advect_vjp) replaces it.
+ * checkpoint_every = OBS_TAPE_ALL keeps every step's positions and stage positions on the
+ * device (nsteps * stages * 2n floats; RK2: 2 GB for 2M particles over 64 steps): the backward
+ * then evaluates no velocity sum, only the VJP gathers.  Gradients are bit-identical to the
+ * checkpointed ones. */
+#define OBS_TAPE_ALL (-1)
 int obs_advect_record_dev(obs_context* ctx, int core, int accum, int order, int n, float* x, float* y,
                           const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
                           int checkpoint_every);

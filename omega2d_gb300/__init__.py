@@ -742,6 +742,8 @@ def advect_dev(ctx: Context, core: int, accum: int, order: int, x, y, r, s, fs, 
 
 
 ADVECT_EULER, ADVECT_RK2_RALSTON, ADVECT_RK3, ADVECT_RK2_HEUN = 1, 2, 3, 4
+# checkpoint_every value that keeps every step's positions and stage positions (no recompute)
+TAPE_ALL = -1
 
 
 def advect_record_dev(ctx: Context, core: int, accum: int, order: int, x, y, r, s, fs, dt, nsteps,

@@ -18,8 +18,9 @@
 //     wu = G_j lu_k - G_k lu_j, wv = G_j lv_k - G_k lv_j, q = dx wv - dy wu,
 //     AX = sum K wv + B q dx,  AY = sum -K wu + B q dy,  AE = sum K (dx lv_j - dy lu_j),
 //     dL/dG_k = -AE                                                          [20 f32x2 ops + rcp]
+//   the far form of ADJ_SELF is evaluated as moments (pa_block_self_far)      [17 f32x2 ops + rcp]
 // Element layout (4 float4): ADJ_SRC  (x,x,y,y) (lv,lv,-lu,-lu) (-2lv,-2lv,2lu,2lu) (z,z,0,0)
-//                            ADJ_SELF (-x,-x,-y,-y) (lv,lv,-lu,-lu) (G,G,-2G,-2G) (z,z,0,0)
+//                            ADJ_SELF (-x,-x,-y,-y) (lv,lv,-lu,-lu) (G,G,-2G,-2G) (z,z,lu,lu)
 #include <algorithm>
 #include <cstring>
 
@@ -100,7 +101,7 @@ __global__ void pa_pack_kernel(const float* __restrict__ x, const float* __restr
       o[1] = make_float4(V, V, -U, -U);
       o[2] = make_float4(G, G, -2.0f * G, -2.0f * G);
     }
-    o[3] = make_float4(z, z, 0.0f, 0.0f);
+    o[3] = make_float4(z, z, MODE == PA_SELF ? U : 0.0f, MODE == PA_SELF ? U : 0.0f);
   } else if (i < n_pad) {
     float4* o = out + (size_t)PA_ELEM * i;
     o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -126,10 +127,84 @@ struct PAAcc {
   float2 ax, ay, ah;
 };
 
-// one 32-element block; FAST: far form only; UNIF: uniform radii (us2, ucf)
-template <int MODE, bool THICK, bool FAST, bool UNIF, int NP>
+// ADJ_SELF far form as moments (one 32-element block).  With K = 1/d^2 and B = -2 K^2,
+//   K wv + B q dx = -wv P + wu Q,   -K wu + B q dy = -wu P - wv Q,
+// P = (dx^2 - dy^2) K^2 = a^2 - b^2 and Q = 2 dx dy K^2 = 2 a b (a = dx K, b = dy K), and
+// splitting wu, wv into their owner and element parts,
+//   AX = -lv_k SP + lu_k SQ + G_k T1,   AY = -lu_k SP - lv_k SQ + G_k T2,
+//   SP = sum G_j P, SQ = sum G_j Q, T1 = sum (lv_j P - lu_j Q), T2 = sum (lu_j P + lv_j Q).
+// The block sums carry n = -P/2 = b^2 - K/2 (a^2 + b^2 = K) and h = Q/2 = a b:
+//   sp = sum G_j n, sq = sum G_j h, t1 = sum (lv_j n + lu_j h) = -T1/2, t2 = sum (-lu_j n + lv_j h) = T2/2,
+// and AE = sum K (dx lv_j - dy lu_j) = sum (a lv_j - b lu_j).  The fold once per block:
+//   AX = 2 lv_k sp + 2 lu_k sq - 2 G_k t1,   AY = 2 lu_k sp - 2 lv_k sq + 2 G_k t2.
+// 17 f32x2 operations per pair of pairs (the direct form: 20), no K^2 formed on its own.
+// FRESH: acc[].ax, ay are zero on entry (compensated sums restart per block) and carry sp, sq.
+template <int NP, bool FRESH>
+__device__ __forceinline__ void pa_block_self_far(const float4* __restrict__ blk, const PAOwn (&w)[NP],
+                                                  PAAcc (&acc)[NP]) {
+  float2 t1[NP], t2[NP], bx[NP], by[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    if constexpr (!FRESH) {
+      bx[p] = acc[p].ax;
+      by[p] = acc[p].ay;
+      acc[p].ax = acc[p].ay = f2(0.0f, 0.0f);
+    }
+    t1[p] = t2[p] = f2(0.0f, 0.0f);
+  }
+  const float2 mhalf = f2(-0.5f, -0.5f);
+#pragma unroll 2
+  for (int jj = 0; jj < PA_BLK; ++jj) {
+    const float4 E0 = blk[PA_ELEM * jj];
+    const float4 E1 = blk[PA_ELEM * jj + 1];
+    const float4 E2 = blk[PA_ELEM * jj + 2];
+    const float2 lu = reinterpret_cast<const float2*>(blk + PA_ELEM * jj + 3)[1];   // (lu, lu) of E3
+    const float2 ex = f2(E0.x, E0.y), ey = f2(E0.z, E0.w);
+    const float2 lv = f2(E1.x, E1.y), nlu = f2(E1.z, E1.w);
+    const float2 G = f2(E2.x, E2.y);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const float2 dx = __fadd2_rn(ex, w[p].c0);
+      const float2 dy = __fadd2_rn(ey, w[p].c1);
+      const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+      const float2 K = f2(rcp_a(d2.x), rcp_a(d2.y));
+      const float2 a = __fmul2_rn(dx, K), b = __fmul2_rn(dy, K);
+      const float2 n = __ffma2_rn(b, b, __fmul2_rn(K, mhalf));
+      const float2 h = __fmul2_rn(a, b);
+      acc[p].ax = __ffma2_rn(G, n, acc[p].ax);    // sp
+      acc[p].ay = __ffma2_rn(G, h, acc[p].ay);    // sq
+      t1[p] = __ffma2_rn(lv, n, __ffma2_rn(lu, h, t1[p]));
+      t2[p] = __ffma2_rn(nlu, n, __ffma2_rn(lv, h, t2[p]));
+      acc[p].ah = __ffma2_rn(a, lv, __ffma2_rn(b, nlu, acc[p].ah));
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    // owner constants: lvk = lv_k, nluk = -lu_k, p2g = 2 G_k, ng = -G_k
+    const float2 sp = acc[p].ax, sq = acc[p].ay;
+    const float2 lv2 = __fmul2_rn(w[p].lvk, f2(2.0f, 2.0f)), lu2 = __fmul2_rn(w[p].nluk, f2(-2.0f, -2.0f));
+    const float2 ng2 = __fmul2_rn(w[p].ng, f2(2.0f, 2.0f)), mlv2 = __fmul2_rn(w[p].lvk, f2(-2.0f, -2.0f));
+    const float2 ax = __ffma2_rn(lv2, sp, __ffma2_rn(lu2, sq, __fmul2_rn(ng2, t1[p])));
+    const float2 ay = __ffma2_rn(lu2, sp, __ffma2_rn(mlv2, sq, __fmul2_rn(w[p].p2g, t2[p])));
+    if constexpr (FRESH) {
+      acc[p].ax = ax;
+      acc[p].ay = ay;
+    } else {
+      acc[p].ax = __fadd2_rn(bx[p], ax);
+      acc[p].ay = __fadd2_rn(by[p], ay);
+    }
+  }
+}
+
+// one 32-element block; FAST: far form only; UNIF: uniform radii (us2, ucf); COMP: acc is zero
+// on entry
+template <int MODE, bool THICK, bool FAST, bool UNIF, int NP, bool COMP>
 __device__ __forceinline__ void pa_block(const float4* __restrict__ blk, const PAOwn (&w)[NP], PAAcc (&acc)[NP],
                                          float us2, float ucf) {
+  if constexpr (MODE == PA_SELF && FAST) {
+    pa_block_self_far<NP, COMP>(blk, w, acc);
+    return;
+  }
 #pragma unroll 2
   for (int jj = 0; jj < PA_BLK; ++jj) {
     const float4 E0 = blk[PA_ELEM * jj];
@@ -216,8 +291,11 @@ __device__ __forceinline__ void pa_store(const PAArgs& a, int i, double ax, doub
   if (a.gg) a.gg[o] = (float)((double)a.gg[o] + sg);
 }
 
+// The compensated self gather keeps 7 CTAs per SM (72 registers): at 8 (64 registers) its far
+// form spills, and measured 3 % slower on the 1M Gaussian patch.
 template <int MODE, bool THICK, bool COMP, int NP>
-__global__ void __launch_bounds__(PA_THREADS, NP == 1 ? 8 : 4) pa_kernel(const PAArgs a) {
+__global__ void __launch_bounds__(PA_THREADS, NP == 1 ? (MODE == PA_SELF && COMP ? 7 : 8) : 4)
+    pa_kernel(const PAArgs a) {
   constexpr int TPT = 2 * NP;
   constexpr int TB = PA_THREADS * TPT;
   constexpr int WT = 32 * TPT;
@@ -327,10 +405,10 @@ __global__ void __launch_bounds__(PA_THREADS, NP == 1 ? 8 : 4) pa_kernel(const P
       for (int b = 0; b < PA_NB; ++b) {
         const float4* blk = tl + PA_ELEM * b * PA_BLK;
         if (unif) {
-          if (smask[warp][b] == 0u) pa_block<MODE, THICK, true, true, NP>(blk, w, acc, us2, ucf);
-          else pa_block<MODE, THICK, false, true, NP>(blk, w, acc, us2, ucf);
+          if (smask[warp][b] == 0u) pa_block<MODE, THICK, true, true, NP, COMP>(blk, w, acc, us2, ucf);
+          else pa_block<MODE, THICK, false, true, NP, COMP>(blk, w, acc, us2, ucf);
         } else {
-          pa_block<MODE, THICK, false, false, NP>(blk, w, acc, us2, ucf);
+          pa_block<MODE, THICK, false, false, NP, COMP>(blk, w, acc, us2, ucf);
         }
         if constexpr (COMP) {
 #pragma unroll

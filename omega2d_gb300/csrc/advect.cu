@@ -16,7 +16,9 @@
 // Positions are recomputed per segment from checkpoints taken every `every` steps (sqrt(K) by
 // default), so the tape holds K/every checkpoints plus one segment of stage positions.  The
 // checkpoints can come from a recorded forward (obs_advect_record_dev), which the backward then
-// reuses without running the forward sweep again.
+// reuses without running the forward sweep again.  every = OBS_TAPE_ALL keeps every step's
+// position and stage positions instead (K*S*2N floats: 2 GB for 2M particles, 64 RK2 steps),
+// and the backward then runs the VJP gathers alone, with no recomputed velocity sum.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -156,10 +158,12 @@ int record(obs_context* ctx, int core, int accum, int order, int n, const float*
   Scheme sc;
   if (!scheme_of(order, &sc)) return OBS_ERR_ARG;
   const size_t N = (size_t)n;
-  const int C = check_every(every, nsteps);
+  const bool full = every == OBS_TAPE_ALL;
+  const int C = full ? 1 : check_every(every, nsteps);
   const int nck = (nsteps + C - 1) / C;
+  const size_t slot = (full ? (size_t)sc.S : 1) * 2 * N;   // floats per checkpoint
   ctx->tape_info.valid = false;
-  int st = ctx->tape.ensure(((size_t)2 * N + (size_t)nck * 2 * N) * 4 + 1024, ctx->stream);
+  int st = ctx->tape.ensure(((size_t)2 * N + (size_t)nck * slot) * 4 + 1024, ctx->stream);
   if (st) return st;
   // state: vel 2SN | working positions 2N | stage positions (S-1)*2N (sized once, before any copy)
   if ((st = ctx->state.ensure(((size_t)2 * sc.S * N + 2 * N + (size_t)(sc.S - 1) * 2 * N) * 4 + 1024, ctx->stream)))
@@ -177,12 +181,14 @@ int record(obs_context* ctx, int core, int accum, int order, int n, const float*
   if ((st = copy(tr, r, N)) || (st = copy(ts, s, N)) || (st = copy(w, x0, N)) || (st = copy(w + N, y0, N))) return st;
   Step p{ctx, core, accum, n, sc, tr, ts, fsx, fsy, dt};
   for (int k = 0; k < nsteps; ++k) {
-    if (k % C == 0 && (st = copy(ck + (size_t)(k / C) * 2 * N, w, 2 * N))) return st;
-    if ((st = step(p, w, w, vel, stages, true))) return st;
+    float* sl = ck + (size_t)(k / C) * slot;
+    if (k % C == 0 && (st = copy(sl, w, 2 * N))) return st;
+    // full tape: the stage positions land in the step's slot, after x_k
+    if ((st = step(p, w, w, vel, full ? sl + 2 * N : stages, true))) return st;
   }
   if (xf && (st = copy(xf, w, N))) return st;
   if (yf && (st = copy(yf, w + N, N))) return st;
-  ctx->tape_info = AdvectTape{true, core, accum, order, n, nsteps, C, nck, fsx, fsy, dt};
+  ctx->tape_info = AdvectTape{true, core, accum, order, n, nsteps, C, nck, fsx, fsy, dt, full};
   return OBS_OK;
 }
 
@@ -195,13 +201,14 @@ int reverse(obs_context* ctx, const float* lx_in, const float* ly_in, float* gs,
   scheme_of(t.order, &sc);
   const int n = t.n, C = t.every, S = sc.S;
   const size_t N = (size_t)n;
-  // state (floats): segment C*S*2N (x_k, y_1..y_{S-1} per step) | vel 2SN | lam 2N | cot 2N |
-  //                 cur 2N | prev 2N | acc 2N
-  const size_t total = (size_t)C * S * 2 * N + (size_t)2 * S * N + 10 * N;
+  // state (floats): segment C*S*2N (x_k, y_1..y_{S-1} per step; none for a full tape, whose
+  //                 slots hold the same layout) | vel 2SN | lam 2N | cot 2N | cur 2N | prev 2N | acc 2N
+  const size_t segf = t.full ? 0 : (size_t)C * S * 2 * N;
+  const size_t total = segf + (size_t)2 * S * N + 10 * N;
   int st = ctx->state.ensure(total * 4 + 1024, ctx->stream);
   if (st) return st;
   float* seg = ctx->state.as<float>();
-  float* vel = seg + (size_t)C * S * 2 * N;
+  float* vel = seg + segf;
   float* lam = vel + (size_t)2 * S * N;
   float* cot = lam + 2 * N;
   float* cur = cot + 2 * N;
@@ -216,39 +223,47 @@ int reverse(obs_context* ctx, const float* lx_in, const float* ly_in, float* gs,
   };
   auto zero = [&](float* d, size_t cnt) { return cuda_status(cudaMemsetAsync(d, 0, cnt * 4, strm)); };
   Step p{ctx, t.core, t.accum, n, sc, tr, ts, t.fsx, t.fsy, t.dt};
-  if ((st = copy(lam, lx_in, N)) || (st = copy(lam + N, ly_in, N))) return st;
-  for (int sg = t.nck - 1; sg >= 0; --sg) {
-    const int k0 = sg * C, k1 = std::min(k0 + C, t.nsteps);
-    // recompute the segment's positions (x_k and its stage positions) from the checkpoint
-    if ((st = copy(seg, ck + (size_t)sg * 2 * N, 2 * N))) return st;
-    for (int k = k0; k < k1; ++k) {
-      float* xk = seg + (size_t)(k - k0) * S * 2 * N;
-      float* next = (k + 1 < k1) ? seg + (size_t)(k + 1 - k0) * S * 2 * N : nullptr;
-      if ((st = step(p, xk, next ? next : xk, vel, xk + 2 * N, next != nullptr))) return st;
-    }
-    for (int k = k1 - 1; k >= k0; --k) {
-      const float* xk = seg + (size_t)(k - k0) * S * 2 * N;
-      if ((st = zero(acc, 2 * N))) return st;
-      for (int s = S - 1; s >= 0; --s) {
-        const float* ys = xk + (size_t)s * 2 * N;   // s = 0: x_k itself
-        const float bdt = (float)(sc.b[s] * t.dt);
-        if (s == S - 1) {
-          axpby_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, bdt, lam, 0.0f, nullptr, cot);
-        } else {
-          axpby_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, bdt, lam, (float)(sc.a[s + 1] * t.dt), prev, cot);
-        }
-        ctx->launches++;
-        if ((st = zero(cur, 2 * N))) return st;
-        if ((st = run_adjoint(ctx, t.core, t.accum, 1, n, ys, ys + N, tr, ts, n, ys, ys + N, tr, ts, cot, cot + N,
-                              cur, cur + N, gs, 0)))
-          return st;
-        add_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, acc, cur);
-        ctx->launches++;
-        std::swap(cur, prev);
+  // reverse of one step from its positions xk (x_k, then y_1..y_{S-1}): lam <- lam + sum_s ybar_s
+  auto vjp_step = [&](const float* xk) -> int {
+    int rc = zero(acc, 2 * N);
+    if (rc) return rc;
+    for (int s = S - 1; s >= 0; --s) {
+      const float* ys = xk + (size_t)s * 2 * N;   // s = 0: x_k itself
+      const float bdt = (float)(sc.b[s] * t.dt);
+      if (s == S - 1) {
+        axpby_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, bdt, lam, 0.0f, nullptr, cot);
+      } else {
+        axpby_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, bdt, lam, (float)(sc.a[s + 1] * t.dt), prev, cot);
       }
-      add_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, lam, acc);
       ctx->launches++;
-      if (cudaGetLastError() != cudaSuccess) return OBS_ERR_CUDA;
+      if ((rc = zero(cur, 2 * N))) return rc;
+      if ((rc = run_adjoint(ctx, t.core, t.accum, 1, n, ys, ys + N, tr, ts, n, ys, ys + N, tr, ts, cot, cot + N, cur,
+                            cur + N, gs, 0)))
+        return rc;
+      add_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, acc, cur);
+      ctx->launches++;
+      std::swap(cur, prev);
+    }
+    add_kernel<<<grid_of(2 * n), 256, 0, strm>>>(2 * n, lam, acc);
+    ctx->launches++;
+    return cudaGetLastError() != cudaSuccess ? OBS_ERR_CUDA : OBS_OK;
+  };
+  if ((st = copy(lam, lx_in, N)) || (st = copy(lam + N, ly_in, N))) return st;
+  if (t.full) {
+    for (int k = t.nsteps - 1; k >= 0; --k)
+      if ((st = vjp_step(ck + (size_t)k * S * 2 * N))) return st;
+  } else {
+    for (int sg = t.nck - 1; sg >= 0; --sg) {
+      const int k0 = sg * C, k1 = std::min(k0 + C, t.nsteps);
+      // recompute the segment's positions (x_k and its stage positions) from the checkpoint
+      if ((st = copy(seg, ck + (size_t)sg * 2 * N, 2 * N))) return st;
+      for (int k = k0; k < k1; ++k) {
+        float* xk = seg + (size_t)(k - k0) * S * 2 * N;
+        float* next = (k + 1 < k1) ? seg + (size_t)(k + 1 - k0) * S * 2 * N : nullptr;
+        if ((st = step(p, xk, next ? next : xk, vel, xk + 2 * N, next != nullptr))) return st;
+      }
+      for (int k = k1 - 1; k >= k0; --k)
+        if ((st = vjp_step(seg + (size_t)(k - k0) * S * 2 * N))) return st;
     }
   }
   if (gx0) { add_kernel<<<grid_of(n), 256, 0, strm>>>(n, gx0, lam); ctx->launches++; }

@@ -202,7 +202,7 @@ int obs_advect_record_dev(obs_context* ctx, int core, int accum, int order, int 
                           const float* r, const float* s, double fsx, double fsy, double dt, int nsteps,
                           int checkpoint_every) {
   if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
-      checkpoint_every < 0)
+      checkpoint_every < OBS_TAPE_ALL)
     return OBS_ERR_ARG;
   if (n > 0 && (!x || !y || !r || !s)) return OBS_ERR_ARG;
   int st = obs::bind(ctx);
@@ -224,7 +224,7 @@ int obs_advect_vjp_dev(obs_context* ctx, int core, int accum, int order, int n, 
                        int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
                        long long* peak_bytes) {
   if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
-      checkpoint_every < 0)
+      checkpoint_every < OBS_TAPE_ALL)
     return OBS_ERR_ARG;
   if (n > 0 && (!x0 || !y0 || !r || !s || !lx || !ly)) return OBS_ERR_ARG;
   int st = obs::bind(ctx);
@@ -238,7 +238,7 @@ int obs_advect_vjp(obs_context* ctx, int core, int accum, int order, int n, cons
                    int checkpoint_every, const float* lx, const float* ly, float* gs, float* gx0, float* gy0,
                    long long* peak_bytes) {
   if (!ctx || bad_core_accum(core, accum) || !obs::advect_order_ok(order) || n < 0 || nsteps < 0 ||
-      checkpoint_every < 0)
+      checkpoint_every < OBS_TAPE_ALL)
     return OBS_ERR_ARG;
   if (n > 0 && (!x0 || !y0 || !r || !s || !lx || !ly)) return OBS_ERR_ARG;
   if (n == 0 || nsteps == 0) return OBS_OK;

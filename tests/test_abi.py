@@ -75,3 +75,17 @@ def test_flops_per_pair_matches_reference_counts(engine_lib, golden):
 def test_external_solver_rejects_null_counts(engine_lib):
     engine_lib.external_vel_solver_f_.restype = ctypes.c_float
     assert engine_lib.external_vel_solver_f_(None, None, None, None, None, None, None, None, None, None) < 0
+
+
+def test_python_constants_mirror_header_defines():
+    """Every OBS_<NAME> integer #define that the Python module also names as <NAME> has the same
+    value there (result types, cores, accumulation modes, schemes, flags, tape modes)."""
+    import omega2d_gb300 as og
+    seen = 0
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        for m in re.finditer(r"^#define\s+OBS_(\w+)\s+\(?(-?\d+)\)?\s*$", open(h).read(), flags=re.M):
+            name, val = m.group(1), int(m.group(2))
+            if hasattr(og, name):
+                assert getattr(og, name) == val, name
+                seen += 1
+    assert seen >= 10 and og.TAPE_ALL == -1

@@ -148,7 +148,7 @@ def test_advect_vjp_centroid_gradient_matches_fp64_reference(ctx, restatement, o
     L = restatement.lib.o_centroid_loss_d(n, po._p(xT), po._p(yT), po._p(s64), po._p(lab32),
                                           po._p(gxT), po._p(gyT), po._p(gs_direct))
     results = []
-    for every in (0, 1, 5, K):
+    for every in (0, 1, 5, K, og.TAPE_ALL):
         gs, gx0, gy0, peak = og.advect_vjp(og.Points(x, y, r, s), gxT, gyT, dt=dt, nsteps=K, order=order,
                                            checkpoint_every=every, env=env)
         results.append((gs, gx0, gy0))

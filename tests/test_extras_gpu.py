@@ -167,13 +167,24 @@ def test_recorded_tape_matches_one_shot_vjp(ctx, order):
     Xf, Yf = X0.clone(), Y0.clone()
     og.advect_dev(ctx, og.CORE_GAUSSIAN, og.COMPENSATED, order, Xf, Yf, R, S, (0.1, 0.0), dt, K)
     b = [torch.zeros(n, device=dev) for _ in range(3)]
+    launches = ctx.launches
     og.advect_vjp_tape_dev(ctx, LX, LY, *b)
+    ck_launches = ctx.launches - launches
     c = [torch.zeros(n, device=dev) for _ in range(3)]
     og.advect_vjp_tape_dev(ctx, LX, LY, *c)                  # the tape can be replayed
+    # full tape: every step's positions and stage positions kept, nothing recomputed
+    X2, Y2 = X0.clone(), Y0.clone()
+    og.advect_record_dev(ctx, og.CORE_GAUSSIAN, og.COMPENSATED, order, X2, Y2, R, S, (0.1, 0.0), dt, K, og.TAPE_ALL)
+    d = [torch.zeros(n, device=dev) for _ in range(3)]
+    launches = ctx.launches
+    og.advect_vjp_tape_dev(ctx, LX, LY, *d)
+    full_launches = ctx.launches - launches
     ctx.synchronize()
     assert torch.equal(X, Xf) and torch.equal(Y, Yf)        # recording moves like advect_dev
-    for u, v, w in zip(a, b, c):
-        assert torch.equal(u, v) and torch.equal(v, w)
+    assert torch.equal(X2, Xf) and torch.equal(Y2, Yf)
+    for u, v, w, z in zip(a, b, c, d):
+        assert torch.equal(u, v) and torch.equal(v, w) and torch.equal(u, z)
+    assert 0 < full_launches < ck_launches                 # no recomputed velocity sums
 
 
 def test_tape_required(ctx):
