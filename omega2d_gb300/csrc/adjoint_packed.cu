@@ -17,10 +17,9 @@
 //   ADJ_SELF (owner = particle k, element = particle j, d = x_k - x_j):
 //     wu = G_j lu_k - G_k lu_j, wv = G_j lv_k - G_k lv_j, q = dx wv - dy wu,
 //     AX = sum K wv + B q dx,  AY = sum -K wu + B q dy,  AE = sum K (dx lv_j - dy lu_j),
-//     dL/dG_k = -AE                                                          [20 f32x2 ops + rcp]
-//   the far form of ADJ_SELF is evaluated as moments (pa_block_self_far)      [17 f32x2 ops + rcp]
+//     dL/dG_k = -AE; the far form is evaluated as moments (pa_block_self_far) [17 f32x2 ops + rcp]
 // Element layout (4 float4): ADJ_SRC  (x,x,y,y) (lv,lv,-lu,-lu) (-2lv,-2lv,2lu,2lu) (z,z,0,0)
-//                            ADJ_SELF (-x,-x,-y,-y) (lv,lv,-lu,-lu) (G,G,-2G,-2G) (z,z,lu,lu)
+//                            ADJ_SELF (-x,-x,-y,-y) (lv,lv,-lu,-lu) (G,G,lu,lu) (z,z,0,0)
 #include <algorithm>
 #include <cstring>
 
@@ -99,9 +98,9 @@ __global__ void pa_pack_kernel(const float* __restrict__ x, const float* __restr
       const float G = g[j];
       o[0] = make_float4(-X, -X, -Y, -Y);
       o[1] = make_float4(V, V, -U, -U);
-      o[2] = make_float4(G, G, -2.0f * G, -2.0f * G);
+      o[2] = make_float4(G, G, U, U);
     }
-    o[3] = make_float4(z, z, MODE == PA_SELF ? U : 0.0f, MODE == PA_SELF ? U : 0.0f);
+    o[3] = make_float4(z, z, 0.0f, 0.0f);
   } else if (i < n_pad) {
     float4* o = out + (size_t)PA_ELEM * i;
     o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -158,10 +157,9 @@ __device__ __forceinline__ void pa_block_self_far(const float4* __restrict__ blk
     const float4 E0 = blk[PA_ELEM * jj];
     const float4 E1 = blk[PA_ELEM * jj + 1];
     const float4 E2 = blk[PA_ELEM * jj + 2];
-    const float2 lu = reinterpret_cast<const float2*>(blk + PA_ELEM * jj + 3)[1];   // (lu, lu) of E3
     const float2 ex = f2(E0.x, E0.y), ey = f2(E0.z, E0.w);
     const float2 lv = f2(E1.x, E1.y), nlu = f2(E1.z, E1.w);
-    const float2 G = f2(E2.x, E2.y);
+    const float2 G = f2(E2.x, E2.y), lu = f2(E2.z, E2.w);
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       const float2 dx = __fadd2_rn(ex, w[p].c0);
@@ -237,7 +235,8 @@ __device__ __forceinline__ void pa_block(const float4* __restrict__ blk, const P
           b1 = (d2.y * ucf > 16.0f) ? -2.0f * k1 * k1 : b1;
         }
         K = f2(k0, k1);
-        B = f2(-0.5f * b0, -0.5f * b1);   // scaled so that B * q2 = B q
+        // ADJ_SRC: scaled so that B * q2 = B q (q2 = -2 q from the element); ADJ_SELF forms q itself
+        B = (MODE == PA_SRC) ? f2(-0.5f * b0, -0.5f * b1) : f2(b0, b1);
       }
       if constexpr (MODE == PA_SRC) {
         const float2 Q1 = f2(E2.x, E2.y), Q2 = f2(E2.z, E2.w);    // -2 lv, 2 lu
@@ -254,22 +253,17 @@ __device__ __forceinline__ void pa_block(const float4* __restrict__ blk, const P
           acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, M, acc[p].ay));
         }
       } else {
-        const float2 G = f2(E2.x, E2.y), m2G = f2(E2.z, E2.w);
+        // full form (the far blocks of ADJ_SELF run pa_block_self_far)
+        const float2 G = f2(E2.x, E2.y);
         const float2 qe = __ffma2_rn(dx, P, __fmul2_rn(dy, M));             // dx lv_j - dy lu_j
         const float2 qo = __ffma2_rn(dx, w[p].lvk, __fmul2_rn(dy, w[p].nluk));
-        const float2 q2 = __ffma2_rn(m2G, qo, __fmul2_rn(w[p].p2g, qe));    // -2 q
+        const float2 q = __ffma2_rn(G, qo, __fmul2_rn(w[p].ng, qe));        // G_j qo - G_k qe
         acc[p].ah = __ffma2_rn(K, qe, acc[p].ah);
         const float2 wv = __ffma2_rn(G, w[p].lvk, __fmul2_rn(w[p].ng, P));
         const float2 nwu = __ffma2_rn(G, w[p].nluk, __fmul2_rn(w[p].ng, M));
-        if constexpr (FAST) {
-          const float2 h = __fmul2_rn(K, q2);
-          acc[p].ax = __ffma2_rn(K, __ffma2_rn(h, dx, wv), acc[p].ax);
-          acc[p].ay = __ffma2_rn(K, __ffma2_rn(h, dy, nwu), acc[p].ay);
-        } else {
-          const float2 bq = __fmul2_rn(B, q2);
-          acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, wv, acc[p].ax));
-          acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, nwu, acc[p].ay));
-        }
+        const float2 bq = __fmul2_rn(B, q);
+        acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, wv, acc[p].ax));
+        acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, nwu, acc[p].ay));
       }
     }
   }
@@ -291,8 +285,8 @@ __device__ __forceinline__ void pa_store(const PAArgs& a, int i, double ax, doub
   if (a.gg) a.gg[o] = (float)((double)a.gg[o] + sg);
 }
 
-// The compensated self gather keeps 7 CTAs per SM (72 registers): at 8 (64 registers) its far
-// form spills, and measured 3 % slower on the 1M Gaussian patch.
+// With one owner pair per thread the compensated self gather keeps 7 CTAs per SM (72
+// registers): at 8 (64 registers) its far form spills.
 template <int MODE, bool THICK, bool COMP, int NP>
 __global__ void __launch_bounds__(PA_THREADS, NP == 1 ? (MODE == PA_SELF && COMP ? 7 : 8) : 4)
     pa_kernel(const PAArgs a) {
@@ -470,13 +464,14 @@ __global__ void pa_reduce_kernel(const PAArgs a) {
   pa_store<MODE>(a, i, c[0], c[1], c[2]);
 }
 
-// f32x2 owner pairs per thread: 2 for the source-side gather (about 110 registers, 4 CTAs per
-// SM), 1 for the self gather (64 registers, 8 CTAs per SM)
+// f32x2 owner pairs per thread: 2 for both gathers (about 110-127 registers, 4 CTAs per SM).
+// The self gather with its moments far form: 615 ms on the 1M Gaussian patch with 2 pairs
+// against 647 ms with 1 pair (72 registers, 7 CTAs per SM) and 662 ms (64 registers, 8 CTAs).
 #ifndef OBS_PA_SRC_NP
 #define OBS_PA_SRC_NP 2
 #endif
 #ifndef OBS_PA_SELF_NP
-#define OBS_PA_SELF_NP 1
+#define OBS_PA_SELF_NP 2
 #endif
 constexpr int pa_np(int mode) { return mode == PA_SRC ? OBS_PA_SRC_NP : OBS_PA_SELF_NP; }
 
