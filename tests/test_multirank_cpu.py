@@ -37,7 +37,7 @@ def _rank_main(rank, ws, port, out):
 
 def test_two_ranks_max_time_and_aggregate_rate():
     ws = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:         # no fork of this multi-threaded process
         out = m.dict()
         mp.start_processes(_rank_main, args=(ws, _free_port(), out), nprocs=ws, join=True, start_method="spawn")
         res = dict(out)
