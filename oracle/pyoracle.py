@@ -266,6 +266,18 @@ class Reference:
         fn(ctypes.c_int(nx.size), _p(nx), _p(ny), ctypes.c_int(npan), _p(idx), _p(out))
         return out.reshape(2 * npan, 2 * npan).T.copy()
 
+    def panels_on_panels_coeff_pair(self, snx, sny, sidx, tnx, tny, tidx):
+        """The reference's block of one body's panels (source) on another body's (target):
+        src/Coefficients.h:155-427 with src != targ, so no self term; (rows, cols) array."""
+        snx, sny, tnx, tny = (_arr(a, np.float32) for a in (snx, sny, tnx, tny))
+        sidx, tidx = _arr(sidx, np.uint32), _arr(tidx, np.uint32)
+        snp, tnp = sidx.size // 2, tidx.size // 2
+        out = np.zeros(4 * snp * tnp, np.float32)
+        self.lib.ref_panels_on_panels_coeff_pair_f(ctypes.c_int(snx.size), _p(snx), _p(sny), ctypes.c_int(snp),
+                                                   _p(sidx), ctypes.c_int(tnx.size), _p(tnx), _p(tny),
+                                                   ctypes.c_int(tnp), _p(tidx), _p(out))
+        return out.reshape(2 * snp, 2 * tnp).T.copy()
+
     def vels_to_rhs_panels(self, nx, ny, idx, pu, pv, bct, bcn):
         nx, ny, pu, pv, bct, bcn = (_arr(a, np.float32) for a in (nx, ny, pu, pv, bct, bcn))
         idx = _arr(idx, np.uint32)

@@ -169,6 +169,34 @@ def make_augment(out):
     np.savez_compressed(out, **d)
 
 
+def make_bodies(out):
+    """Two bodies in one BEM system, assembled block by block as solve_bem does
+    (src/BEMHelper.h:166-221): a circle and an irregular closed polygon; block (t, s) is
+    panels_on_panels_coeff of body s on body t, the self term only on the diagonal blocks."""
+    rng = np.random.default_rng(20240606)
+    bodies = []
+    nx, ny, idx = circle_panels(36)
+    bodies.append((nx, ny, idx))
+    th = -2.0 * np.pi * np.sort(rng.uniform(0, 1, 24))
+    rad = 0.3 + 0.06 * np.sin(2 * th)
+    bodies.append(((1.3 + rad * np.cos(th)).astype(np.float32), (0.4 + rad * np.sin(th)).astype(np.float32),
+                   np.stack([np.arange(24), (np.arange(24) + 1) % 24], 1).ravel().astype(np.uint32)))
+    ref = po.Reference(po.V2)
+    rows = []
+    for t in bodies:
+        blocks = []
+        for s in bodies:
+            if s is t:
+                blocks.append(ref.panels_on_panels_coeff(*s))
+            else:
+                blocks.append(ref.panels_on_panels_coeff_pair(*s, *t))
+        rows.append(np.concatenate(blocks, axis=1))
+    d = {"A": np.concatenate(rows, axis=0)}
+    for k, (nx, ny, idx) in enumerate(bodies):
+        d[f"nx{k}"], d[f"ny{k}"], d[f"idx{k}"] = nx, ny, idx
+    np.savez_compressed(out, **d)
+
+
 def main():
     if not build_ref.available():
         raise SystemExit("the reference tree is needed to generate golden vectors")
@@ -178,6 +206,7 @@ def main():
     make_advect(os.path.join(HERE, "advect.npz"))
     make_extras(os.path.join(HERE, "extras.npz"))
     make_augment(os.path.join(HERE, "augment.npz"))
+    make_bodies(os.path.join(HERE, "bodies.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

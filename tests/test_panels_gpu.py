@@ -378,3 +378,39 @@ def test_panel_autograd_wrapper_matches_c_abi(ctx):
     assert rel_err(targ.u, u.detach().cpu().numpy()) < 1e-6
     gv, gs = og.panels_affect_points_vjp(surf, og.Points(x, y), 2 * targ.u, 2 * targ.v, env)
     assert rel_err(gv, tvs.grad.cpu().numpy()) < 1e-6 and rel_err(gs, tss.grad.cpu().numpy()) < 1e-6
+
+
+def test_two_bodies_matrix_matches_reference_block_assembly(ctx, golden, restatement):
+    """The joined panel set of two bodies against the reference's block-by-block assembly
+    (tests/golden/bodies.npz; src/BEMHelper.h:166-221)."""
+    g = golden("bodies")
+    j, _ = og.join_surfaces([og.Surfaces(g["nx0"], g["ny0"], g["idx0"]), og.Surfaces(g["nx1"], g["ny1"], g["idx1"])])
+    A = og.panels_on_panels_coeff(j, nunk=2, context=ctx)
+    assert A.shape == (120, 120)
+    assert rel_err(g["A"], A) < TOLREF
+    A64 = restatement.panels_on_panels_coeff(2, j.nx, j.ny, j.idx, fp64=True)
+    # the FP32 assembly is 1.2e-5 off FP64 on this pair of bodies (uneven polygon panels near
+    # the circle), as the reference's own float build is (1.2e-5)
+    assert rel_err(A64, A) < 2e-5
+
+
+def test_solve_bem_two_bodies_matches_fp64_restatement(ctx, restatement):
+    rng = np.random.default_rng(5)
+    n = 20_000
+    r = np.sqrt(rng.uniform(0.55 ** 2, 9.0, n))
+    t = rng.uniform(0, 2 * np.pi, n)
+    x, y = r * np.cos(t), r * np.sin(t)
+    keep = np.hypot(x - 1.5, y - 0.3) > 0.36                 # outside the second body too
+    x, y = x[keep].astype(np.float32), y[keep].astype(np.float32)
+    s = rng.normal(0, 1e-2, x.size).astype(np.float32)
+    a, b = og.circle_panels(256), og.circle_panels(128, 0.6, center=(1.5, 0.3))
+    vort = og.Points(x, y, np.full(x.size, 0.01, np.float32), s)
+    rel = og.solve_bem_bodies(vort, [a, b], fs=(1.0, 0.0), nunk=2,
+                              env=og.ExecEnv(accum=og.COMPENSATED, context=ctx))
+    assert rel < 1e-12
+    j, offs = og.join_surfaces([og.circle_panels(256), og.circle_panels(128, 0.6, center=(1.5, 0.3))])
+    assert list(offs) == [0, 256, 384]
+    xr = _restated_bem(restatement, j, x, y, s, (1.0, 0.0), 2)
+    got = np.stack([np.concatenate([a.vs, b.vs]), np.concatenate([a.ss, b.ss])], 1).ravel()
+    # FP32 assembly as in the reference; cond(A) ~ 850 here moves the FP64 solution by ~2e-5
+    assert rel_err(xr, got) < 3e-4
