@@ -31,7 +31,9 @@
 #define CBRT cbrtf
 #define ATAN2 atan2f
 #define FMA fmaf
+#define NEXTAFTER nextafterf
 #include "oracle_impl.h"
+#undef NEXTAFTER
 #undef R
 #undef A
 #undef SFX
@@ -52,7 +54,9 @@
 #define CBRT cbrt
 #define ATAN2 atan2
 #define FMA fma
+#define NEXTAFTER nextafter
 #include "oracle_impl.h"
+#undef NEXTAFTER
 #undef R
 #undef A
 #undef SFX

@@ -555,3 +555,184 @@ void SFX(o_advect_3rd)(int core, int n, R* x, R* y, const R* r, const R* s,
   }
   free(buf);
 }
+
+/* ---------------------------------------------------------------- clear_inner_panp2
+ * src/Reflect.h:491-729 (with panel_point_distance :111-165, init_cut_tables :383-443,
+ * get_cut_entry :448-480 and the panel normals of Surfaces::compute_bases, src/Surfaces.h:
+ * 682-724).  The reference's C++ promotions are spelled out: std::pow(S, 2) and the 1.0
+ * literals are double, so those sub-expressions are formed in double and rounded to R where
+ * the reference stores them. */
+
+/* closest point of the segment (x0,y0)-(x1,y1) to (tx,ty): kind 0 interior, 1 a node (which) */
+static inline void SFX(seg_closest)(R x0, R y0, R x1, R y1, R tx, R ty, R* d2, R* cx, R* cy, int* kind,
+                                    int* which) {
+  const R bx = x1 - x0, by = y1 - y0;
+  const R blensq = bx * bx + by * by;
+  const R ax = tx - x0, ay = ty - y0;
+  const R t = (ax * bx + ay * by) / blensq;
+  if (t > 0.0 && t < 1.0) {
+    const R c = ay * bx - ax * by;
+    *d2 = (R)(((double)c * (double)c) / (double)blensq);
+    *cx = (R)((1.0 - (double)t) * (double)x0 + (double)(t * x1));
+    *cy = (R)((1.0 - (double)t) * (double)y0 + (double)(t * y1));
+    *kind = 0;
+    *which = -1;
+    return;
+  }
+  const R ex = tx - x1, ey = ty - y1;
+  const R r0 = (R)((double)ax * (double)ax + (double)ay * (double)ay);
+  const R r1 = (R)((double)ex * (double)ex + (double)ey * (double)ey);
+  *kind = 1;
+  if (r0 < r1) { *which = 0; *d2 = r0; *cx = x0; *cy = y0; }
+  else { *which = 1; *d2 = r1; *cx = x1; *cy = y1; }
+}
+
+/* init_cut_tables(0.1): entries (position in core radii, strength kept, shift in core radii) */
+#define CUT_N 63
+static void SFX(cut_tables)(R* pos, R* keep, R* shift) {
+  const R max_rad = (R)3.0, dx_in = (R)0.1;
+  const int nx = (int)(0.5 + (double)(max_rad / dx_in));
+  const R dx = max_rad / (R)(float)nx;
+  int k = 0;
+  pos[k] = (R)(-nx - 0.5) * dx; keep[k] = 0; shift[k] = 0; ++k;
+  R twgt = 0, tmom = 0;
+  for (int i = -nx; i < nx + 1; ++i) {
+    const R pi_ = (R)i * dx;
+    const R distxs = (R)((double)pi_ * (double)pi_);
+    R rwgt = 0;
+    for (int j = -nx; j < nx + 1; ++j) {
+      const R pj = (R)j * dx;
+      const R distxys = (R)((double)distxs + (double)pj * (double)pj);
+      rwgt += EXP(-distxys);
+    }
+    rwgt = (R)((double)rwgt * ((double)dx * (double)dx));
+    rwgt = (R)((double)rwgt * (1.0 / M_PI));
+    twgt += rwgt;
+    tmom += ((R)i * dx) * rwgt;
+    pos[k] = (R)(i + 0.5) * dx; keep[k] = twgt; shift[k] = -tmom / twgt; ++k;
+  }
+  pos[k] = (R)(nx + 1.5) * dx; keep[k] = 1; shift[k] = 0;
+}
+
+static void SFX(cut_entry)(const R* pos, const R* keep, const R* shift, R p, R* smult, R* dshift) {
+  *smult = 1;
+  *dshift = 0;
+  if (p < pos[0]) {
+    *smult = 0;
+    *dshift = (R)(1.0 - (double)p);
+  } else if (p > pos[CUT_N - 1]) {
+    return;
+  } else {
+    for (int i = 1; i < CUT_N; ++i) {
+      if (p < pos[i]) {
+        const R frac = (p - pos[i - 1]) / (pos[i] - pos[i - 1]);
+        *smult = (R)((double)(frac * keep[i]) + (1.0 - (double)frac) * (double)keep[i - 1]);
+        *dshift = (R)((double)(frac * shift[i]) + (1.0 - (double)frac) * (double)shift[i - 1]);
+        return;
+      }
+    }
+  }
+}
+
+/* One body's panels clear the particles (r given) or field points (r NULL) lying within the
+ * cutoff layer: method 0 crops strength and shifts outward with the cut tables, method 1
+ * pushes the point onto the layer (src/Reflect.h:644-696).  Each sweep visits the untested
+ * points in order (the reference's OpenMP loop run on one thread); a point stays untested while
+ * it is modified.  Returns the circulation removed (method 0, particles); *ncropped counts the
+ * modifications.  Method 0 on field points never terminates in the reference and is refused
+ * here (returns NAN). */
+double SFX(o_clear_inner)(int method, R cutoff_mult, R ips, int nnodes, const R* nx, const R* ny, int npan,
+                          const unsigned* idx, int n, R* x, R* y, R* s, const R* r, long* ncropped) {
+  const int fld = (r == NULL);
+  if ((method == 0 && fld) || npan <= 0) return NAN;
+  R* pn = (R*)calloc(2 * (size_t)npan + 2 * (size_t)nnodes, sizeof(R));
+  R *pnx = pn, *pny = pn + npan, *nnx = pn + 2 * npan, *nny = nnx + nnodes;
+  for (int j = 0; j < npan; ++j) {
+    const unsigned a = idx[2 * j], b = idx[2 * j + 1];
+    R tx1 = nx[b] - nx[a], ty1 = ny[b] - ny[a];
+    const R base = SQRT(tx1 * tx1 + ty1 * ty1);
+    tx1 = (R)((double)tx1 * (1.0 / (double)base));
+    ty1 = (R)((double)ty1 * (1.0 / (double)base));
+    pnx[j] = -ty1;
+    pny[j] = tx1;
+  }
+  for (int j = 0; j < npan; ++j) {
+    const unsigned a = idx[2 * j], b = idx[2 * j + 1];
+    nnx[a] += pnx[j]; nny[a] += pny[j];
+    nnx[b] += pnx[j]; nny[b] += pny[j];
+  }
+  R cpos[CUT_N], ckeep[CUT_N], cshift[CUT_N];
+  SFX(cut_tables)(cpos, ckeep, cshift);
+  unsigned char* untested = (unsigned char*)malloc((size_t)n + 1);
+  memset(untested, 1, (size_t)n + 1);
+  const R big = (R)(0.1 * (double)(sizeof(R) == 4 ? 3.40282347e+38 : 1.7976931348623157e+308));
+  R circ = 0;
+  long crop = 0;
+  for (;;) {
+    int any = 0;
+    for (int i = 0; i < n; ++i) any |= untested[i];
+    if (!any) break;
+    R part = 0;
+    for (int i = 0; i < n; ++i) {
+      if (!untested[i]) continue;
+      R mind = big, snx = 0, sny = 0, scx = 0, scy = 0;
+      int cnt = 0;
+      for (int j = 0; j < npan; ++j) {
+        const unsigned a = idx[2 * j], b = idx[2 * j + 1];
+        R d2, cx, cy;
+        int kind, which;
+        SFX(seg_closest)(nx[a], ny[a], nx[b], ny[b], x[i], y[i], &d2, &cx, &cy, &kind, &which);
+        int add = 0;
+        if ((double)d2 < nextafter((double)mind, 0.0)) {          /* a new closest */
+          mind = d2;
+          snx = sny = scx = scy = 0;
+          cnt = 0;
+          add = 1;
+        } else if (d2 < NEXTAFTER(mind, big * (R)10)) {            /* a tie */
+          add = 1;
+        }
+        if (add) {
+          if (kind == 0) { snx += pnx[j]; sny += pny[j]; }
+          else { const unsigned nd = which ? b : a; snx += nnx[nd]; sny += nny[nd]; }
+          scx += cx; scy += cy;
+          ++cnt;
+        }
+      }
+      if (cnt == 0) { untested[i] = 0; continue; }
+      const R normilen = (R)(1.0 / (double)SQRT(snx * snx + sny * sny));
+      snx *= normilen;
+      sny *= normilen;
+      scx /= (R)cnt;
+      scy /= (R)cnt;
+      const R dotp = snx * (x[i] - scx) + sny * (y[i] - scy) - cutoff_mult * ips;
+      const R rad = fld ? ips : r[i];
+      if (method == 0) {
+        if (dotp < rad) {
+          R smult, dshift;
+          SFX(cut_entry)(cpos, ckeep, cshift, dotp / rad, &smult, &dshift);
+          part = (R)((double)part + (double)s[i] * (1.0 - (double)smult));
+          s[i] *= smult;
+          x[i] += dshift * rad * snx;
+          y[i] += dshift * rad * sny;
+          ++crop;
+        } else {
+          untested[i] = 0;
+        }
+      } else {
+        if ((double)dotp < -0.001 * (double)ips) {
+          x[i] -= dotp * snx;
+          y[i] -= dotp * sny;
+          ++crop;
+        } else {
+          untested[i] = 0;
+        }
+      }
+    }
+    circ += part;
+  }
+  free(untested);
+  free(pn);
+  if (ncropped) *ncropped = crop;
+  return (double)circ;
+}
+#undef CUT_N

@@ -177,6 +177,24 @@ class Restatement:
                               _p(lu), _p(lv), _p(gx), _p(gy), _p(gs))
         return gx, gy, gs
 
+    def clear_inner(self, method, cutoff_mult, ips, nx, ny, idx, x, y, s=None, r=None, fp64=False):
+        """clear_inner_panp2 (src/Reflect.h:491-729): returns (x, y, s, circulation removed,
+        modifications); r None means field points."""
+        dt = np.float64 if fp64 else np.float32
+        nx, ny = _arr(nx, dt), _arr(ny, dt)
+        idx = _arr(idx, np.uint32)
+        x, y = np.array(x, dt), np.array(y, dt)
+        s = np.array(s, dt) if s is not None else np.zeros(x.size, dt)
+        r = _arr(r, dt)
+        fn = self.lib.o_clear_inner_d if fp64 else self.lib.o_clear_inner_f
+        fn.restype = ctypes.c_double
+        cast = ctypes.c_double if fp64 else ctypes.c_float
+        nc = ctypes.c_long()
+        lost = fn(ctypes.c_int(method), cast(cutoff_mult), cast(ips), ctypes.c_int(nx.size), _p(nx), _p(ny),
+                  ctypes.c_int(idx.size // 2), _p(idx), ctypes.c_int(x.size), _p(x), _p(y), _p(s), _p(r),
+                  ctypes.byref(nc))
+        return x, y, s, lost, nc.value
+
     def rk2_centroid_grad(self, core, x, y, r, s, label, fs, dt_, nsteps):
         x, y, r, s = (_arr(a, np.float64) for a in (x, y, r, s))
         label = _arr(label, np.int32)
@@ -277,6 +295,22 @@ class Reference:
                                                    _p(sidx), ctypes.c_int(tnx.size), _p(tnx), _p(tny),
                                                    ctypes.c_int(tnp), _p(tidx), _p(out))
         return out.reshape(2 * snp, 2 * tnp).T.copy()
+
+    def clear_inner(self, method, cutoff_mult, ips, nx, ny, idx, x, y, s=None, r=None):
+        """The reference's clear_inner_panp2 (src/Reflect.h:491-729) on one body: returns
+        (x, y, s, circulation removed).  Its sweep is an OpenMP loop with a reduction; run the
+        process with OMP_NUM_THREADS=1 for a reproducible circulation sum."""
+        nx, ny = _arr(nx, np.float32), _arr(ny, np.float32)
+        idx = _arr(idx, np.uint32)
+        x, y = np.array(x, np.float32), np.array(y, np.float32)
+        s = np.array(s, np.float32) if s is not None else np.zeros(x.size, np.float32)
+        r = _arr(r, np.float32)
+        fn = self.lib.ref_clear_inner_f
+        fn.restype = ctypes.c_float
+        lost = fn(ctypes.c_int(method), ctypes.c_float(cutoff_mult), ctypes.c_float(ips), ctypes.c_int(nx.size),
+                  _p(nx), _p(ny), ctypes.c_int(idx.size // 2), _p(idx), ctypes.c_int(x.size), _p(x), _p(y), _p(s),
+                  _p(r))
+        return x, y, s, float(lost)
 
     def vels_to_rhs_panels(self, nx, ny, idx, pu, pv, bct, bcn):
         nx, ny, pu, pv, bct, bcn = (_arr(a, np.float32) for a in (nx, ny, pu, pv, bct, bcn))

@@ -1,8 +1,8 @@
 // ref_harness.cpp -- C-ABI wrapper around the reference's own influence code (test infrastructure).
 //
 // This file is compiled, by oracle/build_ref.py, against the reference's unmodified headers
-// (src/Influence.h, src/Kernels.h, src/CoreFunc.h, src/Coefficients.h, src/RHS.h, src/Points.h,
-// src/Surfaces.h, src/ElementBase.h), once per core-function macro (src/CoreFunc.h:35-39).
+// (src/Influence.h, src/Kernels.h, src/CoreFunc.h, src/Coefficients.h, src/RHS.h, src/Reflect.h,
+// src/Points.h, src/Surfaces.h, src/ElementBase.h), once per core-function macro (src/CoreFunc.h:35-39).
 // The resulting libraries live in oracle/_ref/ and are used ONLY as a checker by the tests and
 // by tests/golden/make_golden.py; nothing in the product path links or loads them.
 //
@@ -17,6 +17,7 @@
 #include "InfluenceVort.h"
 #include "Coefficients.h"
 #include "RHS.h"
+#include "Reflect.h"
 
 #include <cstdio>
 #include <cstring>
@@ -466,6 +467,25 @@ int ref_panels_on_panels_coeff_augmented_f(int nnodes, const float* nx, const fl
   std::copy(c.begin(), c.end(), out);
   geom[0] = surf.get_vol();
   return (int)c.size();
+}
+
+// clear_inner_panp2 (src/Reflect.h:491-729): one body's panels clear the particles (or field
+// points when r is null) inside the cutoff layer; method 0 crops with the cut tables, 1 pushes.
+// Updates x, y, s in place; returns the circulation removed.  Run it single-threaded
+// (OMP_NUM_THREADS=1) for a reproducible sum.
+float ref_clear_inner_f(int method, float cutoff_mult, float ips, int nnodes, const float* nx, const float* ny,
+                        int npan, const unsigned* idx, int n, float* x, float* y, float* s, const float* r) {
+  Quiet q;
+  Surfaces<float> surf = make_surfaces<float>(nnodes, nx, ny, npan, idx, nullptr, nullptr, reactive);
+  Points<float> pts = make_points<float>(n, x, y, r, s, r == nullptr);
+  const float lost = clear_inner_panp2<float>(method, surf, pts, cutoff_mult, ips);
+  const auto& pos = pts.get_pos();
+  for (int i = 0; i < n; ++i) { x[i] = pos[0][i]; y[i] = pos[1][i]; }
+  if (r) {
+    const auto& st = pts.get_str();
+    for (int i = 0; i < n; ++i) s[i] = st[i];
+  }
+  return lost;
 }
 
 // flop counts the reference attaches to each kernel (src/Kernels.h flops*, src/CoreFunc.h flops_*)

@@ -7,7 +7,7 @@ Run in a checkout that has the reference tree (it builds oracle/_ref first):
 Every fixture stores its seeded inputs and the reference outputs (float32 storage, double
 accumulators: the reference's default non-Vc build).  The reference itself has no tests or
 fixtures for this path; these vectors are produced by compiling its src/Influence.h,
-src/Kernels.h, src/CoreFunc.h, src/Coefficients.h and src/RHS.h unmodified (see
+src/Kernels.h, src/CoreFunc.h, src/Coefficients.h, src/RHS.h and src/Reflect.h unmodified (see
 oracle/build_ref.py) and calling its drivers through oracle/ref_harness.cpp.
 """
 from __future__ import annotations
@@ -15,7 +15,11 @@ from __future__ import annotations
 import os
 import sys
 
-import numpy as np
+# the reference's clear_inner_panp2 sums the removed circulation in an OpenMP reduction: one
+# thread gives a reproducible order (the other fixtures do not depend on the thread count)
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+
+import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -197,6 +201,44 @@ def make_bodies(out):
     np.savez_compressed(out, **d)
 
 
+def star_panels(arms=5, r_out=0.5, r_in=0.25, center=(0.0, 0.0)):
+    """A clockwise star polygon (concave corners: ties between panels and nodes)."""
+    k = 2 * arms
+    th = -2.0 * np.pi * np.arange(k) / k
+    rad = np.where(np.arange(k) % 2 == 0, r_out, r_in)
+    nx = (center[0] + rad * np.cos(th)).astype(np.float32)
+    ny = (center[1] + rad * np.sin(th)).astype(np.float32)
+    idx = np.stack([np.arange(k), (np.arange(k) + 1) % k], 1).ravel().astype(np.uint32)
+    return nx, ny, idx
+
+
+def make_clear(out):
+    """clear_inner_panp2 (src/Reflect.h:491-729) on a circle and a star: particles scattered
+    across each surface (method 0 crops, method 1 pushes) and field points (method 1)."""
+    rng = np.random.default_rng(20240607)
+    ref = po.Reference(po.V2)
+    cut = np.float32(0.5 / np.sqrt(2.0 * np.pi))       # Convection.h:301's cutoff factor
+    ips = np.float32(0.02)
+    d = {"cut": np.array([cut]), "ips": np.array([ips])}
+    for name, (nx, ny, idx) in {"circle": circle_panels(64), "star": star_panels()}.items():
+        n = 300
+        rad = rng.uniform(0.15, 0.65, n)
+        a = rng.uniform(0, 2 * np.pi, n)
+        x = (rad * np.cos(a)).astype(np.float32)
+        y = (rad * np.sin(a)).astype(np.float32)
+        s = rng.normal(0, 1, n).astype(np.float32)
+        r = rng.uniform(0.015, 0.025, n).astype(np.float32)
+        d[name + "_nx"], d[name + "_ny"], d[name + "_idx"] = nx, ny, idx
+        d[name + "_x"], d[name + "_y"], d[name + "_s"], d[name + "_r"] = x, y, s, r
+        for m in (0, 1):
+            ox, oy, os_, lost = ref.clear_inner(m, cut, ips, nx, ny, idx, x, y, s, r)
+            d[f"{name}_m{m}_x"], d[f"{name}_m{m}_y"], d[f"{name}_m{m}_s"] = ox, oy, os_
+            d[f"{name}_m{m}_lost"] = np.array([lost])
+        fx, fy, _, _ = ref.clear_inner(1, np.float32(0.0), ips, nx, ny, idx, x, y, None, None)
+        d[name + "_fld_x"], d[name + "_fld_y"] = fx, fy
+    np.savez_compressed(out, **d)
+
+
 def main():
     if not build_ref.available():
         raise SystemExit("the reference tree is needed to generate golden vectors")
@@ -207,6 +249,7 @@ def main():
     make_extras(os.path.join(HERE, "extras.npz"))
     make_augment(os.path.join(HERE, "augment.npz"))
     make_bodies(os.path.join(HERE, "bodies.npz"))
+    make_clear(os.path.join(HERE, "clear.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
