@@ -421,6 +421,8 @@ def join_surfaces(bodies) -> tuple[Surfaces, np.ndarray]:
     pair formula is the same as within one body, that matrix equals the coefficients of the
     joined panel set bit for bit in the reference's own arithmetic."""
     bodies = list(bodies)
+    if not bodies:
+        raise ValueError("join_surfaces: no bodies")
     offs = np.zeros(len(bodies) + 1, np.int64)
     node0 = 0
     nx, ny, idx = [], [], []

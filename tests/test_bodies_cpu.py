@@ -29,6 +29,8 @@ def test_join_surfaces_offsets_and_indices():
     np.testing.assert_array_equal(j.nx[12:], b.nx)
     np.testing.assert_array_equal(j.vs, np.concatenate([a.vs, b.vs]))
     assert j.ss is None                                  # only carried when every body has it
+    with pytest.raises(ValueError):
+        og.join_surfaces([])
     # panel k of the joined set is panel k - offs[body] of its body
     for k in (0, 11, 12, 18):
         body, local = (a, k) if k < 12 else (b, k - 12)
