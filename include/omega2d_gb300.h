@@ -272,6 +272,22 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
                   float* vs_out, float* ss_out, double* rel_residual);
 
+/* clear_inner_layer -- replaces src/Reflect.h:733-760 (clear_inner_panp2, :491-729) for one body
+ * and one point set.  The height of a point above the layer at cutoff_mult * ips is measured
+ * along the mean normal of its closest panels or nodes; method 0 (particles only) crops a point
+ * lower than its core radius (strength scaled, point shifted outward by the reference's cut
+ * tables), method 1 pushes a point below the layer onto it.  x, y (and s, method 0) are updated in place;
+ * r holds the points' core radii (NULL: field points, whose radius is ips).  circ_removed
+ * (optional) receives the circulation removed (the body's add_to_reabsorbed), ncropped the
+ * number of modifications.  OBS_ERR_NO_CONVERGENCE when a point was still being modified
+ * after 64 tests (the others are cleared). */
+int obs_clear_inner_layer(obs_context* ctx, int method, float cutoff_mult, float ips, int nnodes, const float* nx,
+                          const float* ny, int npan, const unsigned* idx, int n, float* x, float* y, float* s,
+                          const float* r, double* circ_removed, long long* ncropped);
+int obs_clear_inner_layer_dev(obs_context* ctx, int method, float cutoff_mult, float ips, int nnodes,
+                              const float* nx, const float* ny, int npan, const unsigned* idx, int n, float* x,
+                              float* y, float* s, const float* r, double* circ_removed, long long* ncropped);
+
 /* Rotation augmentation (src/Coefficients.h:429-572, src/BEMHelper.h:114-135, 197-205): the self
  * block of one body gains a bottom row of panel lengths (under the vortex unknowns), a right
  * column of the unit-rotation velocity along each panel (Surfaces::add_unit_rot_strengths about

@@ -613,6 +613,26 @@ def solve_bem_bodies(vort: Points, bodies, fs=(0.0, 0.0), nunk: int = 2, env: Ex
     return rel
 
 
+# Convection.h:301-302's cutoff factor for clear_inner_layer
+CLEAR_CUTOFF = float(0.5 / np.sqrt(2.0 * np.pi))
+
+
+def clear_inner_layer(pts: Points, body: Surfaces, ips: float, method: int = 0, cutoff_mult: float = CLEAR_CUTOFF,
+                      env: ExecEnv | None = None) -> tuple[float, int]:
+    """clear_inner_layer for one body (src/Reflect.h:733-760 over clear_inner_panp2, :491-729):
+    method 0 crops the particles inside the cutoff layer (strengths scaled, points shifted
+    outward by the cut tables), method 1 pushes points (particles, or field points without
+    radii) onto the layer.  Updates pts.x, pts.y (and pts.s) in place; returns (circulation
+    removed, number of modifications)."""
+    env = env or ExecEnv()
+    circ, nc = ctypes.c_double(), ctypes.c_longlong()
+    st = lib().obs_clear_inner_layer(env.ctx().handle, ctypes.c_int(method), ctypes.c_float(cutoff_mult),
+                                     ctypes.c_float(ips), *body._geo(), ctypes.c_int(pts.n), _ptr(pts.x), _ptr(pts.y),
+                                     _ptr(pts.s), _ptr(pts.r), ctypes.byref(circ), ctypes.byref(nc))
+    _check(st, "obs_clear_inner_layer")
+    return circ.value, nc.value
+
+
 # ---------------------------------------------------------------- device-resident panel calls
 # All arrays are CUDA tensors (node coordinates float32, idx int32/uint32 pairs); asynchronous
 # on the context's stream, same semantics as the host calls above.

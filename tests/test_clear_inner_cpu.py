@@ -79,3 +79,106 @@ def test_clear_inner_matches_live_reference(restatement):
     gx, gy, gs, glost = ref.clear_inner(0, cut, ips, nx, ny, idx, x, y, s, r)
     ox, oy, os_, lost, _ = restatement.clear_inner(0, cut, ips, nx, ny, idx, x, y, s, r)
     _check_method0(gx, gy, gs, ox, oy, os_, r)
+
+
+# ------------------------------------------------------------------ the engine's per-point logic
+# omega2d_gb300/csrc/clear_inner.cuh is the code the CUDA kernel runs per point; it also compiles
+# for the host.  This harness runs it over an array the way clear_points_kernel does.
+HARNESS = r"""
+#include "clear_inner.cuh"
+#include <vector>
+extern "C" int host_clear(int method, float cut, float ips, int nnodes, const float* nx, const float* ny, int npan,
+                          const unsigned* idx, int n, float* x, float* y, float* s, const float* r, double* lost,
+                          long long* ncrop) {
+  std::vector<float> pn(2 * (size_t)npan), nn(2 * (size_t)nnodes), ct(3 * obs::clear::CUT_N);
+  if (obs::clear::normals(nnodes, nx, ny, npan, idx, pn.data(), pn.data() + npan, nn.data(), nn.data() + nnodes))
+    return -1;
+  obs::clear::cut_table(ct.data(), ct.data() + obs::clear::CUT_N, ct.data() + 2 * obs::clear::CUT_N);
+  const obs::clear::Geo g{nx, ny, idx, npan, pn.data(), pn.data() + npan, nn.data(), nn.data() + nnodes,
+                          ct.data(), ct.data() + obs::clear::CUT_N, ct.data() + 2 * obs::clear::CUT_N};
+  double tot = 0.0;
+  long long crops = 0;
+  int fail = 0;
+  for (int i = 0; i < n; ++i) {
+    float si = s ? s[i] : 0.0f;
+    double l = 0.0;
+    const int c = obs::clear::clear_point(g, method, cut, ips, r ? r[i] : ips, x[i], y[i], si, l, 64);
+    if (s) s[i] = si;
+    tot += l;
+    if (c < 0) ++fail; else crops += c;
+  }
+  *lost = tot;
+  *ncrop = crops;
+  return fail;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def engine_logic(tmp_path_factory):
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("needs g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    d = tmp_path_factory.mktemp("clear")
+    src = d / "harness.cpp"
+    src.write_text(HARNESS)
+    lib = d / "libharness.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(root, "omega2d_gb300", "csrc"),
+                    str(src), "-o", str(lib)], check=True)
+    L = ctypes.CDLL(str(lib))
+
+    def run(method, cut, ips, nx, ny, idx, x, y, s=None, r=None):
+        f32 = lambda a: None if a is None else np.array(a, np.float32)
+        nx, ny, x, y, s, r = (f32(a) for a in (nx, ny, x, y, s, r))
+        idx = np.ascontiguousarray(idx, np.uint32)
+        lost, nc = ctypes.c_double(), ctypes.c_longlong()
+        fail = L.host_clear(ctypes.c_int(method), ctypes.c_float(cut), ctypes.c_float(ips), ctypes.c_int(nx.size),
+                            po._p(nx), po._p(ny), ctypes.c_int(idx.size // 2), po._p(idx), ctypes.c_int(x.size),
+                            po._p(x), po._p(y), po._p(s), po._p(r), ctypes.byref(lost), ctypes.byref(nc))
+        assert fail == 0
+        return x, y, s, lost.value, nc.value
+    return run
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_engine_point_logic_matches_golden_and_oracle(engine_logic, restatement, golden, shape):
+    g = golden("clear")
+    cut, ips = g["cut"][0], g["ips"][0]
+    nx, ny, idx = g[shape + "_nx"], g[shape + "_ny"], g[shape + "_idx"]
+    x, y, s, r = g[shape + "_x"], g[shape + "_y"], g[shape + "_s"], g[shape + "_r"]
+    ex, ey, es, elost, enc = engine_logic(0, cut, ips, nx, ny, idx, x, y, s, r)
+    _check_method0(g[shape + "_m0_x"], g[shape + "_m0_y"], g[shape + "_m0_s"], ex, ey, es, r)
+    glost = g[shape + "_m0_lost"][0]
+    assert abs(elost - glost) < 1e-5 * max(1.0, abs(glost))
+    # the oracle sweeps all points per pass, the engine repeats each point: same per-point result
+    ox, oy, os_, olost, onc = restatement.clear_inner(0, cut, ips, nx, ny, idx, x, y, s, r)
+    same = (ex == ox) & (ey == oy) & (es == os_)
+    assert same.mean() > 0.95 and enc == onc
+    _check_method0(ox, oy, os_, ex, ey, es, r)
+    px, py, ps, plost, pnc = engine_logic(1, cut, ips, nx, ny, idx, x, y, s, r)
+    assert plost == 0.0 and pnc > 0
+    np.testing.assert_array_equal(ps, s)
+    assert np.max(np.hypot(px - g[shape + "_m1_x"], py - g[shape + "_m1_y"])) < 1e-5
+    fx, fy, _, _, _ = engine_logic(1, 0.0, ips, nx, ny, idx, x, y)
+    assert np.max(np.hypot(fx - g[shape + "_fld_x"], fy - g[shape + "_fld_y"])) < 1e-5
+
+
+def test_engine_point_logic_guards(engine_logic):
+    """A point on a panel and one on a node are pushed out along the panel / node normal; one far
+    outside is untouched; the centre of the diamond ties all four panels, whose normals cancel,
+    and stays put (as in the reference: its normal is NaN, so the test never fires); a NaN point
+    ends without a closest panel."""
+    nx = np.array([0.5, 0.0, -0.5, 0.0], np.float32)
+    ny = np.array([0.0, -0.5, 0.0, 0.5], np.float32)                  # clockwise diamond
+    idx = np.array([0, 1, 1, 2, 2, 3, 3, 0], np.uint32)
+    x = np.array([0.25, 0.5, 10.0, 0.0, np.nan], np.float32)
+    y = np.array([-0.25, 0.0, 0.0, 0.0, 0.0], np.float32)
+    px, py, _, _, nc = engine_logic(1, 0.2, 0.02, nx, ny, idx, x, y)
+    # the reference's own result for the first four (src/Reflect.h:491-729, its float build)
+    np.testing.assert_allclose(px[:4], [0.25282842, 0.504, 10.0, 0.0], rtol=0, atol=1e-7)
+    np.testing.assert_allclose(py[:4], [-0.25282842, 0.0, 0.0, 0.0], rtol=0, atol=1e-7)
+    assert np.isnan(px[4]) and nc == 2

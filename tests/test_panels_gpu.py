@@ -414,3 +414,59 @@ def test_solve_bem_two_bodies_matches_fp64_restatement(ctx, restatement):
     got = np.stack([np.concatenate([a.vs, b.vs]), np.concatenate([a.ss, b.ss])], 1).ravel()
     # FP32 assembly as in the reference; cond(A) ~ 850 here moves the FP64 solution by ~2e-5
     assert rel_err(xr, got) < 3e-4
+
+
+def _clear_check_method0(g_x, g_y, g_s, x, y, s, r):
+    """A fully cropped particle lands exactly on the layer and the rounding of that shift
+    decides one further cut (at most 0.12 core radii, strength already 0): positions of such
+    particles are compared within that shift, everything else tightly."""
+    cropped = g_s == 0.0
+    d = np.hypot(g_x - x, g_y - y)
+    assert np.all(d[~cropped] < 1e-5), np.max(d[~cropped])
+    assert np.all(d[cropped] <= 0.12 * r[cropped] + 1e-6)
+    assert np.all(s[cropped] == 0.0)
+    np.testing.assert_allclose(s, g_s, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("shape", ["circle", "star"])
+def test_clear_inner_layer_matches_reference(ctx, golden, shape):
+    """clear_inner_layer (src/Reflect.h:491-760) against the reference's own routine
+    (tests/golden/clear.npz): crop, push, and push of field points."""
+    g = golden("clear")
+    cut, ips = float(g["cut"][0]), float(g["ips"][0])
+    body = og.Surfaces(g[shape + "_nx"], g[shape + "_ny"], g[shape + "_idx"])
+    env = og.ExecEnv(context=ctx)
+    x, y, s, r = g[shape + "_x"], g[shape + "_y"], g[shape + "_s"], g[shape + "_r"]
+    p = og.Points(x, y, r, s)
+    lost, nc = og.clear_inner_layer(p, body, ips, method=0, cutoff_mult=cut, env=env)
+    _clear_check_method0(g[shape + "_m0_x"], g[shape + "_m0_y"], g[shape + "_m0_s"], p.x, p.y, p.s, r)
+    glost = float(g[shape + "_m0_lost"][0])
+    assert abs(lost - glost) < 1e-5 * max(1.0, abs(glost)) and nc > 0
+    p = og.Points(x, y, r, s)
+    lost, nc = og.clear_inner_layer(p, body, ips, method=1, cutoff_mult=cut, env=env)
+    assert lost == 0.0 and nc > 0
+    np.testing.assert_array_equal(p.s, s)
+    assert np.max(np.hypot(p.x - g[shape + "_m1_x"], p.y - g[shape + "_m1_y"])) < 1e-5
+    f = og.Points(x, y)
+    og.clear_inner_layer(f, body, ips, method=1, cutoff_mult=0.0, env=env)
+    assert np.max(np.hypot(f.x - g[shape + "_fld_x"], f.y - g[shape + "_fld_y"])) < 1e-5
+
+
+def test_clear_inner_layer_large_vs_oracle(ctx, restatement):
+    rng = np.random.default_rng(21)
+    body = og.circle_panels(2048)
+    n = 20_000
+    rad = rng.uniform(0.3, 0.6, n)
+    a = rng.uniform(0, 2 * np.pi, n)
+    x, y = (rad * np.cos(a)).astype(np.float32), (rad * np.sin(a)).astype(np.float32)
+    s = rng.normal(0, 1, n).astype(np.float32)
+    r = np.full(n, 0.004, np.float32)
+    ips = 0.004
+    p = og.Points(x, y, r, s)
+    lost, nc = og.clear_inner_layer(p, body, ips, method=0, env=og.ExecEnv(context=ctx))
+    ox, oy, os_, olost, onc = restatement.clear_inner(0, og.CLEAR_CUTOFF, ips, body.nx, body.ny, body.idx,
+                                                      x, y, s, r)
+    _clear_check_method0(ox, oy, os_, p.x, p.y, p.s, r)
+    assert abs(lost - olost) < 1e-4 * max(1.0, abs(olost))
+    # every particle ends at or above the layer's inner edge
+    assert np.min(np.hypot(p.x, p.y)) > 0.5
