@@ -100,4 +100,27 @@ void points_affect_panels(const SrcPoints& src, TargSurfaces& targ, int accum = 
   if (s != OBS_OK) throw std::runtime_error(std::string("obs_points_affect_panels: ") + obs_status_string(s));
 }
 
+// Mirror of clear_inner_panp2<float>(method, src, targ, cutoff_mult, ips) (src/Reflect.h:491-729):
+// crops (method 0) or pushes (method 1) the points inside the body's cutoff layer, in place, and
+// returns the circulation removed, which clear_inner_layer hands to the body's
+// add_to_reabsorbed (:733-760).  Points without radii (field points) take ips as radius.
+template <class SrcSurfaces, class TargPoints>
+float clear_inner_panp2(int method, const SrcSurfaces& src, TargPoints& targ, float cutoff_mult, float ips) {
+  const auto& nx = src.get_pos();
+  const auto& idx = src.get_idx();
+  static_assert(sizeof(idx[0]) == sizeof(unsigned), "panel node indices must be 32-bit");
+  auto& tx = targ.get_pos();
+  auto& ts = targ.get_str();
+  const auto& tr = targ.get_rad();
+  double lost = 0.0;
+  long long ncropped = 0;
+  const int s = obs_clear_inner_layer(context(), method, cutoff_mult, ips, (int)nx[0].size(), nx[0].data(),
+                                      nx[1].data(), (int)src.get_npanels(),
+                                      reinterpret_cast<const unsigned*>(idx.data()), (int)tx[0].size(),
+                                      tx[0].data(), tx[1].data(), ts.empty() ? nullptr : ts.data(),
+                                      tr.empty() ? nullptr : tr.data(), &lost, &ncropped);
+  if (s != OBS_OK) throw std::runtime_error(std::string("obs_clear_inner_layer: ") + obs_status_string(s));
+  return (float)lost;
+}
+
 }  // namespace omega2d_gb300

@@ -1,6 +1,6 @@
 """The header-only C++ adapters (include/omega2d_gb300_influence.hpp) compile against element
-containers shaped like the reference's (src/Points.h, src/Surfaces.h accessors) and link
-against the engine library.  Without a GPU the first call reports the missing device through
+containers shaped like the reference's (src/Points.h, src/Surfaces.h accessors; the non-const
+get_pos / get_str that clear_inner_panp2 writes through) and link against the engine library.  Without a GPU the first call reports the missing device through
 the adapter's exception, which the program prints."""
 import os
 import shutil
@@ -31,8 +31,10 @@ struct Points {
   size_t get_n() const { return x[0].size(); }
   bool is_inert() const { return inert; }
   const std::array<Vector<float>, 2>& get_pos() const { return x; }
+  std::array<Vector<float>, 2>& get_pos() { return x; }
   const Vector<float>& get_rad() const { return r; }
   const Vector<float>& get_str() const { return s; }
+  Vector<float>& get_str() { return s; }
   std::array<Vector<float>, 2>& get_vel() { return u; }
   Vector<float>& get_vort() { return vort; }
   Vector<float>& get_shear() { return shear; }
@@ -63,6 +65,9 @@ int main() {
   b.idx = {0, 1, 1, 2, 2, 0};
   b.vs = {1.f, 1.f, 1.f};
   b.pu = {Vector<float>(3, 0.f), Vector<float>(3, 0.f)};
+  // compiled and linked here; the engine call behind it is tested through the Python binding
+  float (*clear)(int, const Surfaces&, Points&, float, float) = &omega2d_gb300::clear_inner_panp2<Surfaces, Points>;
+  (void)clear;
   try {
     omega2d_gb300::points_affect_points(p, p, OBS_VELONLY);
     omega2d_gb300::panels_affect_points(b, p);
