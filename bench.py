@@ -890,6 +890,19 @@ def run_rows(args):
     rows[-1]["iterations"] = it_box["it"]
     rows[-1]["relative_residual"] = it_box["rel"]
 
+    # clear_inner_layer over the same points and panels: the annulus starts outside the layer,
+    # so each point is tested once against every panel (the usual case in a run)
+    PRc = torch.full((npt,), 0.01, device=dev)
+    PXc, PYc, PSc = P["px"].clone(), P["py"].clone(), P["pg"].clone()
+    rsub = np.full(psub.size, 0.01, np.float32)
+
+    def clr():
+        PXc.copy_(P["px"]); PYc.copy_(P["py"]); PSc.copy_(P["pg"])
+        og.clear_inner_layer_dev(ctx, 0, og.CLEAR_CUTOFF, 0.01, P["nx"], P["ny"], IDX, PXc, PYc, PSc, PRc)
+    row("clear_inner_layer (crop test of every point)", "src/Reflect.h:491-760", clr, float(npan) * npt, None,
+        cpu_rate(lambda: orc.clear_inner(0, og.CLEAR_CUTOFF, 0.01, bd.nx, bd.ny, bd.idx, px[psub], py[psub],
+                                         pg[psub], rsub), npan * float(psub.size)))
+
     # time stepping: one step of each scheme on the 131072-particle patch
     for order, name in ((1, "E3 Euler step"), (2, "E3 Ralston RK2 step"), (3, "E3 RK3 step"), (4, "E3 Heun RK2 step")):
         X2, Y2 = T["x"].clone(), T["y"].clone()

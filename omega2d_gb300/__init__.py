@@ -633,6 +633,19 @@ def clear_inner_layer(pts: Points, body: Surfaces, ips: float, method: int = 0, 
     return circ.value, nc.value
 
 
+def clear_inner_layer_dev(ctx: Context, method: int, cutoff_mult: float, ips: float, nx, ny, idx, x, y, s=None,
+                          r=None) -> tuple[float, int]:
+    """Device-resident clear_inner_layer (CUDA tensors, updated in place); synchronizes and
+    returns (circulation removed, number of modifications)."""
+    circ, nc = ctypes.c_double(), ctypes.c_longlong()
+    _check(lib().obs_clear_inner_layer_dev(ctx.handle, ctypes.c_int(method), ctypes.c_float(cutoff_mult),
+                                           ctypes.c_float(ips), ctypes.c_int(nx.numel()), _ptr(nx), _ptr(ny),
+                                           ctypes.c_int(idx.numel() // 2), _ptr(idx), ctypes.c_int(x.numel()),
+                                           _ptr(x), _ptr(y), _ptr(s), _ptr(r), ctypes.byref(circ), ctypes.byref(nc)),
+           "obs_clear_inner_layer_dev")
+    return circ.value, nc.value
+
+
 # ---------------------------------------------------------------- device-resident panel calls
 # All arrays are CUDA tensors (node coordinates float32, idx int32/uint32 pairs); asynchronous
 # on the context's stream, same semantics as the host calls above.
