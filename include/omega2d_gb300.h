@@ -280,7 +280,8 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
  * r holds the points' core radii (NULL: field points, whose radius is ips).  circ_removed
  * (optional) receives the circulation removed (the body's add_to_reabsorbed), ncropped the
  * number of modifications.  OBS_ERR_NO_CONVERGENCE when a point was still being modified
- * after 64 tests (the others are cleared). */
+ * after 64 tests (the others are cleared).  The _dev form takes device arrays and, unlike the
+ * other _dev calls, synchronizes the context's stream: its two results are host values. */
 int obs_clear_inner_layer(obs_context* ctx, int method, float cutoff_mult, float ips, int nnodes, const float* nx,
                           const float* ny, int npan, const unsigned* idx, int n, float* x, float* y, float* s,
                           const float* r, double* circ_removed, long long* ncropped);
