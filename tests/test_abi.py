@@ -89,3 +89,21 @@ def test_python_constants_mirror_header_defines():
                 assert getattr(og, name) == val, name
                 seen += 1
     assert seen >= 10 and og.TAPE_ALL == -1
+
+
+def test_clear_inner_layer_rejects_bad_arguments_without_a_device(engine_lib):
+    """obs_clear_inner_layer validates before it binds a device: a null context, an unknown
+    method, a non-positive ips and cropping without radii are OBS_ERR_ARG."""
+    f = engine_lib.obs_clear_inner_layer
+    z = np.zeros(4, np.float32)
+    p = z.ctypes.data_as(ctypes.c_void_p)
+    idx = np.array([0, 1, 1, 0], np.uint32).ctypes.data_as(ctypes.c_void_p)
+    C, F = ctypes.c_int, ctypes.c_float
+
+    def call(ctx, method, ips, r):
+        return f(ctx, C(method), F(0.2), F(ips), C(2), p, p, C(2), idx, C(4), p, p, p, r, None, None)
+    assert call(None, 0, 0.02, p) == -1
+    h = ctypes.c_void_p(1)                      # never dereferenced: the checks come first
+    assert call(h, 2, 0.02, p) == -1
+    assert call(h, 1, 0.0, p) == -1
+    assert call(h, 0, 0.02, None) == -1
