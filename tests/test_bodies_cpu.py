@@ -61,3 +61,27 @@ def test_restatement_joined_matrix_vs_block_golden(restatement, golden):
     R = restatement.panels_on_panels_coeff(2, b[0].nx, b[0].ny, b[0].idx, fp64=True, self_block=False,
                                            tnx=b[1].nx, tny=b[1].ny, tidx=b[1].idx)
     assert rel_err(g["A"][72:, :72], R) < 1e-4
+
+
+def test_solve_bem_bodies_splits_strengths_by_body(monkeypatch):
+    """Host logic of solve_bem_bodies: one solve over the joined set, then each body receives its
+    own slice (the solve is replaced by one that writes the joined panel index)."""
+    calls = []
+
+    def fake_solve(vort, joined, fs=(0.0, 0.0), nunk=2, env=None, reuse_matrix=False, direct_lu=False):
+        calls.append((joined.npan, nunk, reuse_matrix, direct_lu))
+        joined.vs = np.arange(joined.npan, dtype=np.float32)
+        if nunk == 2:
+            joined.ss = -np.arange(joined.npan, dtype=np.float32)
+        return 1e-14
+    monkeypatch.setattr(og, "solve_bem", fake_solve)
+    a, b, c = og.circle_panels(10), og.circle_panels(6, 0.3, center=(2.0, 0.0)), og.circle_panels(4, 0.2, (0, 3))
+    vort = og.Points(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0))
+    assert og.solve_bem_bodies(vort, [a, b, c], nunk=2, reuse_matrix=True) == 1e-14
+    assert calls == [(20, 2, True, False)]
+    np.testing.assert_array_equal(a.vs, np.arange(10))
+    np.testing.assert_array_equal(b.vs, np.arange(10, 16))
+    np.testing.assert_array_equal(c.ss, -np.arange(16, 20))
+    og.solve_bem_bodies(vort, [a, b], nunk=1, direct_lu=True)
+    assert calls[-1] == (16, 1, False, True)
+    np.testing.assert_array_equal(b.vs, np.arange(10, 16))
