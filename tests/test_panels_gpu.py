@@ -418,12 +418,13 @@ def test_solve_bem_two_bodies_matches_fp64_restatement(ctx, restatement):
 
 def _clear_check_method0(g_x, g_y, g_s, x, y, s, r):
     """A fully cropped particle lands exactly on the layer and the rounding of that shift
-    decides one further cut (at most 0.12 core radii, strength already 0): positions of such
-    particles are compared within that shift, everything else tightly."""
+    decides whether it is cut again, possibly along another closest panel or node normal: such
+    particles carry no circulation and their positions are compared within half a core radius;
+    everything else tightly."""
     cropped = g_s == 0.0
     d = np.hypot(g_x - x, g_y - y)
     assert np.all(d[~cropped] < 1e-5), np.max(d[~cropped])
-    assert np.all(d[cropped] <= 0.12 * r[cropped] + 1e-6)
+    assert np.all(d[cropped] <= 0.5 * r[cropped])
     assert np.all(s[cropped] == 0.0)
     np.testing.assert_allclose(s, g_s, rtol=1e-5, atol=1e-6)
 
