@@ -36,7 +36,9 @@ def build(force: bool = False) -> str:
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) > max(os.path.getmtime(src), os.path.getmtime(impl))):
         return LIB
-    subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=gnu11",
+    # no contraction into fused multiply-adds, on x86 and aarch64 alike (GCC fuses by default
+    # where the ISA has FMA): every product and sum rounds as written
+    subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
                     src, "-o", LIB, "-lm"], check=True)
     return LIB
 
@@ -237,6 +239,17 @@ class Reference:
         fn(ctypes.c_int(sx.size), _p(sx), _p(sy), _p(sr), _p(ss), ctypes.c_int(nt), _p(tx), _p(ty), _p(tr),
            ctypes.c_int(restype), _p(tu), _p(tv), _p(ex))
         return tu, tv, ex
+
+    def psi(self, sx, sy, sr, ss, tx, ty, tr=None, fp64=False, tp=None):
+        """The reference's streamfunction kernels kernelp_0v_0b / kernelp_0v_0p
+        (src/Kernels.h:52-74) in the velonly driver loop; tr None selects the 0p kernel."""
+        dt = np.float64 if fp64 else np.float32
+        sx, sy, sr, ss, tx, ty, tr = (_arr(a, dt) for a in (sx, sy, sr, ss, tx, ty, tr))
+        out = np.zeros(tx.size, dt) if tp is None else np.array(tp, dtype=dt)
+        fn = self.lib.ref_psi_d if fp64 else self.lib.ref_psi_f
+        fn(ctypes.c_int(sx.size), _p(sx), _p(sy), _p(sr), _p(ss), ctypes.c_int(tx.size), _p(tx), _p(ty), _p(tr),
+           _p(out))
+        return out
 
     def velgrad_thick(self, sx, sy, sr, ss, tx, ty, tr, fp64=False):
         dt = np.float64 if fp64 else np.float32

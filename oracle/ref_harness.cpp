@@ -166,6 +166,41 @@ int ref_velgrad_thick_d(int ns, const double* sx, const double* sy, const double
   return 0;
 }
 
+// kernelp_0v_0b / kernelp_0v_0p (src/Kernels.h:52-74) have no dispatching driver in the
+// reference (points_affect_points asserts psionly off, src/Influence.h:60); this loop mirrors
+// the velonly x86 loop of src/Influence.h:347-363 (0b) and :199-210 (0p) with the
+// streamfunction kernel in its place.  tr == NULL selects the field-point (0p) kernel.
+// tp accumulates (+=) like the velocity.
+}  // extern "C"
+template <class S>
+int psi_loop(int ns, const S* sx, const S* sy, const S* sr, const S* ss,
+             int nt, const S* tx, const S* ty, const S* tr, S* tp) {
+  #pragma omp parallel for
+  for (int i = 0; i < nt; ++i) {
+    double ap = 0;
+    if (tr) {
+      for (int j = 0; j < ns; ++j)
+        kernelp_0v_0b<S, double>(sx[j], sy[j], sr[j], ss[j], tx[i], ty[i], tr[i], &ap);
+    } else {
+      for (int j = 0; j < ns; ++j)
+        kernelp_0v_0p<S, double>(sx[j], sy[j], sr[j], ss[j], tx[i], ty[i], &ap);
+    }
+    tp[i] += ap;
+  }
+  return 0;
+}
+extern "C" {
+
+int ref_psi_f(int ns, const float* sx, const float* sy, const float* sr, const float* ss,
+              int nt, const float* tx, const float* ty, const float* tr, float* tp) {
+  return psi_loop<float>(ns, sx, sy, sr, ss, nt, tx, ty, tr, tp);
+}
+
+int ref_psi_d(int ns, const double* sx, const double* sy, const double* sr, const double* ss,
+              int nt, const double* tx, const double* ty, const double* tr, double* tp) {
+  return psi_loop<double>(ns, sx, sy, sr, ss, nt, tx, ty, tr, tp);
+}
+
 // panels_affect_points (src/Influence.h:422-614): active panels carrying vortex (vs) and
 // source (ss) sheet strengths; the reference always takes the kernelu_1vs_0p branch here
 // because active Surfaces always hold both strength arrays (src/Surfaces.h:86-92, 139-156).

@@ -239,10 +239,50 @@ def make_clear(out):
     np.savez_compressed(out, **d)
 
 
+def make_pins(out):
+    """The streamfunction and the singular core from the reference's own code.
+
+    * psi: kernelp_0v_0b / kernelp_0v_0p (src/Kernels.h:52-74) in the velonly driver loop,
+      thick and field-point targets, accumulated onto non-zero starting values.
+    * singular: the reference has no separate point-vortex core; it is the Rosenhead-Moore core
+      (src/CoreFunc.h:42-82) with zero radii.  libref_rm with sr = tr = 0 on targets that do not
+      coincide with any source gives the point-vortex velocity (and, through kernelug_0v_0b, its
+      gradient); field-point targets use the 0p kernel with sr = 0."""
+    rng = np.random.default_rng(20240608)
+    ns, nt = 301, 187
+    sx, sy, sr, ss = particles(rng, ns)
+    tx, ty, tr, _ = particles(rng, nt)
+    tx[:30], ty[:30], tr[:30] = sx[:30], sy[:30], sr[:30]     # coincident pairs (psi is finite there)
+    tp0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    tu0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    tv0 = rng.normal(0, 0.1, nt).astype(np.float32)
+    ref = po.Reference(po.RM)
+    d = dict(sx=sx, sy=sy, sr=sr, ss=ss, tx=tx, ty=ty, tr=tr, tp0=tp0, tu0=tu0, tv0=tv0)
+    d["psi_b"] = ref.psi(sx, sy, sr, ss, tx, ty, tr, tp=tp0)
+    d["psi_p"] = ref.psi(sx, sy, sr, ss, tx, ty, None, tp=tp0)
+    # singular: off-source targets only (a coincident pair is 0/0 in the reference)
+    qx, qy, _, _ = particles(rng, 211)
+    z = np.zeros(ns, np.float32)
+    zt = np.zeros(qx.size, np.float32)
+    d.update(qx=qx, qy=qy)
+    for thick in (True, False):
+        tu, tv, _ = ref.points_affect_points(po.VELONLY, sx, sy, z, ss, qx, qy, zt if thick else None)
+        d[f"sing_{'b' if thick else 'p'}_u"], d[f"sing_{'b' if thick else 'p'}_v"] = tu, tv
+    g = ref.velgrad_thick(sx, sy, z, ss, qx, qy, zt)
+    for k, nm in enumerate(["u", "v", "ux", "vx", "uy", "vy"]):
+        d[f"sing_grad_{nm}"] = g[k]
+    np.savez_compressed(out, **d)
+
+
 def main():
     if not build_ref.available():
         raise SystemExit("the reference tree is needed to generate golden vectors")
     build_ref.build()
+    if sys.argv[1:]:
+        # named fixtures only, e.g. `make_golden.py pins`
+        for name in sys.argv[1:]:
+            globals()["make_" + name](os.path.join(HERE, name + ".npz"))
+        return
     make_p2p(os.path.join(HERE, "p2p.npz"))
     make_panels(os.path.join(HERE, "panels.npz"))
     make_advect(os.path.join(HERE, "advect.npz"))
@@ -250,6 +290,7 @@ def main():
     make_augment(os.path.join(HERE, "augment.npz"))
     make_bodies(os.path.join(HERE, "bodies.npz"))
     make_clear(os.path.join(HERE, "clear.npz"))
+    make_pins(os.path.join(HERE, "pins.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -204,3 +204,46 @@ def test_restatement_rk3_heun_golden(restatement, golden, order, key, core, fs):
     x, y = restatement.advect(order, core, g["x"], g["y"], g["r"], g["s"], fs, 0.01, 4)
     disp = np.max(np.hypot(g[key + "_x"] - g["x"], g[key + "_y"] - g["y"]))
     assert np.max(np.hypot(x - g[key + "_x"], y - g[key + "_y"])) < 2e-5 * disp
+
+
+@pytest.mark.parametrize("thick", [True, False])
+def test_restatement_streamfunction_golden(restatement, golden, thick):
+    """psionly against the reference's kernelp_0v_0b / kernelp_0v_0p (src/Kernels.h:52-74)."""
+    g = golden("pins")
+    _, _, ex = restatement.points_affect_points(po.V2, po.PSIONLY, g["sx"], g["sy"], g["sr"], g["ss"], g["tx"],
+                                                g["ty"], g["tr"] if thick else None, extra=[g["tp0"]])
+    assert np.isfinite(ex[0]).all()
+    assert rel_err(g["psi_b" if thick else "psi_p"], ex[0]) < TOL_F32
+
+
+@pytest.mark.parametrize("thick", [True, False])
+def test_restatement_singular_golden(restatement, golden, thick):
+    """The singular core against the reference's Rosenhead-Moore core with zero radii
+    (src/CoreFunc.h:42-82) on targets off the sources; the singular core ignores the radii."""
+    g = golden("pins")
+    k = "b" if thick else "p"
+    for sr in (np.zeros_like(g["sr"]), g["sr"]):
+        tu, tv, _ = restatement.points_affect_points(po.SINGULAR, po.VELONLY, g["sx"], g["sy"], sr, g["ss"],
+                                                     g["qx"], g["qy"], np.zeros_like(g["qx"]) if thick else None)
+        assert rel_err(g[f"sing_{k}_u"], tu) < TOL_F32 and rel_err(g[f"sing_{k}_v"], tv) < TOL_F32
+    tu, tv, ex = restatement.points_affect_points(po.SINGULAR, po.VELANDGRAD, g["sx"], g["sy"], g["sr"], g["ss"],
+                                                  g["qx"], g["qy"], g["sr"][:g["qx"].size])
+    for ref, got in zip([g[f"sing_grad_{nm}"] for nm in ("u", "v", "ux", "vx", "uy", "vy")], [tu, tv] + ex):
+        assert rel_err(ref, got) < TOL_F32
+
+
+@pytest.mark.skipif(not po.Reference.available(po.RM), reason="reference tree not built here")
+def test_live_reference_streamfunction_fp64(restatement):
+    """FP64: the restatement's psionly equals the reference's kernelp in double to rounding."""
+    rng = np.random.default_rng(5)
+    sx, sy = rng.uniform(-1, 1, (2, 400))
+    sr = rng.uniform(0.01, 0.1, 400)
+    ss = rng.normal(0, 0.05, 400)
+    tx, ty = rng.uniform(-1.2, 1.2, (2, 150))
+    tr = rng.uniform(0.01, 0.1, 150)
+    ref = po.Reference(po.RM)
+    for thick in (True, False):
+        a = ref.psi(sx, sy, sr, ss, tx, ty, tr if thick else None, fp64=True)
+        _, _, b = restatement.points_affect_points(po.RM, po.PSIONLY, sx, sy, sr, ss, tx, ty,
+                                                   tr if thick else None, fp64=True)
+        assert rel_err(a, b[0]) < 1e-13

@@ -114,6 +114,40 @@ def test_p2p_streamfunction(ctx, restatement, thick, accum):
     np.testing.assert_array_equal(targ.u, u0)   # psionly leaves the velocity untouched
 
 
+@pytest.mark.parametrize("thick", [True, False])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+@pytest.mark.parametrize("core", [og.CORE_V2, og.CORE_GAUSSIAN])
+def test_p2p_streamfunction_matches_reference_golden(ctx, golden, thick, accum, core):
+    """psionly against the reference's kernelp_0v_0b / kernelp_0v_0p (src/Kernels.h:52-74);
+    the kernel is the same for every core (radius term sr^2 + tr^2), 30 coincident pairs."""
+    g = golden("pins")
+    src = og.Points(g["sx"], g["sy"], g["sr"], g["ss"])
+    targ = og.Points(g["tx"], g["ty"], g["tr"] if thick else None, None)
+    targ.psi = g["tp0"].copy()
+    run(ctx, core, og.PSIONLY, accum, src, targ)
+    assert np.isfinite(targ.psi).all()
+    assert rel_err(g["psi_b" if thick else "psi_p"], targ.psi) < TOL[accum]
+
+
+@pytest.mark.parametrize("thick", [True, False])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+def test_p2p_singular_matches_reference_golden(ctx, golden, thick, accum):
+    """The singular core against the reference's Rosenhead-Moore core with zero radii
+    (src/CoreFunc.h:42-82) on targets off the sources; the singular core ignores radii."""
+    g = golden("pins")
+    k = "b" if thick else "p"
+    for sr in (np.zeros_like(g["sr"]), g["sr"]):
+        src = og.Points(g["sx"], g["sy"], sr, g["ss"])
+        targ = og.Points(g["qx"], g["qy"], np.full(g["qx"].size, 0.03, np.float32) if thick else None, None)
+        run(ctx, og.CORE_SINGULAR, og.VELONLY, accum, src, targ)
+        assert rel_err(g[f"sing_{k}_u"], targ.u) < TOL[accum] and rel_err(g[f"sing_{k}_v"], targ.v) < TOL[accum]
+    src = og.Points(g["sx"], g["sy"], g["sr"], g["ss"])
+    targ = og.Points(g["qx"], g["qy"], np.full(g["qx"].size, 0.03, np.float32), None)
+    run(ctx, og.CORE_SINGULAR, og.VELANDGRAD, accum, src, targ)
+    for ref, got in zip([g[f"sing_grad_{nm}"] for nm in ("u", "v", "ux", "vx", "uy", "vy")], [targ.u, targ.v] + targ.grad):
+        assert rel_err(ref, got) < TOL[accum]
+
+
 SIZES = [0, 1, 2, 31, 33, 255, 257, 1031]
 
 
