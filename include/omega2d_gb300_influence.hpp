@@ -7,6 +7,7 @@
 // src/Points.h:116-117) -- so the reference's Points<float> work unchanged.
 #pragma once
 
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 
@@ -27,6 +28,15 @@ inline int compiled_core() {
 #else
   return OBS_CORE_V2;
 #endif
+}
+
+// The engine takes straight panels: two node indices per panel.  The reference also allows
+// more nodes per element (src/Reflect.h:512 reads idx[nper*j]); such surfaces are rejected
+// here rather than read with the wrong stride.
+template <class Surf>
+inline void require_two_nodes_per_panel(const Surf& s, const char* who) {
+  if (s.get_idx().size() != 2 * (size_t)s.get_npanels())
+    throw std::runtime_error(std::string(who) + ": the engine takes two node indices per panel");
 }
 
 // One context per process and device, created on first use.
@@ -70,6 +80,7 @@ float points_affect_points(const SrcPoints& src, TargPoints& targ, int result,
 // get_src_str() (src/Surfaces.h:231-252).
 template <class SrcSurfaces, class TargPoints>
 void panels_affect_points(const SrcSurfaces& src, TargPoints& targ, int accum = OBS_COMPENSATED) {
+  require_two_nodes_per_panel(src, "panels_affect_points");
   const auto& nx = src.get_pos();
   const auto& idx = src.get_idx();
   static_assert(sizeof(idx[0]) == sizeof(unsigned), "panel node indices must be 32-bit");
@@ -88,6 +99,7 @@ void panels_affect_points(const SrcSurfaces& src, TargPoints& targ, int accum = 
 // panel (the BEM right-hand-side input; the points' core radii are ignored, as there).
 template <class SrcPoints, class TargSurfaces>
 void points_affect_panels(const SrcPoints& src, TargSurfaces& targ, int accum = OBS_COMPENSATED) {
+  require_two_nodes_per_panel(targ, "points_affect_panels");
   const auto& sx = src.get_pos();
   const auto& nx = targ.get_pos();
   const auto& idx = targ.get_idx();
@@ -104,8 +116,12 @@ void points_affect_panels(const SrcPoints& src, TargSurfaces& targ, int accum = 
 // crops (method 0) or pushes (method 1) the points inside the body's cutoff layer, in place, and
 // returns the circulation removed, which clear_inner_layer hands to the body's
 // add_to_reabsorbed (:733-760).  Points without radii (field points) take ips as radius.
+// When a point still lies inside the layer after the engine's sweep limit, the points are
+// updated as far as they went and the circulation removed is returned with a warning on
+// stderr, so the caller's circulation bookkeeping stays whole.
 template <class SrcSurfaces, class TargPoints>
 float clear_inner_panp2(int method, const SrcSurfaces& src, TargPoints& targ, float cutoff_mult, float ips) {
+  require_two_nodes_per_panel(src, "clear_inner_panp2");
   const auto& nx = src.get_pos();
   const auto& idx = src.get_idx();
   static_assert(sizeof(idx[0]) == sizeof(unsigned), "panel node indices must be 32-bit");
@@ -119,6 +135,13 @@ float clear_inner_panp2(int method, const SrcSurfaces& src, TargPoints& targ, fl
                                       reinterpret_cast<const unsigned*>(idx.data()), (int)tx[0].size(),
                                       tx[0].data(), tx[1].data(), ts.empty() ? nullptr : ts.data(),
                                       tr.empty() ? nullptr : tr.data(), &lost, &ncropped);
+  if (s == OBS_ERR_NO_CONVERGENCE) {
+    // the sweep limit ran out for some points: positions, strengths and the circulation
+    // removed are written all the same, so hand the circulation back for add_to_reabsorbed
+    std::fprintf(stderr, "omega2d_gb300::clear_inner_panp2: %s; the circulation removed is returned\n",
+                 obs_status_string(s));
+    return (float)lost;
+  }
   if (s != OBS_OK) throw std::runtime_error(std::string("obs_clear_inner_layer: ") + obs_status_string(s));
   return (float)lost;
 }
