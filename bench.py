@@ -26,6 +26,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -181,7 +182,10 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        # samples go to a temporary file, or to $OBS_CLOCKS_DIR when the caller wants to keep them
+        keep = os.environ.get("OBS_CLOCKS_DIR")
+        self.path = (os.path.join(keep, f"clocks_gpu{gpu_index}.csv") if keep else
+                     os.path.join(tempfile.gettempdir(), f"omega2d_clocks_{os.getpid()}_gpu{gpu_index}.csv"))
 
     def __enter__(self):
         try:
@@ -451,6 +455,11 @@ def run_engine(args):
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if not args.no_configs:
+        # the other configurations, each with its own timings, precision and CPU baseline
+        line["euler20k"] = run_euler20k(args)
+        line["bem2048"] = run_bem2048(args)
+        line["rk2adjoint"] = run_rk2adjoint2M(args, K=args.line_rk_steps, every=8)
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -500,7 +509,8 @@ def _event_time(torch, stream, flush, fn, steps, warmup, prep=None):
 
 def run_euler20k(args):
     """20,000 vortex blobs U[-1,1]^2, G ~ N(0, 1/N), core 0.01, Rosenhead-Moore, freestream
-    (1, 0): one velocity evaluation, then 10 first-order Euler steps with dt = 0.01."""
+    (1, 0): one velocity evaluation, then 10 first-order Euler steps with dt = 0.01.  Returns
+    the result object."""
     torch, og, dev, ctx, stream, flush = _engine_setup()
     n, K, dt, fs = 20_000, 10, 0.01, (1.0, 0.0)
     rng = np.random.default_rng(1)
@@ -549,14 +559,14 @@ def run_euler20k(args):
     tc = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": K * n * n / tc / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                            "sample": "the full workload (10 Euler steps of 20k particles)"}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_bem2048(args):
     """Unit-diameter circle of 2048 panels and 200,000 particles uniform in the annulus
     0.55 < r < 3 (G ~ N(0, 1e-4)): particles-on-panels (RHS), the 4096 x 4096 panels-on-panels
     matrix in FP64, its FP64 GMRES solve (the FP64 LU timed beside it), and panels-on-particles
-    velocity, all on the device."""
+    velocity, all on the device.  Returns the result object."""
     torch, og, dev, ctx, stream, flush = _engine_setup()
     npan, npart = 2048, 200_000
     rng = np.random.default_rng(3)
@@ -673,19 +683,13 @@ def run_bem2048(args):
                            "points_affect_panels_ginter_s": npart * npan / t_d3 / 1e9,
                            "panels_on_panels_coeff_ms": 1e3 * t_b1,
                            "sample": "FP64 restatement of the full particles-on-panels sum and matrix"}
-    print(json.dumps(out), flush=True)
+    return out
 
 
-def run_rk2adjoint2M(args):
-    """Two co-rotating Gaussian patches of 1M particles each (sigma 0.1, centres (+-0.3, 0),
-    total circulation 1 each), core 0.004, Gaussian; `--rk-steps` Ralston RK2 steps with
-    dt = 0.005; loss L = |X_A - X_B|^2 with X_P = sum_P G^2 x / sum_P G^2; gradient of L with
-    respect to the initial strengths through the trajectory, checkpoints every 8 steps
-    (`--checkpoint-every -1`: every step's positions and stage positions kept in HBM, so the
-    backward recomputes nothing)."""
-    torch, og, dev, ctx, stream, flush = _engine_setup()
-    n, K, dt, every = 2_000_000, args.rk_steps, 0.005, args.checkpoint_every
-    rng = np.random.default_rng(5)
+def two_patches(n, seed=5):
+    """Two co-rotating Gaussian patches (sigma 0.1, centres (+-0.3, 0), total circulation 1
+    each; particles alternate between the patches), core 0.004."""
+    rng = np.random.default_rng(seed)
     lab = (np.arange(n) % 2).astype(np.int64)
     cx = np.where(lab == 0, -0.3, 0.3)
     x = cx + rng.normal(0.0, 0.1, n)
@@ -693,62 +697,118 @@ def run_rk2adjoint2M(args):
     w = np.exp(-((x - cx) ** 2 + y ** 2) / (2 * 0.1 ** 2))
     s = np.where(lab == 0, w / w[lab == 0].sum(), w / w[lab == 1].sum())
     x, y, s = x.astype(np.float32), y.astype(np.float32), s.astype(np.float32)
-    r = np.full(n, 0.004, np.float32)
-    X0, Y0, R, S = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
-    X, Y = X0.clone(), Y0.clone()
-    GS, GX, GY = [torch.zeros(n, device=dev) for _ in range(3)]
-    acc = og.COMPENSATED
+    return x, y, np.full(n, 0.004, np.float32), s, lab
+
+
+def centroid_loss_seed(xT, yT, s, lab):
+    """L = |X_A - X_B|^2 with X_P = sum_P G^2 x / sum_P G^2, in FP64 on the host; returns L,
+    dL/d(final x), dL/d(final y) and the direct part of dL/dG (through the weights)."""
+    n = xT.size
+    s64 = s.astype(np.float64)
+    gxT, gyT, gs_direct = np.zeros(n), np.zeros(n), np.zeros(n)
+    cen = []
+    for P in (0, 1):
+        m = lab == P
+        w2 = s64[m] ** 2
+        cen.append((np.sum(w2 * xT[m]) / w2.sum(), np.sum(w2 * yT[m]) / w2.sum(), w2.sum()))
+    dX, dY = cen[0][0] - cen[1][0], cen[0][1] - cen[1][1]
+    for P, sg in ((0, 1.0), (1, -1.0)):
+        m = lab == P
+        W = cen[P][2]
+        gxT[m] = sg * 2 * dX * s64[m] ** 2 / W
+        gyT[m] = sg * 2 * dY * s64[m] ** 2 / W
+        gs_direct[m] = sg * 2 * (dX * (xT[m] - cen[P][0]) + dY * (yT[m] - cen[P][1])) * 2 * s64[m] / W
+    return dX * dX + dY * dY, gxT, gyT, gs_direct
+
+
+def rk2_adjoint(og, torch, dev, ctx, stream, x, y, r, s, lab, K, every, dt=0.005):
+    """Forward: K Ralston RK2 steps recording checkpoints every `every` steps; backward: the
+    gradient of the centroid loss with respect to the initial strengths through the trajectory
+    from those checkpoints.  CUDA events on the launching stream; returns (forward ms, backward
+    ms, L, dL/dG, engine buffer bytes)."""
+    X, Y, R, S = [torch.from_numpy(a).to(dev) for a in (x, y, r, s)]
+    GS = torch.zeros(x.size, device=dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    og.advect_record_dev(ctx, og.CORE_GAUSSIAN, og.COMPENSATED, 2, X, Y, R, S, (0.0, 0.0), dt, K, every)
+    e[1].record(stream)
+    e[1].synchronize()
+    # loss and its seed on the host in FP64 (the loss is not part of the engine)
+    L, gxT, gyT, gs_direct = centroid_loss_seed(X.cpu().numpy().astype(np.float64),
+                                                Y.cpu().numpy().astype(np.float64), s, lab)
+    LX = torch.from_numpy(gxT.astype(np.float32)).to(dev)
+    LY = torch.from_numpy(gyT.astype(np.float32)).to(dev)
+    torch.cuda.synchronize()
+    e[2].record(stream)
+    peak = og.advect_vjp_tape_dev(ctx, LX, LY, GS, None, None)
+    e[3].record(stream)
+    e[3].synchronize()
+    ctx.synchronize()
+    gs = GS.cpu().numpy().astype(np.float64) + gs_direct
+    return e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3]), L, gs, peak
+
+
+def run_rk2adjoint2M(args, K=None, every=None):
+    """Two co-rotating Gaussian patches of 1M particles each (sigma 0.1, centres (+-0.3, 0),
+    total circulation 1 each), core 0.004, Gaussian; K Ralston RK2 steps with dt = 0.005; loss
+    L = |X_A - X_B|^2 with X_P = sum_P G^2 x / sum_P G^2; gradient of L with respect to the
+    initial strengths through the trajectory, checkpoints every 8 steps (`every` -1: every
+    step's positions and stage positions kept in HBM, so the backward recomputes nothing).
+    Beside it: the same engine path on a 4096-particle draw of the same patches against the FP64
+    oracle's trajectory gradient, and the CPU port's velocity sum and FP64 self-VJP.  Returns
+    the result object."""
+    torch, og, dev, ctx, stream, flush = _engine_setup()
+    n, dt = 2_000_000, 0.005
+    K = args.rk_steps if K is None else K
+    every = args.checkpoint_every if every is None else every
+    x, y, r, s, lab = two_patches(n)
     torch.cuda.reset_peak_memory_stats(dev)
     with ClockSampler(0) as clk:
-        og.advect_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, 1)    # warm-up
-        X.copy_(X0)
-        Y.copy_(Y0)
-        torch.cuda.synchronize()
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        e[0].record(stream)
-        # the forward op records its checkpoints for the backward op
-        og.advect_record_dev(ctx, og.CORE_GAUSSIAN, acc, 2, X, Y, R, S, (0.0, 0.0), dt, K, every)
-        e[1].record(stream)
-        e[1].synchronize()
-        # loss and its seed on the host in FP64 (the loss is not part of the engine)
-        xT, yT, s64 = X.cpu().numpy().astype(np.float64), Y.cpu().numpy().astype(np.float64), s.astype(np.float64)
-        gxT, gyT, gs_direct = np.zeros(n), np.zeros(n), np.zeros(n)
-        cen = []
-        for P in (0, 1):
-            m = lab == P
-            w2 = s64[m] ** 2
-            cen.append((np.sum(w2 * xT[m]) / w2.sum(), np.sum(w2 * yT[m]) / w2.sum(), w2.sum()))
-        dX, dY = cen[0][0] - cen[1][0], cen[0][1] - cen[1][1]
-        L = dX * dX + dY * dY
-        for P, sg in ((0, 1.0), (1, -1.0)):
-            m = lab == P
-            W = cen[P][2]
-            gxT[m] = sg * 2 * dX * s64[m] ** 2 / W
-            gyT[m] = sg * 2 * dY * s64[m] ** 2 / W
-            gs_direct[m] = sg * 2 * (dX * (xT[m] - cen[P][0]) + dY * (yT[m] - cen[P][1])) * 2 * s64[m] / W
-        LX = torch.from_numpy(gxT.astype(np.float32)).to(dev)
-        LY = torch.from_numpy(gyT.astype(np.float32)).to(dev)
-        torch.cuda.synchronize()
-        e[2].record(stream)
-        peak = og.advect_vjp_tape_dev(ctx, LX, LY, GS, GX, GY)
-        e[3].record(stream)
-        e[3].synchronize()
-    ctx.synchronize()
-    f_ms, b_ms = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+        rk2_adjoint(og, torch, dev, ctx, stream, x, y, r, s, lab, 1, every, dt)      # warm-up
+        f_ms, b_ms, L, gs, peak = rk2_adjoint(og, torch, dev, ctx, stream, x, y, r, s, lab, K, every, dt)
+    clocks = clk.summary()
     evals = 2.0 * K * float(n) * float(n)
-    gs = GS.cpu().numpy().astype(np.float64) + gs_direct
+    nck = 1 if every == og.TAPE_ALL else -(-K // max(1, every))
+    recomputed = 0 if every == og.TAPE_ALL else (nck - 1) * (2 * min(every, K) - 1)
     out = {"workload": "rk2adjoint2M", "metric": "Ginteractions/s forward and adjoint, 2M particles, RK2",
            "unit": UNIT, "data": "synthetic (seed 5)", "n": n, "rk2_steps": K, "dt": dt, "checkpoint_every": every,
            "forward_ms": f_ms, "forward_ginter_s": evals / (f_ms * 1e-3) / 1e9,
-           "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
-           "adjoint_note": ("from the full tape: no recomputed velocity sum, " if every == og.TAPE_ALL else
-                            "from the recorded checkpoints: recomputes each segment (about 2K velocity sums) and ") +
-                           "runs 2K self-interaction VJP gathers",
+           "adjoint_ms": b_ms, "adjoint_ginter_s": evals / (b_ms * 1e-3) / 1e9, "adjoint_over_forward": b_ms / f_ms,
+           "adjoint_work": {"self_vjp_gathers": 2 * K, "recomputed_velocity_sums": recomputed,
+                            "forward_velocity_sums": 2 * K,
+                            "note": "the recorded forward keeps the last segment's stage positions; every other "
+                                    "segment is recomputed from its checkpoint (its last step needs one sum)"},
            "value": evals / (f_ms * 1e-3) / 1e9, "loss": L, "grad_strength_norm": float(np.linalg.norm(gs)),
            "grad_strength_finite": bool(np.isfinite(gs).all()),
            "peak_hbm_bytes": {"engine": int(peak), "caller_tensors": int(torch.cuda.max_memory_allocated(dev))},
-           "clocks": clk.summary()}
-    print(json.dumps(out), flush=True)
+           "clocks": clocks}
+    # precision: the same engine path on a 4096-particle draw of the patches vs the FP64 oracle
+    from oracle import pyoracle as po
+    orc = po.Restatement()
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    m = 4096
+    xs, ys, rs, ss, ls = two_patches(m, seed=55)
+    _, _, Ls, gss, _ = rk2_adjoint(og, torch, dev, ctx, stream, xs, ys, rs, ss, ls, K, every, dt)
+    Lr, gs_ref, _, _ = orc.rk2_centroid_grad(po.GAUSS, xs, ys, rs, ss, ls, (0.0, 0.0), dt, K)
+    mx, rms = rel_errs(gs_ref, gss)
+    out["precision"] = {"sample": f"{m} particles of the same two patches, {K} steps, checkpoints every {every}",
+                        "loss_rel": abs(Ls - Lr) / abs(Lr), "dL/dG_max_rel": mx, "dL/dG_rms_rel": rms}
+    # CPU: the port's velocity sum on a target sample of the 2M set, the FP64 self VJP on 4096
+    sub = np.random.default_rng(97).choice(n, 512, replace=False)
+    t0 = time.perf_counter()
+    orc.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, x[sub], y[sub], r[sub])
+    tf = time.perf_counter() - t0
+    lu, lv = np.random.default_rng(98).normal(size=(2, m))
+    t0 = time.perf_counter()
+    orc.self_vjp(po.GAUSS, xs, ys, rs, ss, lu, lv)
+    tb = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": 512.0 * n / tf / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": f"velocity sum, 512 seeded targets x {n} sources (float pairs, double sums)",
+                           "adjoint_value": float(m) * m / tb / 1e9,
+                           "adjoint_sample": f"FP64 self-interaction VJP of {m} particles"}
+    return out
 
 
 def run_rows(args):
@@ -948,7 +1008,11 @@ def main():
     ap.add_argument("--n", type=int, default=N, help="particles (the headline workload is 1,000,000)")
     ap.add_argument("--workload", default="patch1M", choices=["patch1M", "euler20k", "bem2048", "rk2adjoint2M", "rows"],
                     help="patch1M is the headline line; the others measure the remaining configurations")
-    ap.add_argument("--rk-steps", type=int, default=64, help="RK2 steps of rk2adjoint2M")
+    ap.add_argument("--rk-steps", type=int, default=64, help="RK2 steps of --workload rk2adjoint2M")
+    ap.add_argument("--line-rk-steps", type=int, default=16,
+                    help="RK2 steps of the rk2adjoint object in the default line (two checkpoint segments)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="the headline line only, without the euler20k, bem2048 and rk2adjoint objects")
     ap.add_argument("--checkpoint-every", type=int, default=8,
                     help="rk2adjoint2M checkpoint interval; -1 keeps the whole trajectory (no recompute)")
     args = ap.parse_args()
@@ -956,11 +1020,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "euler20k":
-        run_euler20k(args)
+        print(json.dumps(run_euler20k(args)), flush=True)
     elif args.workload == "bem2048":
-        run_bem2048(args)
+        print(json.dumps(run_bem2048(args)), flush=True)
     elif args.workload == "rk2adjoint2M":
-        run_rk2adjoint2M(args)
+        print(json.dumps(run_rk2adjoint2M(args)), flush=True)
     elif args.workload == "rows":
         run_rows(args)
     else:

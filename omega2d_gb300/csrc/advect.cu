@@ -16,7 +16,9 @@
 // Positions are recomputed per segment from checkpoints taken every `every` steps (sqrt(K) by
 // default), so the tape holds K/every checkpoints plus one segment of stage positions.  The
 // checkpoints can come from a recorded forward (obs_advect_record_dev), which the backward then
-// reuses without running the forward sweep again.  every = OBS_TAPE_ALL keeps every step's
+// reuses without running the forward sweep again; the recorded forward also keeps the last
+// segment's positions and stage positions, which the backward reads first, so it recomputes
+// every segment but that one.  every = OBS_TAPE_ALL keeps every step's
 // position and stage positions instead (K*S*2N floats: 2 GB for 2M particles, 64 RK2 steps),
 // and the backward then runs the VJP gathers alone, with no recomputed velocity sum.
 #include <algorithm>
@@ -162,8 +164,12 @@ int record(obs_context* ctx, int core, int accum, int order, int n, const float*
   const int C = full ? 1 : check_every(every, nsteps);
   const int nck = (nsteps + C - 1) / C;
   const size_t slot = (full ? (size_t)sc.S : 1) * 2 * N;   // floats per checkpoint
+  // after the checkpoints: the last segment's x_k and stage positions, in the backward's
+  // segment layout (S*2N floats per step), so the backward need not recompute that segment
+  const int klast = (nck - 1) * C;
+  const size_t lastf = full ? 0 : (size_t)(nsteps - klast) * sc.S * 2 * N;
   ctx->tape_info.valid = false;
-  int st = ctx->tape.ensure(((size_t)2 * N + (size_t)nck * slot) * 4 + 1024, ctx->stream);
+  int st = ctx->tape.ensure(((size_t)2 * N + (size_t)nck * slot + lastf) * 4 + 1024, ctx->stream);
   if (st) return st;
   // state: vel 2SN | working positions 2N | stage positions (S-1)*2N (sized once, before any copy)
   if ((st = ctx->state.ensure(((size_t)2 * sc.S * N + 2 * N + (size_t)(sc.S - 1) * 2 * N) * 4 + 1024, ctx->stream)))
@@ -180,15 +186,23 @@ int record(obs_context* ctx, int core, int accum, int order, int n, const float*
   };
   if ((st = copy(tr, r, N)) || (st = copy(ts, s, N)) || (st = copy(w, x0, N)) || (st = copy(w + N, y0, N))) return st;
   Step p{ctx, core, accum, n, sc, tr, ts, fsx, fsy, dt};
+  float* lastseg = ck + (size_t)nck * slot;
   for (int k = 0; k < nsteps; ++k) {
     float* sl = ck + (size_t)(k / C) * slot;
     if (k % C == 0 && (st = copy(sl, w, 2 * N))) return st;
-    // full tape: the stage positions land in the step's slot, after x_k
-    if ((st = step(p, w, w, vel, full ? sl + 2 * N : stages, true))) return st;
+    float* stg = stages;
+    if (full) {
+      stg = sl + 2 * N;                      // full tape: the stage positions follow x_k in its slot
+    } else if (k >= klast) {
+      float* xk = lastseg + (size_t)(k - klast) * sc.S * 2 * N;
+      if ((st = copy(xk, w, 2 * N))) return st;
+      stg = xk + 2 * N;
+    }
+    if ((st = step(p, w, w, vel, stg, true))) return st;
   }
   if (xf && (st = copy(xf, w, N))) return st;
   if (yf && (st = copy(yf, w + N, N))) return st;
-  ctx->tape_info = AdvectTape{true, core, accum, order, n, nsteps, C, nck, fsx, fsy, dt, full};
+  ctx->tape_info = AdvectTape{true, core, accum, order, n, nsteps, C, nck, fsx, fsy, dt, full, !full};
   return OBS_OK;
 }
 
@@ -255,15 +269,20 @@ int reverse(obs_context* ctx, const float* lx_in, const float* ly_in, float* gs,
   } else {
     for (int sg = t.nck - 1; sg >= 0; --sg) {
       const int k0 = sg * C, k1 = std::min(k0 + C, t.nsteps);
-      // recompute the segment's positions (x_k and its stage positions) from the checkpoint
-      if ((st = copy(seg, ck + (size_t)sg * 2 * N, 2 * N))) return st;
-      for (int k = k0; k < k1; ++k) {
-        float* xk = seg + (size_t)(k - k0) * S * 2 * N;
-        float* next = (k + 1 < k1) ? seg + (size_t)(k + 1 - k0) * S * 2 * N : nullptr;
-        if ((st = step(p, xk, next ? next : xk, vel, xk + 2 * N, next != nullptr))) return st;
+      const float* sp = seg;
+      if (sg == t.nck - 1 && t.last_seg) {
+        sp = ck + (size_t)t.nck * 2 * N;     // kept by the recorded forward
+      } else {
+        // recompute the segment's positions (x_k and its stage positions) from the checkpoint
+        if ((st = copy(seg, ck + (size_t)sg * 2 * N, 2 * N))) return st;
+        for (int k = k0; k < k1; ++k) {
+          float* xk = seg + (size_t)(k - k0) * S * 2 * N;
+          float* next = (k + 1 < k1) ? seg + (size_t)(k + 1 - k0) * S * 2 * N : nullptr;
+          if ((st = step(p, xk, next ? next : xk, vel, xk + 2 * N, next != nullptr))) return st;
+        }
       }
       for (int k = k1 - 1; k >= k0; --k)
-        if ((st = vjp_step(seg + (size_t)(k - k0) * S * 2 * N))) return st;
+        if ((st = vjp_step(sp + (size_t)(k - k0) * S * 2 * N))) return st;
     }
   }
   if (gx0) { add_kernel<<<grid_of(n), 256, 0, strm>>>(n, gx0, lam); ctx->launches++; }

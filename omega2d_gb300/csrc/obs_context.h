@@ -36,6 +36,7 @@ struct AdvectTape {
   int core = 0, accum = 0, order = 0, n = 0, nsteps = 0, every = 0, nck = 0;
   double fsx = 0.0, fsy = 0.0, dt = 0.0;
   bool full = false;   // every step's positions and stage positions kept (OBS_TAPE_ALL)
+  bool last_seg = false;   // the last segment's positions and stage positions kept after the checkpoints
 };
 
 struct Timing {

@@ -24,8 +24,10 @@ import sys
 import tempfile
 from concurrent.futures import ThreadPoolExecutor
 
-REF_ROOT = os.environ.get("OMEGA2D_REFERENCE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout: $OMEGA2D_REFERENCE, else a directory named `reference` beside this
+# repository's checkout
+REF_ROOT = os.environ.get("OMEGA2D_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 OUT = os.path.join(HERE, "_ref")
 
 # core id -> macro in src/CoreFunc.h
