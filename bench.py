@@ -263,7 +263,7 @@ def cpu_sample(kind_pref, x, y, r, s, sample, threads):
         t0 = time.perf_counter()
         ref.points_affect_points(po.VELONLY, x, y, r, s, tx, ty, tr)
         return time.perf_counter() - t0, "reference"
-    orc = po.Restatement()
+    orc = po.Restatement(native=True)
     t0 = time.perf_counter()
     orc.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, tx, ty, tr)
     return time.perf_counter() - t0, "port"
@@ -554,8 +554,9 @@ def run_euler20k(args):
         out[name]["position_error_max_over_displacement"] = float(ex.max() / disp)
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    nat = po.Restatement(native=True)
     t0 = time.perf_counter()
-    orc.advect(1, po.RM, x, y, r, s, fs, dt, K)
+    nat.advect(1, po.RM, x, y, r, s, fs, dt, K)
     tc = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": K * n * n / tc / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                            "sample": "the full workload (10 Euler steps of 20k particles)"}
@@ -797,8 +798,9 @@ def run_rk2adjoint2M(args, K=None, every=None):
                         "loss_rel": abs(Ls - Lr) / abs(Lr), "dL/dG_max_rel": mx, "dL/dG_rms_rel": rms}
     # CPU: the port's velocity sum on a target sample of the 2M set, the FP64 self VJP on 4096
     sub = np.random.default_rng(97).choice(n, 512, replace=False)
+    nat = po.Restatement(native=True)
     t0 = time.perf_counter()
-    orc.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, x[sub], y[sub], r[sub])
+    nat.points_affect_points(po.GAUSS, po.VELONLY, x, y, r, s, x[sub], y[sub], r[sub])
     tf = time.perf_counter() - t0
     lu, lv = np.random.default_rng(98).normal(size=(2, m))
     t0 = time.perf_counter()
@@ -818,7 +820,7 @@ def run_rows(args):
     C restatement (float pairs, double sums, all host cores) on a target sample beside it."""
     torch, og, dev, ctx, stream, flush = _engine_setup()
     from oracle import pyoracle as po
-    orc = po.Restatement()
+    orc = po.Restatement(native=True)          # timed only: the Release-flag build
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
     peaks = measured_peaks()

@@ -24,6 +24,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-
 # Extra flags, e.g. OBS_NVCC_EXTRA=-DOBS_DEVICE_CHECKS for a bounds-checked debug build
 # (build into a separate tree with OBS_BUILD_DIR / OBS_LIB to keep the release library).
 NVCC_FLAGS += os.environ.get("OBS_NVCC_EXTRA", "").split()
+# per-file flags: clear_inner_layer follows the reference's float arithmetic operation by
+# operation, so its products and sums are not fused (the oracle is built the same way)
+# (device code: -fmad=false; host code, the cut table: -ffp-contract=off, which matters where the
+# host ISA has FMA, e.g. aarch64)
+FILE_FLAGS = {"clear_inner.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 BUILD = os.environ.get("OBS_BUILD_DIR", BUILD)
 LIB = os.environ.get("OBS_LIB", LIB)
 
@@ -48,7 +53,8 @@ def _compile(src: str, newest_header: float, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_header):
         return obj
-    cmd = [nvcc()] + NVCC_FLAGS + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
+    cmd = ([nvcc()] + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + (["-Xptxas", "-v"] if verbose else [])
+           + ["-c", src, "-o", obj])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")

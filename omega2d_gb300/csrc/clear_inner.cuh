@@ -9,7 +9,9 @@
 //
 // Float semantics follow the reference's float build: std::pow(S, 2) and the 1.0 literals
 // promote to double, so those sub-expressions are formed in double and rounded to float where
-// the reference stores them.  Its closest-panel tests `d < nextafter(min, 0.0)` (a double
+// the reference stores them.  Every build of this file forms each product and sum separately
+// (no fused multiply-add: nvcc -fmad=false, host -ffp-contract=off), which is how the oracle is
+// built too, so the engine and the oracle agree bit for bit.  Its closest-panel tests `d < nextafter(min, 0.0)` (a double
 // nextafter: strictly below) and `d < nextafterf(min, FLT_MAX)` (at most equal) are, for float
 // d, "new closest if d < min" and "tie if d == min".
 #pragma once
@@ -141,61 +143,140 @@ OBS_HD void cut_entry(const Geo& g, float p, float& smult, float& dshift) {
   }
 }
 
-// One point, tested until it passes (at most max_sweeps times).  rad = the point's core radius
-// (ips for field points).  Returns the number of modifications, or -1 when max_sweeps ran out;
-// lost receives the circulation removed (method 0).
+// A lower bound, in FP32, on the squared distance seg_closest computes for one panel (its
+// exact float/double arithmetic).  The differences ax, ay, bx, by, the cross product c and the
+// dot product are formed exactly as seg_closest forms them, so they are the same floats; only
+// t = dot/blensq is taken as dot * ibl (ibl = 1/blensq in FP32, within a few ulps).  Where t is
+// at least 2^-20 inside (0, 1), seg_closest takes the panel case, c^2/blensq; where it is at
+// least 2^-20 outside, the node case, min(ax^2 + ay^2, ex^2 + ey^2) -- either way the FP32 value
+// is within a few ulps of seg_closest's double-then-float one, and (1 - 2^-20) times it bounds
+// that from below.  In the 2^-20 band around 0 and 1 the bound is the smaller of the two cases
+// (seg_closest's value is one of them).  Non-finite inputs give NaN or inf, which never reject.
+OBS_HD float seg_lower_bound(float x0, float y0, float x1, float y1, float ibl, float tx, float ty) {
+  const float bx = x1 - x0, by = y1 - y0;
+  const float ax = tx - x0, ay = ty - y0;
+  const float t = (ax * bx + ay * by) * ibl;
+  const float c = ay * bx - ax * by;
+  const float dp = (c * c) * ibl;
+  const float ex = tx - x1, ey = ty - y1;
+  const float dn = fminf(ax * ax + ay * ay, ex * ex + ey * ey);
+  const float eps = 9.5367431640625e-7f;          // 2^-20
+  const bool inside = t > eps && t < 1.0f - eps;
+  const bool outside = t < -eps || t > 1.0f + eps;
+  const float d = inside ? dp : (outside ? dn : fminf(dp, dn));
+  return d * 0.99999904632568359375f;
+}
+
+// bound > T (1 + 2^-16): the panel cannot be the closest or tie it when T bounds the minimum
+OBS_HD bool beyond(float bound, float T) { return bound > T * 1.0000152587890625f && bound <= 3.0e38f; }
+
+// the closest panels or nodes of one point (ties kept), as clear_inner_panp2's hits
+// (src/Reflect.h:560-604), reduced to the sums its normal and closest-point averages need
+struct Closest {
+  float mind, snx, sny, scx, scy;
+  int cnt;
+};
+
+OBS_HD void closest_init(Closest& c) {
+  c.mind = (float)(0.1 * 3.4028234663852886e38);
+  c.snx = c.sny = c.scx = c.scy = 0.0f;
+  c.cnt = 0;
+}
+
+// panel j (nodes a -> b at (x0, y0) -> (x1, y1), normal (pnx, pny)) against the point (tx, ty)
+OBS_HD void closest_add(const Geo& g, Closest& c, unsigned a, unsigned b, float x0, float y0, float x1, float y1,
+                        float pnx, float pny, float tx, float ty) {
+  float d2, cx, cy;
+  int kind, which;
+  seg_closest(x0, y0, x1, y1, tx, ty, d2, cx, cy, kind, which);
+  if (d2 < c.mind) {                         // a new closest panel or node
+    c.mind = d2;
+    c.snx = c.sny = c.scx = c.scy = 0.0f;
+    c.cnt = 0;
+  } else if (!(d2 == c.mind)) {
+    return;
+  }
+  if (kind == 0) {
+    c.snx += pnx;
+    c.sny += pny;
+  } else {
+    const unsigned nd = which ? b : a;
+    c.snx += g.nnx[nd];
+    c.sny += g.nny[nd];
+  }
+  c.scx += cx;
+  c.scy += cy;
+  ++c.cnt;
+}
+
+// The test after one sweep (src/Reflect.h:606-700): crop (method 0) or push (method 1) the point
+// when it lies inside the layer.  Returns 0 when the point passes (done), 1 when it was
+// modified (test it again), 2 when no panel was found.
+OBS_HD int clear_apply(const Geo& g, const Closest& c, int method, float cutoff_mult, float ips, float rad, float& x,
+                       float& y, float& s, double& lost) {
+  if (c.cnt == 0) return 2;                  // no panel (the reference would spin)
+  float snx = c.snx, sny = c.sny;
+  const float normilen = (float)(1.0 / (double)sqrtf(snx * snx + sny * sny));
+  snx *= normilen;
+  sny *= normilen;
+  const float scx = c.scx / (float)c.cnt;
+  const float scy = c.scy / (float)c.cnt;
+  const float dotp = snx * (x - scx) + sny * (y - scy) - cutoff_mult * ips;
+  if (method == 0) {
+    if (!(dotp < rad)) return 0;
+    float smult, dshift;
+    cut_entry(g, dotp / rad, smult, dshift);
+    lost += (double)s * (1.0 - (double)smult);
+    s *= smult;
+    x += dshift * rad * snx;
+    y += dshift * rad * sny;
+  } else {
+    if (!((double)dotp < -0.001 * (double)ips)) return 0;
+    x -= dotp * snx;
+    y -= dotp * sny;
+  }
+  return 1;
+}
+
+// One point, tested until it passes (at most max_sweeps times), against all panels of g read
+// from its arrays.  rad = the point's core radius (ips for field points).  Returns the number
+// of modifications, or -1 when max_sweeps ran out; lost receives the circulation removed
+// (method 0).  Each sweep takes two passes: the panel with the smallest lower bound gives, by
+// its exact distance, a bound T on the minimum; then only panels whose lower bound does not
+// exceed T are evaluated exactly, in panel order.  The reference's hits are the panels at the
+// exact minimum (ties included, in panel order), which this reproduces bit for bit.  The CUDA
+// kernel runs the same passes over panel records staged in shared memory.
 OBS_HD int clear_point(const Geo& g, int method, float cutoff_mult, float ips, float rad, float& x, float& y,
                        float& s, double& lost, int max_sweeps) {
-  const float big = (float)(0.1 * 3.4028234663852886e38);
   int crops = 0;
   lost = 0.0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    float mind = big, snx = 0.0f, sny = 0.0f, scx = 0.0f, scy = 0.0f;
-    int cnt = 0;
+    float lbmin = 3.4028234663852886e38f;
+    int jstar = -1;
     for (int j = 0; j < g.npan; ++j) {
       const unsigned a = g.idx[2 * j], b = g.idx[2 * j + 1];
-      float d2, cx, cy;
+      const float bx = g.nx[b] - g.nx[a], by = g.ny[b] - g.ny[a];
+      const float lb = seg_lower_bound(g.nx[a], g.ny[a], g.nx[b], g.ny[b], 1.0f / (bx * bx + by * by), x, y);
+      if (lb < lbmin) { lbmin = lb; jstar = j; }
+    }
+    float T = INFINITY;                           // no candidate: no rejection
+    if (jstar >= 0) {
+      const unsigned a = g.idx[2 * jstar], b = g.idx[2 * jstar + 1];
+      float cx, cy;
       int kind, which;
-      seg_closest(g.nx[a], g.ny[a], g.nx[b], g.ny[b], x, y, d2, cx, cy, kind, which);
-      if (d2 < mind) {                       // a new closest panel or node
-        mind = d2;
-        snx = sny = scx = scy = 0.0f;
-        cnt = 0;
-      } else if (!(d2 == mind)) {
-        continue;
-      }
-      if (kind == 0) {
-        snx += g.pnx[j];
-        sny += g.pny[j];
-      } else {
-        const unsigned nd = which ? b : a;
-        snx += g.nnx[nd];
-        sny += g.nny[nd];
-      }
-      scx += cx;
-      scy += cy;
-      ++cnt;
+      seg_closest(g.nx[a], g.ny[a], g.nx[b], g.ny[b], x, y, T, cx, cy, kind, which);
     }
-    if (cnt == 0) return crops;                // no panel (the reference would spin)
-    const float normilen = (float)(1.0 / (double)sqrtf(snx * snx + sny * sny));
-    snx *= normilen;
-    sny *= normilen;
-    scx /= (float)cnt;
-    scy /= (float)cnt;
-    const float dotp = snx * (x - scx) + sny * (y - scy) - cutoff_mult * ips;
-    if (method == 0) {
-      if (!(dotp < rad)) return crops;
-      float smult, dshift;
-      cut_entry(g, dotp / rad, smult, dshift);
-      lost += (double)s * (1.0 - (double)smult);
-      s *= smult;
-      x += dshift * rad * snx;
-      y += dshift * rad * sny;
-    } else {
-      if (!((double)dotp < -0.001 * (double)ips)) return crops;
-      x -= dotp * snx;
-      y -= dotp * sny;
+    Closest c;
+    closest_init(c);
+    for (int j = 0; j < g.npan; ++j) {
+      const unsigned a = g.idx[2 * j], b = g.idx[2 * j + 1];
+      const float x0 = g.nx[a], y0 = g.ny[a], x1 = g.nx[b], y1 = g.ny[b];
+      const float bx = x1 - x0, by = y1 - y0;
+      if (beyond(seg_lower_bound(x0, y0, x1, y1, 1.0f / (bx * bx + by * by), x, y), T)) continue;
+      closest_add(g, c, a, b, x0, y0, x1, y1, g.pnx[j], g.pny[j], x, y);
     }
+    const int r = clear_apply(g, c, method, cutoff_mult, ips, rad, x, y, s, lost);
+    if (r != 1) return crops;
     ++crops;
   }
   return -1;

@@ -43,6 +43,25 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+LIB_NATIVE = os.path.join(HERE, "liboracle_native.so")
+
+
+def build_native(force: bool = False) -> str:
+    """Compile oracle.c once more with the reference's Release flags (CMakeLists.txt:57:
+    -O3 -march=native, OpenMP; -mcpu=native on aarch64) into liboracle_native.so: the timed CPU
+    baseline.  The checker (liboracle.so) keeps the portable, non-fused build."""
+    import platform
+    src = os.path.join(HERE, "oracle.c")
+    impl = os.path.join(HERE, "oracle_impl.h")
+    if (not force and os.path.exists(LIB_NATIVE)
+            and os.path.getmtime(LIB_NATIVE) > max(os.path.getmtime(src), os.path.getmtime(impl))):
+        return LIB_NATIVE
+    arch = "-mcpu=native" if platform.machine().lower() in ("aarch64", "arm64") else "-march=native"
+    subprocess.run(["gcc", "-O3", arch, "-fopenmp", "-fPIC", "-shared", "-std=gnu11",
+                    src, "-o", LIB_NATIVE, "-lm"], check=True)
+    return LIB_NATIVE
+
+
 def _p(a):
     return None if a is None else a.ctypes.data_as(_vp)
 
@@ -52,10 +71,11 @@ def _arr(a, dt):
 
 
 class Restatement:
-    def __init__(self):
-        if not os.path.exists(LIB):
-            build()
-        self.lib = ctypes.CDLL(LIB)
+    def __init__(self, native: bool = False):
+        """native: the build with the reference's Release flags (the timed CPU baseline)."""
+        path = build_native() if native else (LIB if os.path.exists(LIB) else build())
+        self.native = native
+        self.lib = ctypes.CDLL(path)
         for name in ("o_centroid_loss_d", "o_rk2_centroid_grad_d", "o_rk2_centroid_loss_d"):
             getattr(self.lib, name).restype = ctypes.c_double
 

@@ -128,7 +128,9 @@ def engine_logic(tmp_path_factory):
     src = d / "harness.cpp"
     src.write_text(HARNESS)
     lib = d / "libharness.so"
-    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(root, "omega2d_gb300", "csrc"),
+    # built like the CUDA file and the oracle: no fused multiply-adds
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+                    "-I", os.path.join(root, "omega2d_gb300", "csrc"),
                     str(src), "-o", str(lib)], check=True)
     L = ctypes.CDLL(str(lib))
 
@@ -155,11 +157,13 @@ def test_engine_point_logic_matches_golden_and_oracle(engine_logic, restatement,
     _check_method0(g[shape + "_m0_x"], g[shape + "_m0_y"], g[shape + "_m0_s"], ex, ey, es, r)
     glost = g[shape + "_m0_lost"][0]
     assert abs(elost - glost) < 1e-5 * max(1.0, abs(glost))
-    # the oracle sweeps all points per pass, the engine repeats each point: same per-point result
+    # the oracle sweeps all points per pass, the engine repeats each point: the same per-point
+    # result, bit for bit (both built without fused multiply-adds)
     ox, oy, os_, olost, onc = restatement.clear_inner(0, cut, ips, nx, ny, idx, x, y, s, r)
-    same = (ex == ox) & (ey == oy) & (es == os_)
-    assert same.mean() > 0.95 and enc == onc
-    _check_method0(ox, oy, os_, ex, ey, es, r)
+    np.testing.assert_array_equal(ex, ox)
+    np.testing.assert_array_equal(ey, oy)
+    np.testing.assert_array_equal(es, os_)
+    assert enc == onc
     px, py, ps, plost, pnc = engine_logic(1, cut, ips, nx, ny, idx, x, y, s, r)
     assert plost == 0.0 and pnc > 0
     np.testing.assert_array_equal(ps, s)

@@ -430,7 +430,7 @@ def _clear_check_method0(g_x, g_y, g_s, x, y, s, r):
 
 
 @pytest.mark.parametrize("shape", ["circle", "star"])
-def test_clear_inner_layer_matches_reference(ctx, golden, shape):
+def test_clear_inner_layer_matches_reference(ctx, golden, restatement, shape):
     """clear_inner_layer (src/Reflect.h:491-760) against the reference's own routine
     (tests/golden/clear.npz): crop, push, and push of field points."""
     g = golden("clear")
@@ -441,6 +441,12 @@ def test_clear_inner_layer_matches_reference(ctx, golden, shape):
     p = og.Points(x, y, r, s)
     lost, nc = og.clear_inner_layer(p, body, ips, method=0, cutoff_mult=cut, env=env)
     _clear_check_method0(g[shape + "_m0_x"], g[shape + "_m0_y"], g[shape + "_m0_s"], p.x, p.y, p.s, r)
+    # the oracle is built without fused multiply-adds, like the kernel: equal bit for bit
+    ox, oy, os_, _, onc = restatement.clear_inner(0, cut, ips, body.nx, body.ny, body.idx, x, y, s, r)
+    np.testing.assert_array_equal(p.x, ox)
+    np.testing.assert_array_equal(p.y, oy)
+    np.testing.assert_array_equal(p.s, os_)
+    assert nc == onc
     glost = float(g[shape + "_m0_lost"][0])
     assert abs(lost - glost) < 1e-5 * max(1.0, abs(glost)) and nc > 0
     p = og.Points(x, y, r, s)
@@ -467,7 +473,38 @@ def test_clear_inner_layer_large_vs_oracle(ctx, restatement):
     lost, nc = og.clear_inner_layer(p, body, ips, method=0, env=og.ExecEnv(context=ctx))
     ox, oy, os_, olost, onc = restatement.clear_inner(0, og.CLEAR_CUTOFF, ips, body.nx, body.ny, body.idx,
                                                       x, y, s, r)
-    _clear_check_method0(ox, oy, os_, p.x, p.y, p.s, r)
+    # the kernel and the oracle both round every product and sum as written: bit for bit
+    np.testing.assert_array_equal(p.x, ox)
+    np.testing.assert_array_equal(p.y, oy)
+    np.testing.assert_array_equal(p.s, os_)
+    assert nc == onc
     assert abs(lost - olost) < 1e-4 * max(1.0, abs(olost))
     # every particle ends at or above the layer's inner edge
     assert np.min(np.hypot(p.x, p.y)) > 0.5
+
+
+def test_clear_inner_layer_shared_node_and_tiles_vs_oracle(ctx, restatement):
+    """Two triangles joined at one node (four panels meet there: its normal is summed in panel
+    order, as in the reference) and a 5000-panel circle (several shared-memory tiles of panel
+    records per sweep): the kernel equals the oracle bit for bit."""
+    rng = np.random.default_rng(31)
+    nx = np.array([0.0, 0.4, 0.4, -0.4, -0.4], np.float32)
+    ny = np.array([0.0, -0.2, 0.2, 0.2, -0.2], np.float32)
+    idx = np.array([0, 1, 1, 2, 2, 0, 0, 3, 3, 4, 4, 0], np.uint32)       # clockwise bow tie
+    bowtie = og.Surfaces(nx, ny, idx)
+    big = og.circle_panels(5000)
+    for body, n, lo, hi in ((bowtie, 3000, 0.0, 0.45), (big, 8000, 0.3, 0.6)):
+        rad = rng.uniform(lo, hi, n)
+        a = rng.uniform(0, 2 * np.pi, n)
+        x, y = (rad * np.cos(a)).astype(np.float32), (rad * np.sin(a)).astype(np.float32)
+        s = rng.normal(0, 1, n).astype(np.float32)
+        r = np.full(n, 0.01, np.float32)
+        for method in (0, 1):
+            p = og.Points(x, y, r, s)
+            lost, nc = og.clear_inner_layer(p, body, 0.01, method=method, env=og.ExecEnv(context=ctx))
+            ox, oy, os_, olost, onc = restatement.clear_inner(method, og.CLEAR_CUTOFF, 0.01, body.nx, body.ny,
+                                                              body.idx, x, y, s, r)
+            np.testing.assert_array_equal(p.x, ox)
+            np.testing.assert_array_equal(p.y, oy)
+            np.testing.assert_array_equal(p.s, os_)
+            assert nc == onc and nc > 0
