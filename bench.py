@@ -616,6 +616,17 @@ def run_bem2048(args):
     def pipeline():
         d3(); b2(); b1(); solve(); d2()
 
+    # clear_inner_layer of the same particles against the body (src/Reflect.h:491-760): every
+    # particle is tested against every panel; those inside the layer are cropped
+    CX, CY, CS = PX.clone(), PY.clone(), PS.clone()
+    CR = torch.full((npart,), 0.01, device=dev)
+
+    def clear_reset():
+        CX.copy_(PX); CY.copy_(PY); CS.copy_(PS)
+
+    def clear():
+        box["clear"] = og.clear_inner_layer_dev(ctx, 0, og.CLEAR_CUTOFF, 0.01, NX, NY, IDX, CX, CY, CS, CR)
+
     # the literal 2048 x 2048 system: vortex strengths only (the nunk == 1 branch,
     # src/Coefficients.h:366-385)
     RHS1 = torch.zeros(npan, dtype=torch.float64, device=dev)
@@ -643,12 +654,14 @@ def run_bem2048(args):
                               ("points_affect_panels", d3), ("vels_to_rhs", b2), ("panels_on_panels_coeff_f64", b1),
                               ("lu_solve_f64", solve_lu), ("gmres_solve_f64", solve), ("panels_affect_points", d2),
                               ("pipeline", pipeline))}
+        times["clear_inner_layer"] = _event_time(torch, stream, flush, clear, args.steps, args.warmup, prep=clear_reset)
     ctx.synchronize()
     out["clocks"] = clk.summary()
     out["ms"] = times
     out["value"] = times["pipeline"]
     out["ginter_s"] = {"points_affect_panels": npart * npan / (times["points_affect_panels"] * 1e-3) / 1e9,
                        "panels_affect_points": npart * npan / (times["panels_affect_points"] * 1e-3) / 1e9,
+                       "clear_inner_layer_pairs": npart * npan / (times["clear_inner_layer"] * 1e-3) / 1e9,
                        "lu_tflops_f64": (2.0 / 3.0) * m ** 3 / (times["lu_solve_f64"] * 1e-3) / 1e12}
     # GMRES: one FP64 matrix-vector product per iteration reads the 4096^2 matrix from HBM
     out["gmres"] = {"iterations": box.get("it"), "relative_residual": box.get("rel"),
@@ -680,10 +693,26 @@ def run_bem2048(args):
     out["precision"] = {"strengths_max_rel": float(np.max(np.abs(sol - x64)) / np.max(np.abs(x64))),
                         "panels_affect_points_subset_max_rel":
                             float(np.max(np.abs(np.concatenate([tu[sub], tv[sub]]) - vel)) / np.max(np.abs(vel)))}
+    # clear_inner_layer: parity with the oracle on a 4096-particle sample, and its CPU time
+    cres = box.get("clear")
+    cx_, cy_, cs_ = CX.cpu().numpy(), CY.cpu().numpy(), CS.cpu().numpy()
+    rs = np.full(sub.size, 0.01, np.float32)
+    ox, oy, os_, _, _ = orc.clear_inner(0, og.CLEAR_CUTOFF, 0.01, bd.nx, bd.ny, bd.idx, px[sub], py[sub], ps[sub], rs)
+    out["clear_inner_layer"] = {"particles": npart, "panels": npan, "ms": times["clear_inner_layer"],
+                                "circulation_removed_and_modifications": cres,
+                                "particles_moved": int(((cx_ != px) | (cy_ != py)).sum()),
+                                "sample_equal_to_oracle": bool((ox == cx_[sub]).all() and (oy == cy_[sub]).all()
+                                                               and (os_ == cs_[sub]).all())}
+    nat = po.Restatement(native=True)
+    t0 = time.perf_counter()
+    nat.clear_inner(0, og.CLEAR_CUTOFF, 0.01, bd.nx, bd.ny, bd.idx, px[sub], py[sub], ps[sub], rs)
+    t_cl = time.perf_counter() - t0
     out["cpu_baseline"] = {"kind": "port", "cores": threads,
                            "points_affect_panels_ginter_s": npart * npan / t_d3 / 1e9,
                            "panels_on_panels_coeff_ms": 1e3 * t_b1,
-                           "sample": "FP64 restatement of the full particles-on-panels sum and matrix"}
+                           "clear_inner_layer_pairs_per_s": sub.size * npan / t_cl,
+                           "sample": "FP64 restatement of the full particles-on-panels sum and matrix; "
+                                     "clear_inner_layer on 4096 of the particles"}
     return out
 
 

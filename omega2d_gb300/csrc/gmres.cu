@@ -32,6 +32,8 @@ struct GmState {
   int kdone;       // iterations completed in this cycle
   double beta;     // residual norm at the start of the cycle
   double tolabs;   // absolute tolerance on the residual norm
+  double tolcyc;   // the cycle's target: tolabs, or a relative reduction when the cycle's
+                   // products use the FP32 plane of A (iterative refinement)
 };
 
 // part[c][i] = sum_{j in chunk c} A[j*n + i] * (x[j] * dinv[j])   (column-major A)
@@ -135,11 +137,13 @@ __global__ void scale_kernel(const double* __restrict__ w, int n, const double* 
   if (i < n) v[i] = w[i] / *nrm;
 }
 
-// start of a cycle: beta = ||r||, g = (beta, 0, ...), V_0 = r / beta; done when beta is small
-__global__ void cycle_start_kernel(GmState* st, const double* nrm, double* g, int m) {
+// start of a cycle: beta = ||r||, g = (beta, 0, ...), V_0 = r / beta; done when beta is small;
+// the cycle's target is max(tolabs, eta * beta)
+__global__ void cycle_start_kernel(GmState* st, const double* nrm, double* g, int m, double eta) {
   st->beta = *nrm;
   st->kdone = 0;
   st->done = (*nrm <= st->tolabs) ? 1 : 0;
+  st->tolcyc = fmax(st->tolabs, eta * *nrm);
   for (int k = 0; k <= m; ++k) g[k] = 0.0;
   g[0] = *nrm;
 }
@@ -163,7 +167,7 @@ __global__ void givens_kernel(double* H, int ldh, int j, double* cs, double* sn,
   g[j + 1] = -s * g[j];
   g[j] = c * g[j];
   st->kdone = j + 1;
-  if (fabs(g[j + 1]) <= st->tolabs || b == 0.0) st->done = 1;
+  if (fabs(g[j + 1]) <= st->tolcyc || b == 0.0) st->done = 1;
 }
 
 // y = R^{-1} g (R upper triangular k x k in H), into yv
@@ -194,47 +198,46 @@ __global__ void diag_inv_kernel(const double* __restrict__ A, int n, double* __r
 }
 
 // ---------------------------------------------------------------- one restart cycle in one launch
-// FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU, so the operator
-// product of the fused cycle multiplies in double-float: A is held as two FP32 planes
-// (hi = fl(a), lo = fl(a - hi): 48 of a's 53 significand bits) and the vector the same way;
-// each product is formed exactly with an FMA and summed in an unevaluated (S, s) pair.
-// Everything else (Gram-Schmidt, norms, Givens, back substitution, the restart residual)
-// stays FP64.
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU, and the FP64 matrix
+// (8 n^2 bytes) does not fit in L2, so the operator product of the fused cycle uses the FP32
+// plane of A (hi: its top 24 significand bits, 4 n^2 bytes, which stays in L2 across the
+// cycle's iterations) against the vector in double-float (hi + lo), each product formed exactly
+// with an FMA and summed in an unevaluated (S, s) pair.  The cycle thus solves with A_hi, whose
+// entries carry a relative error below 2^-23, and stops at a relative reduction of 2^-20; the
+// restart residual b - A x is formed with the FP64 matrix, so every restart corrects the
+// solution against A itself (iterative refinement): the final residual meets the FP64
+// tolerance.  Everything else (Gram-Schmidt, norms, Givens, back substitution, the restart
+// residual) stays FP64.
 
+constexpr double kRefineEta = 9.5367431640625e-7;   // 2^-20: a cycle's relative reduction on A_hi
 constexpr int GC_THREADS = 1024;
 constexpr int GC_WARPS = GC_THREADS / 32;
 constexpr int GC_MAXM = 64;                     // restart length supported by the fused kernel
 
-// hi/lo planes of A, split from the bits of each double without FP64 arithmetic (double <->
-// float conversions run on the slow FP64 path of this GPU): hi keeps the sign, the exponent and
-// the top 23 stored significand bits (truncated), lo is the remaining 29 bits as an integer
-// converted to FP32 (rounded to 24 bits) and scaled by 2^(e-1075) in two normal steps; hi + lo
-// carries 48 significand bits.  Flags entries outside 2^+-99 (other than 0), where the planes
-// would lose precision or overflow.
-__device__ __forceinline__ float2 split_bits(double a, int& bad) {
+// hi plane of A, from the bits of each double without FP64 arithmetic (double <-> float
+// conversions run on the slow FP64 path of this GPU): the sign, the exponent and the top 23
+// stored significand bits (truncated: relative error below 2^-23).  Flags entries outside
+// 2^+-99 (other than 0), where the plane would lose precision or overflow.
+__device__ __forceinline__ float hi_bits(double a, int& bad) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(a);
   const int e = (int)((u >> 52) & 0x7ff);
   const unsigned long long mant = u & ((1ull << 52) - 1);
   const unsigned sign = (unsigned)(u >> 63) << 31;
   bad |= (e != 0 && (e < 1023 - 99 || e > 1023 + 99)) || (e == 0 && mant != 0);
-  if (e == 0) return make_float2(__uint_as_float(sign), 0.0f);
-  const unsigned hib = sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29);
-  const int sh = e - 1075, s1 = sh / 2, s2 = sh - s1;            // each in [-76, 24] when not flagged
-  const float p1 = __uint_as_float((unsigned)(s1 + 127) << 23), p2 = __uint_as_float((unsigned)(s2 + 127) << 23);
-  const float lo = __int2float_rn((int)(mant & ((1ull << 29) - 1))) * p1 * p2;
-  return make_float2(__uint_as_float(hib), __uint_as_float(__float_as_uint(lo) | sign));
+  if (e == 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
 }
 
-__global__ void split_planes_kernel(const double* __restrict__ A, size_t nn, float2* __restrict__ AP,
-                                    int* __restrict__ range_flag) {
+__global__ void split_hi_kernel(const double* __restrict__ A, size_t nn, float* __restrict__ AH,
+                                int* __restrict__ range_flag) {
   int bad = 0;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x)
-    AP[k] = split_bits(A[k], bad);
+    AH[k] = hi_bits(A[k], bad);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(range_flag, 1);
 }
 
 struct GcArgs {
-  const float2* AP;                             // hi/lo planes of A, column-major
+  const float* AH;                              // hi plane of A, column-major
   const double* dinv;
   int n, m, mc;                                 // order, restart length, iterations this cycle
   int gpb;                                      // row groups a block owns (at most)
@@ -369,7 +372,7 @@ __device__ __forceinline__ void df_add(float& S, float& s, float T, float t) {
 
 // One restart cycle of right-preconditioned GMRES(m) with CGS2, back substitution and the
 // update of x, in one cooperative launch.  Blocks own groups of 32 consecutive rows
-// (column-major A: a warp reads 256 contiguous bytes of the planes per column) and keep those
+// (column-major A: a warp reads 128 contiguous bytes of the hi plane per column) and keep those
 // rows of the basis in shared memory; only the split vector Dinv v_j and the per-block partial
 // sums cross between blocks.  Iteration j:
 //   (1) w = A Dinv v_j on the owned rows; partial V^T w                         -> barrier
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
       hc[jc + 1] = 0.0;
       gs[jc + 1] = -sg * gs[jc];
       gs[jc] = c * gs[jc];
-      sdone = (fabs(gs[jc + 1]) <= a.st->tolabs || x1 == 0.0) ? 1 : 0;
+      sdone = (fabs(gs[jc + 1]) <= a.st->tolcyc || x1 == 0.0) ? 1 : 0;
     }
     const bool more = j < a.mc;
     // (1) w = A Dinv v_j on the owned rows, double-float; columns split over the warps, the
@@ -453,14 +456,14 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
       const int i = row(q);
       const int ic = min(i, a.n - 1);            // rows past n compute a dummy sum, never stored
       float S0 = 0.f, s0 = 0.f, S1 = 0.f, s1 = 0.f;
-      const float2* col = a.AP + (size_t)c0 * a.n + ic;
+      const float* col = a.AH + (size_t)c0 * a.n + ic;
       int c = c0;
 #pragma unroll 8
       for (; c + 1 < c1; c += 2, col += 2 * (size_t)a.n) {
-        df_fma(__ldg(col), a.vs[c], S0, s0);
-        df_fma(__ldg(col + a.n), a.vs[c + 1], S1, s1);
+        df_fma(make_float2(__ldg(col), 0.0f), a.vs[c], S0, s0);
+        df_fma(make_float2(__ldg(col + a.n), 0.0f), a.vs[c + 1], S1, s1);
       }
-      if (c < c1) df_fma(__ldg(col), a.vs[c], S0, s0);
+      if (c < c1) df_fma(make_float2(__ldg(col), 0.0f), a.vs[c], S0, s0);
       df_add(S0, s0, S1, s1);
       redf[wp][lane] = make_float2(S0, s0);
       __syncthreads();
@@ -631,7 +634,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   const size_t o_gv = o_gp + al((size_t)2 * gc_grid * (m + 2) * 8);
   const size_t o_gb = o_gv + al(N * 8);
   const size_t o_ap = o_gb + 256;
-  const size_t total = fused ? o_ap + al(N * N * 8) : o_gb + 256;
+  const size_t total = fused ? o_ap + al(N * N * 4) : o_gb + 256;
   int s = ctx->work.ensure(total, ctx->stream);
   if (s) return s;
   GmState* st = ctx->work.as<GmState>(o_st);
@@ -649,7 +652,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   double* gpart = ctx->work.as<double>(o_gp);
   float2* gvs = ctx->work.as<float2>(o_gv);
   unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag, [2] x != 0
-  float2* AP = fused ? ctx->work.as<float2>(o_ap) : nullptr;
+  float* AH = fused ? ctx->work.as<float>(o_ap) : nullptr;
   cudaStream_t strm = ctx->stream;
   const int gb = (n + GM_THREADS - 1) / GM_THREADS;
   const dim3 ggrid(gb, nchunk);
@@ -662,7 +665,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
   launched(1);
   if (fused) {
-    split_planes_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, N * N, AP, reinterpret_cast<int*>(gbar + 1));
+    split_hi_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, N * N, AH, reinterpret_cast<int*>(gbar + 1));
     launched(1);
   }
   double bnorm = 0.0;
@@ -674,7 +677,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   if (e != cudaSuccess) return cuda_status(e);
   if (range_bad) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
   const double bref = (bnorm == 0.0) ? 1.0 : bnorm;   // src/BEM.h:227-229 divides by 1 then
-  GmState h0{0, 0, 0.0, tol * bref};
+  GmState h0{0, 0, 0.0, tol * bref, tol * bref};
   if ((e = cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, strm)) != cudaSuccess) return cuda_status(e);
 
   // r = b - A x in FP64 (the true residual), its norm into nrm
@@ -690,12 +693,16 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     if ((e = cudaMemcpyAsync(w, b, N * 8, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess) return cuda_status(e);
   }
   int total_it = 0;
-  double rel = 0.0;
+  double rel = 0.0, prev_rn = -1.0;
   for (;;) {
     double rn = 0.0;
     e = cudaMemcpyAsync(&rn, nrm, 8, cudaMemcpyDeviceToHost, strm);
     if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
     if (e != cudaSuccess) return cuda_status(e);
+    // a refinement cycle (FP32 plane) that did not halve the true residual: A is too
+    // ill-conditioned for its FP32 entries, so finish with FP64 products throughout
+    if (fused && prev_rn > 0.0 && !(rn < 0.5 * prev_rn)) fused = false;
+    prev_rn = rn;
     if (total_it > 0) {
       // the cycle's iteration count; a barrier that gave up leaves its record in the status block
       int kd = 0, flag = 0;
@@ -708,13 +715,13 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     }
     rel = rn / bref;
     if (!(rn > tol * bref) || total_it >= maxiter) break;   // converged (or NaN) / out of budget
-    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m);
+    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m, fused ? kRefineEta : 0.0);
     scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, nrm, V, nullptr);
     launched(2);
     const int mc = std::min(m, maxiter - total_it);
     if (fused) {
       if ((e = cudaMemsetAsync(gbar, 0, sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
-      GcArgs ga{AP, dinv, n, m, mc, gc_gpb, V, gvs, x, gpart, gbar, st, ctx->d_status};
+      GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvs, x, gpart, gbar, st, ctx->d_status};
       void* args[] = {&ga};
       e = cudaLaunchCooperativeKernel((const void*)gmres_cycle_kernel, dim3(gc_grid), dim3(GC_THREADS), args, gc_smem,
                                       strm);

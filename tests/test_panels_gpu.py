@@ -235,9 +235,10 @@ def test_gmres_dense_and_no_convergence(ctx):
 
 @pytest.mark.parametrize("n", [1, 5, 33, 1000, 4100])
 def test_gmres_fused_cycle_matches_per_step_kernels(n):
-    """One cooperative launch per restart cycle (restart <= 64) against one kernel per step:
-    the same Krylov method, so the iteration counts agree and both solutions are exact to
-    the tolerance; ragged orders leave part of the last 32-row group empty."""
+    """One cooperative launch per restart cycle (restart <= 64; products with the FP32 plane of
+    A, each restart refining against the FP64 matrix) against one FP64 kernel per step: both
+    solutions are exact to the tolerance, and refinement costs at most a few extra
+    iterations; ragged orders leave part of the last 32-row group empty."""
     rng = np.random.default_rng(90 + n)
     A = np.eye(n) * 3.0 + rng.normal(0, 1.0 / np.sqrt(n), (n, n))
     xt = rng.normal(size=n)
@@ -249,7 +250,7 @@ def test_gmres_fused_cycle_matches_per_step_kernels(n):
         out[variant] = og.solve_gmres_f64(A, b, tol=1e-12, restart=40, maxiter=400, context=c)
     (xf, itf, relf), (xg, itg, relg) = out[og.VARIANT_AUTO], out[og.VARIANT_GENERIC]
     assert relf < 1e-12 and relg < 1e-12
-    assert abs(itf - itg) <= 1
+    assert itf <= itg + 12
     assert np.max(np.abs(xf - xt)) < 1e-9 * np.max(np.abs(xt))
     assert np.max(np.abs(xf - xg)) < 1e-9 * np.max(np.abs(xt))
 
