@@ -407,6 +407,34 @@ int obs_points_affect_points_noalloc(void* cuda_stream, int core, int result, in
                                      float* extra0, float* extra1, float* extra2, float* extra3);
 
 /*
+ * points_affect_points by treecode -- the reference's Barnes-Hut summation slot
+ * (summation_t barneshut, src/ExecEnv.h:26-31), which the reference itself reaches only through
+ * the external solver hook (onbody's treecode, src/Influence.h:31-38, 74-98).  Velocity only
+ * (results_t velonly), every core, thick (tr) or field-point (tr == NULL) targets; outputs
+ * accumulated like obs_points_affect_points (OBS_FLAG_FINALIZE applies finalize_vels).
+ * Sources in Morton order form a tree of 32-source leaves and 4-way nodes carrying `order`
+ * multipole coefficients; a node acts on a warp of 32 targets through its expansion when its
+ * radius is at most theta times the distance from its centre to the targets' box and every
+ * pair lies where the core equals 1/d^2 (exactly for the Gaussian and compact exponential cut-
+ * offs and the singular core; within 2^-24 for the others), else it opens, down to direct
+ * sums over leaves with the core.  Truncation per node is below theta^order/(1 - theta) of
+ * its summed |strength|/distance.  theta in (0, 1) (0 selects the default), order 1..32 (0:
+ * default).  Compensated accumulation; flops (optional) receives the direct-sum count of the
+ * same call.  _dev: device arrays, asynchronous on the context's stream.
+ */
+#define OBS_TREE_THETA_DEFAULT 0.5
+#define OBS_TREE_ORDER_DEFAULT 24
+#define OBS_TREE_ORDER_MAX 32
+int obs_points_affect_points_tree(obs_context* ctx, int core, int flags, double fsx, double fsy, double theta,
+                                  int order, int ns, const float* sx, const float* sy, const float* sr,
+                                  const float* ss, int nt, const float* tx, const float* ty, const float* tr,
+                                  float* tu, float* tv, double* flops);
+int obs_points_affect_points_tree_dev(obs_context* ctx, int core, int flags, double fsx, double fsy, double theta,
+                                      int order, int ns, const float* sx, const float* sy, const float* sr,
+                                      const float* ss, int nt, const float* tx, const float* ty, const float* tr,
+                                      float* tu, float* tv, double* flops);
+
+/*
  * Source-compatible replacements for the reference's external direct-solver hook
  * (src/Influence.h:31-38, called at :74-98 when built with -DEXTERNAL_VEL_SOLVE).
  * Same argument order (note ss before sr), counts by pointer, velocities ACCUMULATED and
@@ -422,6 +450,13 @@ float external_vel_solver_tr_f_(int* ns, const float* sx, const float* sy, const
 float external_vel_solver_d_(int* ns, const double* sx, const double* sy, const double* ss, const double* sr,
                              int* nt, const double* tx, const double* ty, double* tu, double* tv);
 int obs_external_configure(int core, int accum);
+/* Summation behind the external hook: OBS_SUMMATION_DIRECT (default) or OBS_SUMMATION_TREE
+ * (obs_points_affect_points_tree with theta and order; 0 selects their defaults) -- the values
+ * of summation_t direct and barneshut (src/ExecEnv.h:26-31).  external_vel_solver_d_ always
+ * sums directly in FP64. */
+#define OBS_SUMMATION_DIRECT 1
+#define OBS_SUMMATION_TREE 2
+int obs_external_configure_summation(int summation, double theta, int order);
 
 #ifdef __cplusplus
 }

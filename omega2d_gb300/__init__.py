@@ -291,6 +291,48 @@ def points_affect_points(src: Points, targ: Points, restype: ResultsType | int =
     return flops.value
 
 
+TREE_THETA_DEFAULT = 0.5
+TREE_ORDER_DEFAULT = 24
+SUMMATION_DIRECT, SUMMATION_TREE = 1, 2      # summation_t direct, barneshut (src/ExecEnv.h:26-31)
+
+
+def points_affect_points_tree(src: Points, targ: Points, env: ExecEnv | None = None, theta: float = 0.0,
+                              order: int = 0, finalize: bool = False, fs=(0.0, 0.0)) -> float:
+    """Velocity of the source particles at the targets by treecode (the reference's
+    summation_t barneshut slot, src/ExecEnv.h:26-31): accumulated into targ.u, targ.v like
+    points_affect_points with VELONLY.  theta (0: 0.5) and order (0: 24 terms) set the
+    multipole acceptance and truncation.  Returns the direct-sum flop count of the call."""
+    env = env or ExecEnv()
+    flops = ctypes.c_double()
+    st = lib().obs_points_affect_points_tree(
+        env.ctx().handle, ctypes.c_int(env.core), ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+        ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(theta), ctypes.c_int(order),
+        ctypes.c_int(src.n), _ptr(src.x), _ptr(src.y), _ptr(src.r), _ptr(src.s),
+        ctypes.c_int(targ.n), _ptr(targ.x), _ptr(targ.y), _ptr(targ.r), _ptr(targ.u), _ptr(targ.v),
+        ctypes.byref(flops))
+    _check(st, "obs_points_affect_points_tree")
+    return flops.value
+
+
+def points_affect_points_tree_dev(ctx: "Context", core: int, sx, sy, sr, ss, tx, ty, tr, tu, tv,
+                                  theta: float = 0.0, order: int = 0, finalize: bool = False,
+                                  fs=(0.0, 0.0)) -> float:
+    """Device-resident treecode velocity (CUDA tensors); asynchronous on the context's stream."""
+    ns, nt = sx.numel(), tx.numel()
+    for name, t, need in (("sy", sy, ns), ("sr", sr, ns), ("ss", ss, ns), ("ty", ty, nt), ("tr", tr, nt),
+                          ("tu", tu, nt), ("tv", tv, nt)):
+        if t is not None and t.numel() < need:
+            raise ValueError(f"{name} has {t.numel()} elements, the call needs {need}")
+    flops = ctypes.c_double()
+    st = lib().obs_points_affect_points_tree_dev(
+        ctx.handle, ctypes.c_int(core), ctypes.c_int(FLAG_FINALIZE if finalize else 0),
+        ctypes.c_double(fs[0]), ctypes.c_double(fs[1]), ctypes.c_double(theta), ctypes.c_int(order),
+        ctypes.c_int(ns), _ptr(sx), _ptr(sy), _ptr(sr), _ptr(ss),
+        ctypes.c_int(nt), _ptr(tx), _ptr(ty), _ptr(tr), _ptr(tu), _ptr(tv), ctypes.byref(flops))
+    _check(st, "obs_points_affect_points_tree_dev")
+    return flops.value
+
+
 def points_affect_points_vorticity(src: Points, targ: Points, env: ExecEnv | None = None,
                                    finalize: bool = False) -> None:
     """points_affect_points_vorticity (src/InfluenceVort.h:47-126): accumulate the Gaussian-blob

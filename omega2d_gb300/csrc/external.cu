@@ -17,6 +17,9 @@ std::mutex g_mu;
 obs_context* g_ctx = nullptr;
 int g_core = OBS_CORE_V2;        // the reference's compiled-in default (src/CoreFunc.h:38)
 int g_accum = OBS_COMPENSATED;   // closest to the reference's double accumulators
+int g_summation = OBS_SUMMATION_DIRECT;
+double g_theta = OBS_TREE_THETA_DEFAULT;
+int g_order = OBS_TREE_ORDER_DEFAULT;
 
 obs_context* global_ctx() {
   if (!g_ctx) {
@@ -75,15 +78,30 @@ float run_external_f(int* ns, const float* sx, const float* sy, const float* ss,
   obs_context* ctx = global_ctx();
   if (!ctx) return -1.0f;
   double flops = 0.0;
-  const int s = obs_points_affect_points(ctx, g_core, OBS_VELONLY, g_accum, 0, 0.0, 0.0,
-                                         *ns, sx, sy, sr, ss, *nt, tx, ty, tr, tu, tv,
-                                         nullptr, nullptr, nullptr, nullptr, &flops);
+  const int s = g_summation == OBS_SUMMATION_TREE
+                    ? obs_points_affect_points_tree(ctx, g_core, 0, 0.0, 0.0, g_theta, g_order, *ns, sx, sy, sr, ss,
+                                                    *nt, tx, ty, tr, tu, tv, &flops)
+                    : obs_points_affect_points(ctx, g_core, OBS_VELONLY, g_accum, 0, 0.0, 0.0,
+                                               *ns, sx, sy, sr, ss, *nt, tx, ty, tr, tu, tv,
+                                               nullptr, nullptr, nullptr, nullptr, &flops);
   return s == OBS_OK ? (float)flops : -1.0f;
 }
 
 }  // namespace
 
 extern "C" {
+
+int obs_external_configure_summation(int summation, double theta, int order) {
+  if (summation != OBS_SUMMATION_DIRECT && summation != OBS_SUMMATION_TREE) return OBS_ERR_ARG;
+  if (theta == 0.0) theta = OBS_TREE_THETA_DEFAULT;
+  if (order == 0) order = OBS_TREE_ORDER_DEFAULT;
+  if (!(theta > 0.0 && theta < 1.0) || order < 1 || order > OBS_TREE_ORDER_MAX) return OBS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_summation = summation;
+  g_theta = theta;
+  g_order = order;
+  return OBS_OK;
+}
 
 int obs_external_configure(int core, int accum) {
   if (core < OBS_CORE_RM || core > OBS_CORE_COMPACT_EXP) return OBS_ERR_ARG;

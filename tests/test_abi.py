@@ -107,3 +107,21 @@ def test_clear_inner_layer_rejects_bad_arguments_without_a_device(engine_lib):
     assert call(h, 2, 0.02, p) == -1
     assert call(h, 1, 0.0, p) == -1
     assert call(h, 0, 0.02, None) == -1
+
+
+def test_tree_entry_points_check_arguments(engine_lib):
+    """The treecode entry points reject a null context, theta outside (0, 1), an order beyond 32
+    and missing arrays before touching a device; the external hook's summation switch rejects
+    unknown summations."""
+    z = np.zeros(4, np.float32)
+    p = z.ctypes.data_as(ctypes.c_void_p)
+    for fn in (engine_lib.obs_points_affect_points_tree, engine_lib.obs_points_affect_points_tree_dev):
+        args = lambda theta, order, sr=p: (None, 2, 0, ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(theta),
+                                           ctypes.c_int(order), 4, p, p, sr, p, 4, p, p, None, p, p, None)
+        assert fn(*args(0.5, 24)) == -1                     # null context
+    sw = engine_lib.obs_external_configure_summation
+    assert sw(3, ctypes.c_double(0.5), 24) == -1
+    assert sw(2, ctypes.c_double(1.0), 24) == -1
+    assert sw(2, ctypes.c_double(0.5), 33) == -1
+    assert sw(2, ctypes.c_double(0.0), 0) == 0             # defaults
+    assert sw(1, ctypes.c_double(0.0), 0) == 0             # back to direct sums
