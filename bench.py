@@ -159,6 +159,24 @@ def time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args):
     return out
 
 
+def time_tree(og, torch, ctx, stream, flush, X, Y, R, S, args):
+    """The same N x N velocity evaluation by treecode (obs_points_affect_points_tree: theta 0.5,
+    24 terms), CUDA events on the launching stream, L2 flushed; its error against the FP64 direct
+    sum is filled in with the headline's precision check."""
+    n = X.numel()
+    U, V = torch.zeros(n, device=X.device), torch.zeros(n, device=X.device)
+
+    def call():
+        U.zero_()
+        V.zero_()
+        og.points_affect_points_tree_dev(ctx, og.CORE_GAUSSIAN, X, Y, R, S, X, Y, R, U, V)
+    ms = _event_time(torch, stream, flush, call, max(1, args.steps // 2), 2)
+    return {"kernel": "tree_eval_kernel (Morton-ordered tree of 32-source leaves, 4-way nodes, 24-term "
+                      "multipole expansions; theta 0.5)", "ms": ms,
+            "effective_ginter_s": float(n) * n / (ms * 1e-3) / 1e9,
+            "_uv": (U, V)}
+
+
 def workload_config() -> dict:
     """The headline workload, named the same way by both arms."""
     return {"workload": f"gaussian_patch_{N}", "n": N, "core": "gaussian", "sigma": SIGMA,
@@ -351,6 +369,7 @@ def run_engine(args):
         ms_plain, main_plain, _ = timed(og.PLAIN_F32, max(1, args.steps // 2), 1)
         adjoint, adj_launches, adj_host = time_adjoint(og, torch, ctx, stream, dev, flush, args.steps, args.warmup)
         gradient = time_gradient(og, torch, ctx, stream, dev, flush, X, Y, R, S, args)
+        tree = time_tree(og, torch, ctx, stream, flush, X, Y, R, S, args)
     clocks = clk.summary()
 
     # end to end through the host-pointer C ABI call (copies in the timed region), the host
@@ -403,6 +422,9 @@ def run_engine(args):
         prec[name] = {"max_rel": mx, "rms_rel": rms}
     # velocity-gradient precision on the same 1024 targets (du/dx, dv/dx, du/dy, dv/dy)
     _, _, g64 = orc.points_affect_points(po.GAUSS, po.VELANDGRAD, x, y, r, s, x[sub], y[sub], r[sub], fp64=True)
+    U_t, V_t = tree.pop("_uv")
+    mx, rms = rel_errs(ref64, np.concatenate([U_t.cpu().numpy()[sub], V_t.cpu().numpy()[sub]]))
+    tree.update(max_rel=mx, rms_rel=rms, speedup_over_direct=ms_comp / tree["ms"])
     ref_g = np.concatenate(g64)
     for name in ("compensated", "plain"):
         got = np.concatenate([a[sub] for a in gradient.pop("_grad_" + name)])
@@ -452,6 +474,7 @@ def run_engine(args):
                          "sample": f"{args.cpu_sample} seeded targets x {N} sources"},
         "adjoint": adjoint,
         "gradient": gradient,
+        "treecode": tree,
         "gpu_launches": launches,
         "clocks": clocks,
     }
