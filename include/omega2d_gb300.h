@@ -307,6 +307,29 @@ int obs_solve_bem_augmented(obs_context* ctx, int nunk, int accum, int flags, do
                             const float* bcn, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
                             double* rel_residual);
 
+/* Several bodies in one BEM system (src/BEMHelper.h:147-221 assembles it block by block;
+ * src/Coefficients.h:429-572 augments each rotating body): the bodies' nodes and panels are
+ * joined in one set (node indices global, body k owns panels [panel_off[k], panel_off[k+1])),
+ * the panel unknowns come first in panel order, then one rotation unknown per body with
+ * augmented[k] != 0, in body order.  Rotating body a adds a row (its panel lengths under its
+ * vortex unknowns, 0 under every other panel, 2 * its area on the diagonal, 0 under the other
+ * rotation unknowns) and a column (the velocity of its unit-rotation sheet at every panel of the
+ * set, finalized, along each panel's tangent and normal).  The reference orders each body's
+ * rotation unknown after that body's panels; this is the same system with its rows and
+ * columns permuted.  obs_panels_on_panels_coeff_bodies returns the FP64 matrix (column-major)
+ * and geom = (area, centroid x, centroid y) per body; obs_solve_bem_bodies solves it with
+ * circ_rhs[k] as body k's rotation right-hand side and writes its rotation rate to
+ * omega_out[k] (augmented bodies only).  At most 64 rotating bodies (OBS_ERR_UNSUPPORTED). */
+int obs_panels_on_panels_coeff_bodies(obs_context* ctx, int nunk, int accum, int nnodes, const float* nx,
+                                      const float* ny, int npan, const unsigned* idx, int nbodies,
+                                      const int* panel_off, const int* augmented, double* A64, double* geom);
+int obs_solve_bem_bodies(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                         int ns, const float* sx, const float* sy, const float* ss,
+                         int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                         const float* bcn, int nbodies, const int* panel_off, const int* augmented,
+                         const double* circ_rhs, float* vs_out, float* ss_out, double* omega_out,
+                         double* rel_residual);
+
 /*
  * Reverse mode (no counterpart in the reference, which has no adjoint).  Cotangents lu, lv are
  * on the FINALIZED velocities u = fs + (1/2 pi) sum (OBS_FLAG_FINALIZE); gradient outputs are

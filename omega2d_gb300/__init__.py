@@ -401,7 +401,7 @@ class Surfaces:
     """1-D elements (src/Surfaces.h): straight panels between nodes (nx, ny) with node-index
     pairs idx[2k], idx[2k+1]; the fluid is to the left walking node0 -> node1.  vs / ss are the
     vortex / source sheet strengths, bcn the normal-velocity boundary condition, (pu, pv) the
-    panel-centre velocities."""
+    panel-centre velocities; omega the body's rotation rate after a rotation-augmented solve."""
     nx: np.ndarray
     ny: np.ndarray
     idx: np.ndarray
@@ -410,6 +410,7 @@ class Surfaces:
     bcn: np.ndarray | None = None
     pu: np.ndarray = field(default=None)
     pv: np.ndarray = field(default=None)
+    omega: float | None = None   # rotation rate from an augmented solve (solve_bem_bodies)
 
     def __post_init__(self):
         self.nx, self.ny = _own32(self.nx), _own32(self.ny)
@@ -638,21 +639,65 @@ def solve_bem(vort: Points, bdry: Surfaces, fs=(0.0, 0.0), nunk: int = 2, env: E
 
 
 def solve_bem_bodies(vort: Points, bodies, fs=(0.0, 0.0), nunk: int = 2, env: ExecEnv | None = None,
-                     reuse_matrix: bool = False, direct_lu: bool = False) -> float:
-    """solve_bem for several fixed bodies (src/BEMHelper.h:43-260 over a list of boundary
+                     reuse_matrix: bool = False, direct_lu: bool = False, augmented=None, circ_rhs=None) -> float:
+    """solve_bem for several bodies (src/BEMHelper.h:43-260 over a list of boundary
     collections): one system over the joined panel set (join_surfaces), whose matrix is the
     reference's block assembly; sets each body's vs (and ss for nunk == 2) and returns the
-    relative residual.  The reference rebuilds only the blocks of bodies in relative motion
-    (:147-193); here the whole matrix is rebuilt unless reuse_matrix (no body moved), since
-    assembling it costs about 2 % of a BEM step (4096 unknowns: 0.05 ms of 2.9 ms)."""
+    relative residual.  augmented[k] makes body k rotate (src/Coefficients.h:429-572): its
+    rotation row takes circ_rhs[k] as right-hand side and its rotation rate is set as
+    bodies[k].omega.  The reference rebuilds only the blocks of bodies in relative motion
+    (:147-193); here the whole matrix is rebuilt unless reuse_matrix (no body moved, none
+    rotating), since assembling it costs about 2 % of a BEM step (4096 unknowns: 0.05 ms of
+    2.7 ms)."""
     bodies = list(bodies)
     joined, offs = join_surfaces(bodies)
-    rel = solve_bem(vort, joined, fs=fs, nunk=nunk, env=env, reuse_matrix=reuse_matrix, direct_lu=direct_lu)
+    if augmented is None or not any(augmented):
+        rel = solve_bem(vort, joined, fs=fs, nunk=nunk, env=env, reuse_matrix=reuse_matrix, direct_lu=direct_lu)
+        omegas = None
+    else:
+        env = env or ExecEnv()
+        aug = np.ascontiguousarray([1 if a else 0 for a in augmented], np.int32)
+        circ = np.ascontiguousarray(np.zeros(len(bodies)) if circ_rhs is None else circ_rhs, np.float64)
+        if aug.size != len(bodies) or circ.size != len(bodies):
+            raise ValueError("solve_bem_bodies: one augmented flag and one circulation per body")
+        vs = np.zeros(joined.npan, np.float32)
+        ss = np.zeros(joined.npan, np.float32) if nunk == 2 else None
+        omegas = np.zeros(len(bodies))
+        off32 = np.ascontiguousarray(offs, np.int32)
+        rel_c = ctypes.c_double()
+        _check(lib().obs_solve_bem_bodies(env.ctx().handle, ctypes.c_int(nunk), ctypes.c_int(env.accum),
+                                          ctypes.c_int(4 if direct_lu else 0), ctypes.c_double(fs[0]),
+                                          ctypes.c_double(fs[1]), ctypes.c_int(vort.n), _ptr(vort.x), _ptr(vort.y),
+                                          _ptr(vort.s), *joined._geo(), _ptr(joined.bcn), ctypes.c_int(len(bodies)),
+                                          _ptr(off32), _ptr(aug), _ptr(circ), _ptr(vs), _ptr(ss), _ptr(omegas),
+                                          ctypes.byref(rel_c)), "obs_solve_bem_bodies")
+        joined.vs, joined.ss, rel = vs, ss, rel_c.value
     for k, b in enumerate(bodies):
         b.vs = joined.vs[offs[k]:offs[k + 1]].copy()
         if nunk == 2:
             b.ss = joined.ss[offs[k]:offs[k + 1]].copy()
+        if omegas is not None and augmented[k]:
+            b.omega = float(omegas[k])
     return rel
+
+
+def panels_on_panels_coeff_bodies(bodies, augmented, nunk: int = 2, accum: int = COMPENSATED,
+                                  context: Context | None = None):
+    """The BEM matrix of several bodies, some rotating (augmented[k]), over their joined panel
+    set: panel unknowns first, then one rotation unknown per rotating body.  Returns the FP64
+    (rows, cols) array and (area, centroid x, centroid y) per body (rotating bodies)."""
+    ctx = context or default_context()
+    bodies = list(bodies)
+    joined, offs = join_surfaces(bodies)
+    aug = np.ascontiguousarray([1 if a else 0 for a in augmented], np.int32)
+    m = joined.npan * nunk + int(aug.sum())
+    out = np.zeros(m * m)
+    geom = np.zeros(3 * len(bodies))
+    _check(lib().obs_panels_on_panels_coeff_bodies(ctx.handle, ctypes.c_int(nunk), ctypes.c_int(accum),
+                                                   *joined._geo(), ctypes.c_int(len(bodies)),
+                                                   _ptr(np.ascontiguousarray(offs, np.int32)), _ptr(aug), _ptr(out),
+                                                   _ptr(geom)), "obs_panels_on_panels_coeff_bodies")
+    return out.reshape(m, m).T.copy(), geom.reshape(len(bodies), 3)
 
 
 # Convection.h:301-302's cutoff factor for clear_inner_layer

@@ -474,23 +474,72 @@ int obs_solve_gmres_f64(obs_context* ctx, int n, const double* A, const double* 
 
 namespace {
 
-// solve_bem for one body (src/BEMHelper.h:43-260); with `augment`, the system gains the rotation
-// row and column (src/Coefficients.h:429-572) and the right-hand side the circulation value
-// circ_rhs (src/BEMHelper.h:114-135); the extra unknown is the body's rotation rate.
+// Bodies joined in one panel set, some of them rotating (the rotation-augmented BEM).
+struct BodySpec {
+  int nbodies;            // bodies in the panel set, in order
+  const int* panel_off;   // nbodies + 1 panel offsets
+  const int* augmented;   // per body: nonzero adds its rotation row and column
+  const double* circ;     // per body: the right-hand side of its rotation row
+  double* omega;          // per body: receives its rotation rate (augmented bodies only)
+};
+
+int check_bodies(const BodySpec* b, int npan, int* naug) {
+  *naug = 0;
+  if (!b) return OBS_OK;
+  if (b->nbodies < 1 || !b->panel_off || !b->augmented || !b->circ) return OBS_ERR_ARG;
+  if (b->panel_off[0] != 0 || b->panel_off[b->nbodies] != npan) return OBS_ERR_ARG;
+  for (int k = 0; k < b->nbodies; ++k) {
+    if (b->panel_off[k + 1] <= b->panel_off[k]) return OBS_ERR_ARG;
+    if (b->augmented[k]) ++*naug;
+  }
+  return *naug > obs::kMaxAugBodies ? OBS_ERR_UNSUPPORTED : OBS_OK;
+}
+
+// The augmented matrix of bodies joined in the device panel set ps (host copies nx, ny, idx give
+// each rotating body's area and centre, src/Surfaces.h:629-660); geom (optional) receives
+// (area, cx, cy) per body.
+int bodies_augmented_matrix(obs_context* ctx, const PanelSet& ps, int nunk, int accum, int nnodes, const float* nx,
+                            const float* ny, const unsigned* idx, const BodySpec* b, double* dA, double* geom) {
+  obs::AugBodies ab;
+  std::memset(&ab, 0, sizeof(ab));
+  std::vector<float> cx, cy;
+  for (int k = 0; k < b->nbodies; ++k) {
+    double vol, gx, gy;
+    const int p0 = b->panel_off[k], p1 = b->panel_off[k + 1];
+    obs::geom_center_host(nnodes, nx, ny, p1 - p0, idx + 2 * (size_t)p0, &vol, &gx, &gy);
+    if (geom) { geom[3 * k] = vol; geom[3 * k + 1] = gx; geom[3 * k + 2] = gy; }
+    if (!b->augmented[k]) continue;
+    ab.p0[ab.naug] = p0;
+    ab.p1[ab.naug] = p1;
+    ab.vol2[ab.naug] = 2.0 * vol;
+    cx.push_back((float)gx);
+    cy.push_back((float)gy);
+    ++ab.naug;
+  }
+  return obs::run_panels_on_panels_coeff_bodies_augmented(ctx, ps, nunk, accum, ab, cx.data(), cy.data(),
+                                                          b->nbodies, b->panel_off, dA);
+}
+
+// solve_bem (src/BEMHelper.h:43-260) over one panel set: one body, or several joined (their
+// matrix is the reference's block assembly).  Each rotating body (`bodies`) adds a rotation row
+// and column (src/Coefficients.h:429-572) and the circulation value of its right-hand side
+// (src/BEMHelper.h:114-135); the extra unknowns are the rotation rates, after the panel unknowns.
 int solve_bem_impl(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
                    int ns, const float* sx, const float* sy, const float* ss,
                    int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
-                   bool augment, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
-                   double* rel_residual) {
+                   const BodySpec* bodies, float* vs_out, float* ss_out, double* rel_residual) {
   if (!ctx || (nunk != 1 && nunk != 2) || npan <= 0 || !vs_out || (nunk == 2 && !ss_out)) return OBS_ERR_ARG;
   if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
   int s = check_panels(nnodes, nx, ny, npan, idx);
   if (s) return s;
   if (ns < 0 || (ns > 0 && (!sx || !sy || !ss))) return OBS_ERR_ARG;
   if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  int naug = 0;
+  if ((s = check_bodies(bodies, npan, &naug))) return s;
   if ((s = obs::bind(ctx))) return s;
+  const bool augment = naug > 0;
   const int nb = npan * nunk;               // panel unknowns
-  const int n = nb + (augment ? 1 : 0);     // system order
+  const int n = nb + naug;                  // system order
   const size_t nn = (size_t)n * n;
   const bool use_lu = (flags & OBS_BEM_DIRECT_LU) != 0;
   // ctx->dense: A (FP64, kept for reuse and residuals) | LU factors | pivots; bem_n > 0 marks a
@@ -535,8 +584,11 @@ int solve_bem_impl(obs_context* ctx, int nunk, int accum, int flags, double fsx,
   if (!s) s = obs::run_vels_to_rhs(ctx, ps, nunk, dpu, dpv, dbc, nullptr, drhs);
   if (s) return s;
   if (augment) {
-    e = cudaMemcpyAsync(drhs + nb, &circ_rhs, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // circ_rhs is a stack value
+    std::vector<double> circ;
+    for (int k = 0; k < bodies->nbodies; ++k)
+      if (bodies->augmented[k]) circ.push_back(bodies->circ[k]);
+    e = cudaMemcpyAsync(drhs + nb, circ.data(), circ.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);   // circ is a host temporary
     if (e != cudaSuccess) return obs::cuda_status(e);
   }
   const size_t lu_bytes = use_lu ? nn * sizeof(double) : 0;
@@ -550,10 +602,12 @@ int solve_bem_impl(obs_context* ctx, int nunk, int accum, int flags, double fsx,
   double* lu = ctx->dense.as<double>(nn * sizeof(double));
   int* piv = ctx->dense.as<int>(nn * sizeof(double) + lu_bytes);
   if (!reuse) {
-    if (augment) {
+    if (augment && bodies->nbodies == 1) {
       double vol, cx, cy;
       obs::geom_center_host(nnodes, nx, ny, npan, idx, &vol, &cx, &cy);
       s = obs::run_panels_on_panels_coeff_augmented(ctx, ps, nunk, accum, vol, cx, cy, dA);
+    } else if (augment) {
+      s = bodies_augmented_matrix(ctx, ps, nunk, accum, nnodes, nx, ny, idx, bodies, dA, nullptr);
     } else {
       s = obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
     }
@@ -595,7 +649,11 @@ int solve_bem_impl(obs_context* ctx, int nunk, int accum, int flags, double fsx,
       vs_out[i] = (float)hx[i];
     }
   }
-  if (augment && omega_out) *omega_out = hx[nb];
+  if (augment && bodies->omega) {
+    int a = 0;
+    for (int k = 0; k < bodies->nbodies; ++k)
+      if (bodies->augmented[k]) bodies->omega[k] = hx[nb + a++];
+  }
   return OBS_OK;
 }
 
@@ -608,8 +666,54 @@ int obs_solve_bem(obs_context* ctx, int nunk, int accum, int flags, double fsx, 
                   int ns, const float* sx, const float* sy, const float* ss,
                   int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx, const float* bcn,
                   float* vs_out, float* ss_out, double* rel_residual) {
-  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, false, 0.0,
-                        vs_out, ss_out, nullptr, rel_residual);
+  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, nullptr,
+                        vs_out, ss_out, rel_residual);
+}
+
+int obs_solve_bem_bodies(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
+                         int ns, const float* sx, const float* sy, const float* ss,
+                         int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
+                         const float* bcn, int nbodies, const int* panel_off, const int* augmented,
+                         const double* circ_rhs, float* vs_out, float* ss_out, double* omega_out,
+                         double* rel_residual) {
+  const BodySpec b{nbodies, panel_off, augmented, circ_rhs, omega_out};
+  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny,
+                        npan, idx, bcn, &b, vs_out, ss_out, rel_residual);
+}
+
+int obs_panels_on_panels_coeff_bodies(obs_context* ctx, int nunk, int accum, int nnodes, const float* nx,
+                                      const float* ny, int npan, const unsigned* idx, int nbodies,
+                                      const int* panel_off, const int* augmented, double* A64, double* geom) {
+  if (!ctx || (nunk != 1 && nunk != 2) || npan <= 0 || !A64) return OBS_ERR_ARG;
+  if (accum != OBS_PLAIN_F32 && accum != OBS_COMPENSATED) return OBS_ERR_ARG;
+  int s = check_panels(nnodes, nx, ny, npan, idx);
+  if (s) return s;
+  if ((s = check_host_idx(nnodes, npan, idx))) return s;
+  std::vector<double> zero((size_t)std::max(nbodies, 0), 0.0);
+  const BodySpec b{nbodies, panel_off, augmented, zero.data(), nullptr};
+  int naug = 0;
+  if ((s = check_bodies(&b, npan, &naug))) return s;
+  if ((s = obs::bind(ctx))) return s;
+  const int n = npan * nunk + naug;
+  const size_t nn = (size_t)n * n;
+  Stage g(ctx);
+  for (int k = 0; k < 2; ++k) g.reserve((size_t)nnodes * 4);
+  g.reserve((size_t)npan * 8);
+  g.reserve(nn * 8);
+  if ((s = g.commit())) return s;
+  const float* dnx = g.take(nx, nnodes);
+  const float* dny = g.take(ny, nnodes);
+  const unsigned* didx = g.take(idx, 2 * (size_t)npan);
+  double* dA = g.take<double>(nullptr, nn);
+  if (g.err) return obs::cuda_status(g.err);
+  PanelSet ps{nnodes, dnx, dny, npan, didx};
+  std::vector<double> hg(3 * (size_t)nbodies);
+  s = naug ? bodies_augmented_matrix(ctx, ps, nunk, accum, nnodes, nx, ny, idx, &b, dA, hg.data())
+           : obs::run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, dA);
+  if (!s) s = obs::take_device_status(ctx);
+  if (s) return s;
+  if (geom && naug) std::memcpy(geom, hg.data(), hg.size() * sizeof(double));
+  return copy_back(ctx, {{A64, {dA, nn * 8}}});
 }
 
 int obs_solve_bem_augmented(obs_context* ctx, int nunk, int accum, int flags, double fsx, double fsy,
@@ -617,8 +721,11 @@ int obs_solve_bem_augmented(obs_context* ctx, int nunk, int accum, int flags, do
                             int nnodes, const float* nx, const float* ny, int npan, const unsigned* idx,
                             const float* bcn, double circ_rhs, float* vs_out, float* ss_out, double* omega_out,
                             double* rel_residual) {
-  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, true,
-                        circ_rhs, vs_out, ss_out, omega_out, rel_residual);
+  const int one = 1;
+  const int off[2] = {0, npan};
+  const BodySpec b{1, off, &one, &circ_rhs, omega_out};
+  return solve_bem_impl(ctx, nunk, accum, flags, fsx, fsy, ns, sx, sy, ss, nnodes, nx, ny, npan, idx, bcn, &b,
+                        vs_out, ss_out, rel_residual);
 }
 
 int obs_panels_on_panels_coeff_augmented(obs_context* ctx, int nunk, int accum, int nnodes, const float* nx,

@@ -34,6 +34,21 @@ void geom_center_host(int nnodes, const float* nx, const float* ny, int npan, co
                       double* cx, double* cy);
 int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, int nunk, int accum, double vol,
                                          double cx, double cy, double* Aa);
+// Several bodies joined in one panel set, some rotating: panel unknowns first, then one rotation
+// unknown per augmented body (panel range [p0, p1) of the joined set, 2 * area); cx, cy: the
+// augmented bodies' centres; panel_off[0..nbodies]: every body's panel range (each body is its
+// own target for the unit-rotation velocity, so its collocation spacing follows its own first
+// panel).  Aa receives the (nunk * npan + naug)^2 column-major matrix.
+constexpr int kMaxAugBodies = 64;
+struct AugBodies {
+  int naug;
+  int p0[kMaxAugBodies];
+  int p1[kMaxAugBodies];
+  double vol2[kMaxAugBodies];
+};
+int run_panels_on_panels_coeff_bodies_augmented(obs_context* ctx, const PanelSet& ps, int nunk, int accum,
+                                                const AugBodies& ab, const float* cx, const float* cy,
+                                                int nbodies, const int* panel_off, double* Aa);
 int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const PanelSet& targ, int nunk, int self,
                                float* A32, double* A64);
 int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,

@@ -221,6 +221,89 @@ int run_panels_on_panels_coeff_augmented(obs_context* ctx, const PanelSet& ps, i
   return cuda_status(cudaGetLastError());
 }
 
+// Several bodies in one system, some of them rotating (the reference's block assembly,
+// src/BEMHelper.h:166-221 with src/Coefficients.h:429-572 per block): the panel unknowns of the
+// joined panel set first (An, nunk * npan), then one rotation unknown per augmented body a --
+//   row a   : the panel lengths of body a in its vortex-strength columns, 0 in every other
+//             panel column; 2 * area(a) on the diagonal, 0 for the other rotation columns;
+//   column a: the velocity of body a's unit-rotation sheet at every panel of the joined set
+//             (panels_affect_panels, finalized with zero freestream), along each panel's
+//             tangent (and normal for the source unknowns).
+__global__ void augment_bodies_kernel(const double* __restrict__ An, int np, int nunk, const float* __restrict__ nx,
+                                      const float* __restrict__ ny, int nnodes, const unsigned* __restrict__ idx,
+                                      int npan, const float* __restrict__ pu, const float* __restrict__ pv,
+                                      const AugBodies ab, double* __restrict__ Aa, int* status) {
+  const int n = np + ab.naug;
+  const size_t total = (size_t)n * n;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / n), i = (int)(k % n);
+    double v;
+    if (i < np && j < np) {
+      v = An[(size_t)j * np + i];
+    } else if (j < np) {
+      const int a = i - np;
+      const int pj = (nunk == 1) ? j : j / 2;
+      const bool mine = pj >= ab.p0[a] && pj < ab.p1[a] && (nunk == 1 || (j % 2) == 0);
+      v = mine ? (double)panel_geom(nx, ny, idx, nnodes, pj, status).len : 0.0;
+    } else if (i < np) {
+      const int a = j - np;
+      const int pi = (nunk == 1) ? i : i / 2;
+      const PanelGeom g = panel_geom(nx, ny, idx, nnodes, pi, status);
+      const float tx = g.ny, ty = -g.nx;   // tangent from the normal (n = (-t_y, t_x))
+      const bool tang = (nunk == 1) || (i % 2) == 0;
+      const float u = pu[(size_t)a * npan + pi], w = pv[(size_t)a * npan + pi];
+      v = tang ? (double)(u * tx + w * ty) : (double)(u * g.nx + w * g.ny);
+    } else {
+      v = (i == j) ? ab.vol2[i - np] : 0.0;
+    }
+    Aa[k] = v;
+  }
+}
+
+int run_panels_on_panels_coeff_bodies_augmented(obs_context* ctx, const PanelSet& ps, int nunk, int accum,
+                                                const AugBodies& ab, const float* cx, const float* cy,
+                                                int nbodies, const int* panel_off, double* Aa) {
+  const int np = ps.npan * nunk;
+  const size_t N = (size_t)ps.npan;
+  const size_t nn = (size_t)np * np;
+  // state: the collocation scratch of panels_affect_panels | An (np^2 doubles) | unit strengths
+  // vs, ss | induced pu, pv per augmented body
+  const size_t base = (pap_scratch_bytes(ps.npan) + 255) & ~(size_t)255;
+  int s = ctx->state.ensure(base + nn * 8 + (2 * N + 2 * N * (size_t)ab.naug) * 4 + 1024, ctx->stream);
+  if (s) return s;
+  double* An = reinterpret_cast<double*>(ctx->state.as<char>() + base);
+  float* vs = reinterpret_cast<float*>(An + nn);
+  float* ss = vs + N;
+  float* pu = ss + N;
+  float* pv = pu + N * ab.naug;
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaMemsetAsync(pu, 0, 2 * N * ab.naug * 4, st);
+  if (e != cudaSuccess) return cuda_status(e);
+  for (int a = 0; a < ab.naug; ++a) {
+    const int nb = ab.p1[a] - ab.p0[a];
+    const PanelSet body{ps.nnodes, ps.nx, ps.ny, nb, ps.idx + 2 * (size_t)ab.p0[a]};
+    unit_rot_strengths_kernel<<<(nb + 255) / 256, 256, 0, st>>>(body.nx, body.ny, body.nnodes, body.idx, nb, cx[a],
+                                                               cy[a], vs, ss, ctx->d_status);
+    ctx->launches++;
+    // the unit-rotation velocity of body a at every panel, finalized with zero freestream, one
+    // target body at a time: a body's collocation points are spaced by its own first panel
+    // (src/Surfaces.h:846-865 through src/Influence.h:783)
+    for (int t = 0; t < nbodies; ++t) {
+      const int q0 = panel_off[t], q1 = panel_off[t + 1];
+      if (q1 <= q0) continue;
+      const PanelSet targ{ps.nnodes, ps.nx, ps.ny, q1 - q0, ps.idx + 2 * (size_t)q0};
+      if ((s = run_panels_affect_panels(ctx, body, vs, ss, accum, OBS_FLAG_FINALIZE, 0.0, 0.0, targ,
+                                        pu + N * a + q0, pv + N * a + q0)))
+        return s;
+    }
+  }
+  if ((s = run_panels_on_panels_coeff(ctx, ps, ps, nunk, 1, nullptr, An))) return s;
+  augment_bodies_kernel<<<2 * ctx->num_sms, 256, 0, st>>>(An, np, nunk, ps.nx, ps.ny, ps.nnodes, ps.idx, ps.npan, pu,
+                                                          pv, ab, Aa, ctx->d_status);
+  ctx->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
 int run_panels_affect_panels(obs_context* ctx, const PanelSet& src, const float* vs, const float* ss, int accum,
                              int flags, double fsx, double fsy, const PanelSet& targ, float* pu, float* pv) {
   if (src.npan == 0 || targ.npan == 0) return OBS_OK;

@@ -306,6 +306,38 @@ int ref_panels_on_panels_coeff_d(int nnodes, const double* nx, const double* ny,
 }
 
 // off-diagonal block: distinct source and target collections (no self term)
+// One off-diagonal block of a multi-body system whose bodies both rotate (augmented BEM), the
+// way solve_bem assembles it (src/BEMHelper.h:183-216): the source body's unit-rotation sheet
+// acts on the target's panels (panels_affect_panels, finalized with zero freestream), then
+// panels_on_panels_coeff(src, targ) adds the source's augmented column and the target's
+// augmented row (src/Coefficients.h:429-572).  Output: (2 tnp + 1) x (2 snp + 1), column-major.
+int ref_panels_on_panels_coeff_augmented_pair_f(int snn, const float* snx, const float* sny, int snp,
+                                                const unsigned* sidx, int tnn, const float* tnx, const float* tny,
+                                                int tnp, const unsigned* tidx, float* out) {
+  Quiet q;
+  auto make = [](int nn, const float* nx, const float* ny, int np, const unsigned* idx) {
+    std::vector<float> xy(2 * (size_t)nn);
+    for (int i = 0; i < nn; ++i) { xy[2*i] = nx[i]; xy[2*i+1] = ny[i]; }
+    std::vector<Int> id(idx, idx + 2 * (size_t)np);
+    std::vector<float> val(2 * (size_t)np, 0.0f);
+    ElementPacket<float> pk(xy, id, val, (size_t)np, 1);
+    return Surfaces<float>(pk, reactive, fixed, std::make_shared<Body>());
+  };
+  Surfaces<float> src = make(snn, snx, sny, snp, sidx);
+  Surfaces<float> targ = make(tnn, tnx, tny, tnp, tidx);
+  src.set_geom_center();
+  targ.set_geom_center();
+  targ.zero_vels();
+  src.zero_strengths();
+  src.add_unit_rot_strengths();
+  panels_affect_panels<float, double>(src, targ, ResultsType(velonly), ExecEnv(true, direct, cpu_x86));
+  src.zero_strengths();
+  targ.finalize_vels(std::array<double, Dimensions>({0.0, 0.0}));
+  Vector<float> c = panels_on_panels_coeff<float>(src, targ);
+  std::copy(c.begin(), c.end(), out);
+  return (int)c.size();
+}
+
 int ref_panels_on_panels_coeff_pair_f(int snn, const float* snx, const float* sny, int snp, const unsigned* sidx,
                                       int tnn, const float* tnx, const float* tny, int tnp, const unsigned* tidx,
                                       float* out) {

@@ -201,6 +201,48 @@ def make_bodies(out):
     np.savez_compressed(out, **d)
 
 
+def make_bodies_aug(out):
+    """Two rotating bodies in one BEM system, assembled as solve_bem does (src/BEMHelper.h:
+    166-221): block (t, s) is panels_on_panels_coeff of body s on body t with both augmented
+    (src/Coefficients.h:429-572; the source's unit-rotation sheet acting on the target's panels
+    supplies the augmented column), each body's rows and columns followed by its rotation row
+    and column.  Stored in the reference's order with the bodies' volumes."""
+    import ctypes
+    rng = np.random.default_rng(20240609)
+    bodies = [circle_panels(36)]
+    th = -2.0 * np.pi * np.sort(rng.uniform(0, 1, 24))
+    rad = 0.3 + 0.06 * np.sin(2 * th)
+    bodies.append(((1.3 + rad * np.cos(th)).astype(np.float32), (0.4 + rad * np.sin(th)).astype(np.float32),
+                   np.stack([np.arange(24), (np.arange(24) + 1) % 24], 1).ravel().astype(np.uint32)))
+    ref = po.Reference(po.V2)
+    d = {}
+    rows = []
+    for ti, (tnx, tny, tidx) in enumerate(bodies):
+        blocks = []
+        tn = tidx.size // 2
+        for si, (snx, sny, sidx) in enumerate(bodies):
+            sn = sidx.size // 2
+            if si == ti:
+                m = 2 * sn + 1
+                A = np.zeros(m * m, np.float32)
+                geom = np.zeros(4)
+                ref.lib.ref_panels_on_panels_coeff_augmented_f(ctypes.c_int(snx.size), po._p(snx), po._p(sny),
+                                                               ctypes.c_int(sn), po._p(sidx), po._p(A), po._p(geom))
+                blocks.append(A.reshape(m, m).T)
+                d[f"vol{si}"] = geom[:1]
+            else:
+                A = np.zeros((2 * tn + 1) * (2 * sn + 1), np.float32)
+                ref.lib.ref_panels_on_panels_coeff_augmented_pair_f(
+                    ctypes.c_int(snx.size), po._p(snx), po._p(sny), ctypes.c_int(sn), po._p(sidx),
+                    ctypes.c_int(tnx.size), po._p(tnx), po._p(tny), ctypes.c_int(tn), po._p(tidx), po._p(A))
+                blocks.append(A.reshape(2 * sn + 1, 2 * tn + 1).T)
+        rows.append(np.concatenate(blocks, axis=1))
+    d["A"] = np.concatenate(rows, axis=0)
+    for k, (nx, ny, idx) in enumerate(bodies):
+        d[f"nx{k}"], d[f"ny{k}"], d[f"idx{k}"] = nx, ny, idx
+    np.savez_compressed(out, **d)
+
+
 def star_panels(arms=5, r_out=0.5, r_in=0.25, center=(0.0, 0.0)):
     """A clockwise star polygon (concave corners: ties between panels and nodes)."""
     k = 2 * arms
@@ -291,6 +333,7 @@ def main():
     make_bodies(os.path.join(HERE, "bodies.npz"))
     make_clear(os.path.join(HERE, "clear.npz"))
     make_pins(os.path.join(HERE, "pins.npz"))
+    make_bodies_aug(os.path.join(HERE, "bodies_aug.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

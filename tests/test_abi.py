@@ -125,3 +125,33 @@ def test_tree_entry_points_check_arguments(engine_lib):
     assert sw(2, ctypes.c_double(0.5), 33) == -1
     assert sw(2, ctypes.c_double(0.0), 0) == 0             # defaults
     assert sw(1, ctypes.c_double(0.0), 0) == 0             # back to direct sums
+
+
+def test_bodies_entry_points_check_arguments(engine_lib):
+    """obs_panels_on_panels_coeff_bodies and obs_solve_bem_bodies reject a null context, panel
+    offsets that do not start at 0, end at npan and increase, and missing body arrays, before
+    they bind a device."""
+    nx = np.array([1, 0, -1, 0, 3, 2, 3], np.float32)
+    ny = np.array([0, -1, 0, 1, 0, 0, 1], np.float32)
+    idx = np.array([0, 1, 1, 2, 2, 3, 3, 0, 4, 5, 5, 6, 6, 4], np.uint32)
+    out = np.zeros(64, np.float64)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    aug = np.array([1, 1], np.int32)
+    h = ctypes.c_void_p(1)                      # never dereferenced: the checks come first
+    coeff = engine_lib.obs_panels_on_panels_coeff_bodies
+
+    def call(ctx, off, augp=P(aug)):
+        return coeff(ctx, 2, 1, 7, P(nx), P(ny), 7, P(idx), 2, P(off), augp, P(out), None)
+    good = np.array([0, 4, 7], np.int32)
+    assert call(None, good) == -1
+    for bad in ([1, 4, 7], [0, 4, 6], [0, 4, 4], [0, 8, 7]):
+        assert call(h, np.array(bad, np.int32)) == -1, bad
+    assert call(h, good, None) == -1
+    solve = engine_lib.obs_solve_bem_bodies
+    z = np.zeros(8, np.float32)
+    circ = np.zeros(2, np.float64)
+    D = ctypes.c_double
+    assert solve(None, 2, 1, 0, D(0), D(0), 0, None, None, None, 7, P(nx), P(ny), 7, P(idx), None, 2, P(good),
+                 P(aug), P(circ), P(z), P(z), P(circ), None) == -1
+    assert solve(h, 2, 1, 0, D(0), D(0), 0, None, None, None, 7, P(nx), P(ny), 7, P(idx), None, 2,
+                 P(np.array([0, 7, 7], np.int32)), P(aug), P(circ), P(z), P(z), P(circ), None) == -1

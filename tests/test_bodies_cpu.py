@@ -85,3 +85,58 @@ def test_solve_bem_bodies_splits_strengths_by_body(monkeypatch):
     og.solve_bem_bodies(vort, [a, b], nunk=1, direct_lu=True)
     assert calls[-1] == (16, 1, False, True)
     np.testing.assert_array_equal(b.vs, np.arange(10, 16))
+
+
+def _geom_center(nx, ny, idx):
+    """Area and centroid of a closed body from the triangles (origin, node j, node j+1)
+    (src/Surfaces.h:623-677), in FP64."""
+    x0, y0 = nx[idx[0::2]].astype(np.float64), ny[idx[0::2]].astype(np.float64)
+    x1, y1 = nx[idx[1::2]].astype(np.float64), ny[idx[1::2]].astype(np.float64)
+    px, py = x1 - x0, y1 - y0
+    a, b, c = np.hypot(x0, y0), np.hypot(px, py), np.hypot(x1, y1)
+    hs = 0.5 * (a + b + c)
+    ar = np.sqrt(np.maximum(hs * (hs - a) * (hs - b) * (hs - c), 0.0))
+    ar = np.where(y0 * px - x0 * py < 0.0, -ar, ar)
+    return ar.sum(), (ar * (x0 + x1) / 3.0).sum() / ar.sum(), (ar * (y0 + y1) / 3.0).sum() / ar.sum()
+
+
+def test_restatement_rotating_bodies_vs_golden(restatement, golden):
+    """The rotation rows and columns of two rotating bodies in one system (golden bodies_aug.npz,
+    the reference's block assembly, src/BEMHelper.h:166-221 with src/Coefficients.h:429-572),
+    restated: column s is body s's unit-rotation sheet (src/Surfaces.h:570-620) acting on each
+    body's panels through that body's own collocation points (src/Influence.h:775-795: the
+    target's represent_as_particles spaces them by the target's first panel), over 2 pi,
+    projected on tangent and normal; row t is body t's panel lengths under its vortex unknowns;
+    the corner is 2 * area on the diagonal, zero across bodies."""
+    g = golden("bodies_aug")
+    bodies = [(g[f"nx{k}"], g[f"ny{k}"], g[f"idx{k}"]) for k in range(2)]
+    sizes = [b[2].size // 2 for b in bodies]
+    start = [0, 2 * sizes[0] + 1]                            # reference order: panels, then rotation
+    R = g["A"].astype(np.float64)
+    for s, (snx, sny, sidx) in enumerate(bodies):
+        vol, cx, cy = _geom_center(snx, sny, sidx)
+        assert abs(vol - g[f"vol{s}"][0]) < 1e-6 * abs(vol)
+        x0, y0, x1, y1 = snx[sidx[0::2]], sny[sidx[0::2]], snx[sidx[1::2]], sny[sidx[1::2]]
+        L = np.hypot(x1 - x0, y1 - y0)
+        ui, vi = -(0.5 * (y0 + y1) - cy), 0.5 * (x0 + x1) - cx
+        tx, ty = (x1 - x0) / L, (y1 - y0) / L
+        vs, ss = -(ui * tx + vi * ty), -(ui * ty - vi * tx)
+        col = start[s] + 2 * sizes[s]
+        for t, (tnx, tny, tidx) in enumerate(bodies):
+            pu, pv = restatement.panels_affect_panels(snx, sny, sidx, vs, ss, tnx, tny, tidx)
+            pu, pv = pu / (2 * np.pi), pv / (2 * np.pi)
+            ax, ay = tnx[tidx[0::2]], tny[tidx[0::2]]
+            bx, by = tnx[tidx[1::2]], tny[tidx[1::2]]
+            Lt = np.hypot(bx - ax, by - ay)
+            ttx, tty = (bx - ax) / Lt, (by - ay) / Lt
+            want = np.stack([pu * ttx + pv * tty, pu * -tty + pv * ttx], 1).ravel()
+            got = R[start[t]:start[t] + 2 * sizes[t], col]
+            assert rel_err(got, want) < 1e-5, (s, t)
+            # the rotation row of body t under body s's unknowns
+            row = R[start[t] + 2 * sizes[t], start[s]:start[s] + 2 * sizes[s]]
+            if s == t:
+                np.testing.assert_allclose(row[0::2], L, rtol=1e-6)
+                assert not row[1::2].any()
+                assert R[col, col] == np.float32(2 * g[f"vol{s}"][0])
+            else:
+                assert not row.any() and R[start[t] + 2 * sizes[t], col] == 0.0

@@ -509,3 +509,73 @@ def test_clear_inner_layer_shared_node_and_tiles_vs_oracle(ctx, restatement):
             np.testing.assert_array_equal(p.y, oy)
             np.testing.assert_array_equal(p.s, os_)
             assert nc == onc and nc > 0
+
+
+def _two_rotating_bodies(golden):
+    g = golden("bodies_aug")
+    bodies = [og.Surfaces(g[f"nx{k}"], g[f"ny{k}"], g[f"idx{k}"]) for k in range(2)]
+    n0, n1 = bodies[0].npan, bodies[1].npan
+    npu = 2 * (n0 + n1)
+    # reference order: body 0's panel unknowns, its rotation; body 1's, its rotation
+    perm = np.concatenate([np.arange(2 * n0), [npu], np.arange(2 * n0, npu), [npu + 1]])
+    return g, bodies, perm
+
+
+def test_bodies_augmented_matrix_matches_reference(ctx, golden):
+    """Two rotating bodies in one system against the reference's own block assembly
+    (src/BEMHelper.h:166-221, each block from src/Coefficients.h:155-572; golden
+    bodies_aug.npz), after permuting the engine's order (panels first, rotations last)."""
+    g, bodies, perm = _two_rotating_bodies(golden)
+    A, geom = og.panels_on_panels_coeff_bodies(bodies, [True, True], context=ctx)
+    R = g["A"].astype(np.float64)
+    B = A[np.ix_(perm, perm)]
+    for k in range(2):
+        assert abs(geom[k, 0] - g[f"vol{k}"][0]) < 1e-6 * abs(geom[k, 0])
+    rot = [2 * bodies[0].npan, R.shape[0] - 1]
+    pan = np.setdiff1d(np.arange(R.shape[0]), rot)
+    # the reference forms every block in FP32; on this pair of bodies its float assembly is
+    # 1.2e-5 off FP64 (test_two_bodies_matrix_matches_reference_block_assembly)
+    assert rel_err(R[np.ix_(pan, pan)], B[np.ix_(pan, pan)]) < 2e-5
+    assert rel_err(R[np.ix_(pan, rot)], B[np.ix_(pan, rot)]) < 2e-5           # unit-rotation columns
+    np.testing.assert_allclose(B[rot, :], R[rot, :], rtol=0, atol=1e-6 * np.max(np.abs(R[rot, :])))
+
+
+@pytest.mark.parametrize("augmented", [(True, True), (True, False)])
+def test_bodies_augmented_solve(ctx, golden, restatement, augmented):
+    """The solve of two bodies, one or both rotating, against an FP64 solve of the reference's
+    matrix (golden; a non-rotating body drops its rotation row and column) with the right-hand
+    side from the FP64 restatement and the prescribed circulations."""
+    g, bodies, perm = _two_rotating_bodies(golden)
+    rng = np.random.default_rng(41)
+    n = 5000
+    r = np.sqrt(rng.uniform(0.55 ** 2, 4.0, n))
+    t = rng.uniform(0, 2 * np.pi, n)
+    x, y = r * np.cos(t), r * np.sin(t)
+    keep = np.hypot(x - 1.3, y - 0.4) > 0.45
+    x, y = x[keep].astype(np.float32), y[keep].astype(np.float32)
+    s = rng.normal(0, 1e-2, x.size).astype(np.float32)
+    circ = [0.3, -0.2]
+    rel = og.solve_bem_bodies(og.Points(x, y, np.full(x.size, 0.01, np.float32), s), bodies, fs=(1.0, 0.0),
+                              nunk=2, env=og.ExecEnv(accum=og.COMPENSATED, context=ctx), augmented=list(augmented),
+                              circ_rhs=circ)
+    assert rel < 1e-12
+    joined, offs = og.join_surfaces([og.Surfaces(b.nx, b.ny, b.idx) for b in bodies])
+    pu, pv = restatement.points_affect_panels(x, y, s, joined.nx, joined.ny, joined.idx, fp64=True)
+    pu, pv = 1.0 + pu / (2 * np.pi), pv / (2 * np.pi)
+    rhs_p = restatement.vels_to_rhs_panels(2, joined.nx, joined.ny, joined.idx, pu, pv, fp64=True)
+    npu = rhs_p.size
+    rhs = np.concatenate([rhs_p, circ])[perm]
+    R = g["A"].astype(np.float64)
+    keep_rows = np.array([not (p >= npu and not augmented[p - npu]) for p in perm])
+    xr = np.linalg.solve(R[np.ix_(keep_rows, keep_rows)], rhs[keep_rows])
+    full = np.full(perm.size, np.nan)
+    full[keep_rows] = xr
+    unperm = np.empty_like(full)
+    unperm[perm] = full
+    got = np.stack([np.concatenate([b.vs for b in bodies]), np.concatenate([b.ss for b in bodies])], 1).ravel()
+    assert rel_err(unperm[:npu], got) < 3e-4
+    for k in range(2):
+        if augmented[k]:
+            assert abs(bodies[k].omega - unperm[npu + k]) < 3e-4 * max(1.0, abs(unperm[npu + k]))
+        else:
+            assert bodies[k].omega is None
