@@ -176,22 +176,29 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const bool bin_s = gauss_packed && (order == OBS_ORDER_BINNED || (order == OBS_ORDER_AUTO && big));
   const bool same_pts = bin_t && bin_s && rq.sx == rq.tx && rq.sy == rq.ty && rq.ns == rq.nt;
 
-  // ---- work buffer: header | packed sources | partials | target order (perm, x, y, r) |
-  //      source order (perm) | sort scratch
+  // the packed velocity kernel reduces its splits itself (P2PArgs::blkcnt): partial rows padded
+  // to whole target blocks, one arrival count per block
+  const bool fused = packed && res == RES_VEL && nsplit > 1;
+  const size_t pst = fused ? (size_t)ntb * tb : (size_t)rq.nt;
+
+  // ---- work buffer: header | block counts | packed sources | partials | target order
+  //      (perm, x, y, r) | source order (perm) | sort scratch
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t hdr = 256;
+  const size_t cnt_bytes = fused ? al((size_t)ntb * sizeof(int)) : 0;
   const size_t src_bytes = (size_t)nst * SRC_TILE * sizeof(float4) * (packed ? PK_ELEM : 1);
-  const size_t part_bytes = nsplit > 1 ? al((size_t)nc * nsplit * rq.nt * (comp ? sizeof(double) : sizeof(float))) : 0;
+  const size_t part_bytes = nsplit > 1 ? al((size_t)nc * nsplit * pst * (comp ? sizeof(double) : sizeof(float))) : 0;
   const size_t tvec = al((size_t)rq.nt * sizeof(float));
   const size_t svec = (bin_s && !same_pts) ? al((size_t)rq.ns * sizeof(int)) : 0;
   const size_t sort_bytes = (bin_t || bin_s) ? bin_scratch_bytes(std::max(bin_t ? rq.nt : 0, bin_s ? rq.ns : 0)) : 0;
   const size_t bin_bytes = (bin_t ? 4 * tvec : 0) + svec + sort_bytes;
-  int s = ctx->work.ensure(hdr + src_bytes + part_bytes + bin_bytes, st);
+  int s = ctx->work.ensure(hdr + cnt_bytes + src_bytes + part_bytes + bin_bytes, st);
   if (s) return s;
   WorkHeader* h = ctx->work.as<WorkHeader>(0);
-  float4* src = ctx->work.as<float4>(hdr);
-  void* part = part_bytes ? ctx->work.as<char>(hdr + src_bytes) : nullptr;
-  size_t off = hdr + src_bytes + part_bytes;
+  int* blkcnt = fused ? ctx->work.as<int>(hdr) : nullptr;
+  float4* src = ctx->work.as<float4>(hdr + cnt_bytes);
+  void* part = part_bytes ? ctx->work.as<char>(hdr + cnt_bytes + src_bytes) : nullptr;
+  size_t off = hdr + cnt_bytes + src_bytes + part_bytes;
   int* tperm = nullptr;
   float *bx = nullptr, *by = nullptr, *br = nullptr;
   if (bin_t) {
@@ -209,7 +216,7 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   void* sort_scratch = sort_bytes ? ctx->work.as<char>(off) : nullptr;
 
   timing_begin(ctx);
-  e = cudaMemsetAsync(h, 0, sizeof(WorkHeader), st);
+  e = cudaMemsetAsync(h, 0, fused ? hdr + cnt_bytes : sizeof(WorkHeader), st);
   if (e != cudaSuccess) return cuda_status(e);
   {
     int nl = 0;
@@ -260,13 +267,14 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   a.direct = nsplit == 1;
   a.finalize = (rq.flags & OBS_FLAG_FINALIZE) ? 1 : 0;
   a.fsx = rq.fsx; a.fsy = rq.fsy;
+  a.blkcnt = blkcnt;
 
   timing_main_begin(ctx);
   e = launch(&a, grid, nullptr);
   ctx->launches++;
   timing_main_end(ctx);
   if (e != cudaSuccess) return cuda_status(e);
-  if (nsplit > 1) {
+  if (nsplit > 1 && !fused) {
     e = p2p_reduce(res, comp, a, st);
     ctx->launches++;
     if (e != cudaSuccess) return cuda_status(e);

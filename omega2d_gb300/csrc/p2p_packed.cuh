@@ -24,6 +24,8 @@
 // accumulation arithmetic.
 #pragma once
 
+#include <type_traits>
+
 #include "p2p_kernel.cuh"
 
 namespace obs {
@@ -229,6 +231,39 @@ __device__ __forceinline__ void general_block(const float4* __restrict__ blk, co
   }
 }
 
+// The last split of target block tb to finish: sum the block's partials in split order (the
+// order of p2p_reduce_kernel, so the bits do not depend on which split arrived last), write the
+// targets, then drop the consumed partial lines from L2 (discard.global.L2: no write-back), so
+// the partials stay an L2-resident exchange instead of HBM traffic.
+template <bool COMP, int TB>
+__device__ __noinline__ void split_block_reduce(const P2PArgs& a, int tb, size_t pst) {
+  using T = typename std::conditional<COMP, double, float>::type;
+  static_assert((TB * sizeof(T)) % 128 == 0, "a block's partial row is whole L2 lines");
+  const T* part = static_cast<const T*>(a.part);
+  for (int j = threadIdx.x; j < TB; j += blockDim.x) {
+    const int i = tb * TB + j;
+    if (i >= a.nt) break;
+    double c[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const T* p = part + (size_t)q * a.nsplit * pst + i;
+      T s = 0;
+      for (int k = 0; k < a.nsplit; ++k) s += __ldcg(p + (size_t)k * pst);
+      c[q] = (double)s;
+    }
+    store_target<RES_VEL>(a, i, c);
+  }
+  __syncthreads();
+  constexpr int LINES = (int)(TB * sizeof(T) / 128);
+  const int total = 2 * a.nsplit * LINES;
+  for (int l = threadIdx.x; l < total; l += blockDim.x) {
+    const int seg = l / LINES, w = l - seg * LINES;
+    const T* row = part + (size_t)seg * pst + (size_t)tb * TB;
+    const size_t g = __cvta_generic_to_global(row) + (size_t)w * 128;
+    if ((g & 127) == 0) asm volatile("discard.global.L2 [%0], 128;" ::"l"(g) : "memory");
+  }
+}
+
 // NP = 2 fits 64 registers without spills: 8 CTAs (32 warps) per SM; NP = 4 keeps its 128
 // registers (4 CTAs per SM).
 template <int CORE, bool THICK, bool COMP, int NP>
@@ -241,10 +276,12 @@ p2p_packed_kernel(const P2PArgs a) {
   __shared__ __align__(128) float4 tile[NSTAGE][SRC_TILE * PK_ELEM];
   __shared__ __align__(8) uint64_t bar[NSTAGE];
   __shared__ unsigned smask[P2P_THREADS / 32][PK_NB];
-  __shared__ int s_item;
+  __shared__ int s_item, s_last;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
+  const bool fused = a.blkcnt != nullptr;
+  const size_t pst = fused ? (size_t)a.ntb * TB : (size_t)a.nt;   // partials' row stride
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
     fence_mbar_init();
@@ -273,8 +310,10 @@ p2p_packed_kernel(const P2PArgs a) {
     __syncthreads();
     const int item = *static_cast<volatile int*>(&s_item);
     if (item >= a.nitems) break;
-    const int tb = item % a.ntb;
-    const int sp = item / a.ntb;
+    // fused: target-block-major, so a block's splits run close together and most of its
+    // partials are still in L2 when the last one reduces them; otherwise split-major
+    const int tb = fused ? item / a.nsplit : item % a.ntb;
+    const int sp = fused ? item - tb * a.nsplit : item / a.ntb;
     const int tile0 = sp * a.tiles_per_split;
     const int ntile = min(a.tiles_per_split, a.nst - tile0);
     if (tid == 0) {
@@ -399,13 +438,24 @@ p2p_packed_kernel(const P2PArgs a) {
           store_target<RES_VEL>(a, i, c);
         } else if (COMP) {
           double* qp = static_cast<double*>(a.part);
-          qp[((size_t)0 * a.nsplit + sp) * a.nt + i] = c[0];
-          qp[((size_t)1 * a.nsplit + sp) * a.nt + i] = c[1];
+          qp[((size_t)0 * a.nsplit + sp) * pst + i] = c[0];
+          qp[((size_t)1 * a.nsplit + sp) * pst + i] = c[1];
         } else {
           float* qp = static_cast<float*>(a.part);
-          qp[((size_t)0 * a.nsplit + sp) * a.nt + i] = (float)c[0];
-          qp[((size_t)1 * a.nsplit + sp) * a.nt + i] = (float)c[1];
+          qp[((size_t)0 * a.nsplit + sp) * pst + i] = (float)c[0];
+          qp[((size_t)1 * a.nsplit + sp) * pst + i] = (float)c[1];
         }
+      }
+    }
+    if (fused && !a.direct) {
+      // publish this split's partials, count it in; the block's last split reduces
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) s_last = atomicAdd(&a.blkcnt[tb], 1) == a.nsplit - 1;
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        split_block_reduce<COMP, TB>(a, tb, pst);
       }
     }
     __syncthreads();

@@ -257,3 +257,26 @@ def test_packed_gradient_results_vs_generic_and_fp64(ctx, restatement, result, t
         for k, (a, b) in enumerate(zip(ref, got)):
             ok = np.isfinite(a)
             assert rel_err(a[ok], b[ok]) < tol, (v, k)
+
+
+@pytest.mark.parametrize("ns,nt", [(200_000, 1000), (20_000, 70_001), (60_000, 513)])
+@pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
+@pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED4])
+def test_split_reduce_in_kernel_is_deterministic(ctx, restatement, ns, nt, accum, variant):
+    """Many source splits per target block, reduced inside the velocity kernel: the block's last
+    split to finish sums the partials in split order, so repeated calls give the same bits
+    whichever split arrives last; the sums match FP64, ragged last block included."""
+    rng = np.random.default_rng(ns + nt + 10 * accum + variant)
+    sx, sy, sr, ss = cloud(rng, ns, True)
+    tx, ty, tr, _ = cloud(rng, nt, True)
+    src = og.Points(sx, sy, sr, ss)
+    runs = [_vel(ctx, src, tx, ty, tr, og.CORE_GAUSSIAN, accum, og.ORDER_INPUT, variant) for _ in range(3)]
+    for u, v in runs[1:]:
+        np.testing.assert_array_equal(u, runs[0][0])
+        np.testing.assert_array_equal(v, runs[0][1])
+    pick = np.unique(np.concatenate([rng.choice(nt, min(nt, 1500), replace=False), np.arange(max(0, nt - 40), nt)]))
+    u64, v64, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, 1, sx, sy, sr, ss, tx[pick], ty[pick], tr[pick],
+                                                   fp64=True, tu=np.full(pick.size, 0.5), tv=np.zeros(pick.size))
+    u64, v64 = 1.0 + u64 / (2 * np.pi), -0.25 + v64 / (2 * np.pi)
+    tol = 2e-6 if accum == og.COMPENSATED else 5e-5
+    assert rel_err(u64, runs[0][0][pick]) < tol and rel_err(v64, runs[0][1][pick]) < tol
