@@ -9,8 +9,9 @@
 // estimate drops below the tolerance the remaining kernels of the cycle return at once (a
 // device flag), and the host reads back only the true residual at the end of each cycle.
 //
-// Cost per iteration: one FP64 matrix-vector product (n^2 doubles from HBM: the bound) plus
-// O(n j) vector work.  Every reduction has a fixed order, so results are reproducible.
+// Cost per iteration (per-step path): one FP64 matrix-vector product (n^2 doubles from HBM)
+// plus O(n j) vector work; the fused cycle below reads the FP32 plane of A from L2 instead.
+// Every reduction has a fixed order, so results are reproducible.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -206,8 +207,13 @@ __global__ void diag_inv_kernel(const double* __restrict__ A, int n, double* __r
 // entries carry a relative error below 2^-23, and stops at a relative reduction of 2^-20; the
 // restart residual b - A x is formed with the FP64 matrix, so every restart corrects the
 // solution against A itself (iterative refinement): the final residual meets the FP64
-// tolerance.  Everything else (Gram-Schmidt, norms, Givens, back substitution, the restart
-// residual) stays FP64.
+// tolerance.  Inside the cycle the basis, w, the Gram-Schmidt dot products, the sums over
+// blocks and the updates are double-float (hi + lo FP32 pairs, about 2^-48) on the FP32 pipes;
+// the preconditioner is Dinv rounded to FP32 (used alike in the operator and in the update of
+// x); the Hessenberg matrix, Givens rotations, back substitution and the update of x are FP64.
+// Measured on the 4096 unknowns of a 2048-panel circle: an FP32 basis left each cycle's true
+// residual 7x above its estimate (72 iterations instead of 57, the FP64 count); the
+// double-float basis reproduces the FP64 cycle's residuals.
 
 constexpr double kRefineEta = 9.5367431640625e-7;   // 2^-20: a cycle's relative reduction on A_hi
 constexpr int GC_THREADS = 1024;
@@ -228,23 +234,32 @@ __device__ __forceinline__ float hi_bits(double a, int& bad) {
   return __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
 }
 
-__global__ void split_hi_kernel(const double* __restrict__ A, size_t nn, float* __restrict__ AH,
+// hi plane in column pairs, AH[(c/2) * n + i] = (hi(A[c][i]), hi(A[c+1][i])) (a zero column
+// pads an odd order), so one 8-byte load feeds the f32x2 product of two columns
+__global__ void split_hi_kernel(const double* __restrict__ A, int n, float2* __restrict__ AH,
                                 int* __restrict__ range_flag) {
   int bad = 0;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x)
-    AH[k] = hi_bits(A[k], bad);
+  const size_t N = (size_t)n, total = (N + 1) / 2 * N;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t cp = k / N, i = k - cp * N;
+    const size_t c = 2 * cp;
+    const float lo = hi_bits(A[c * N + i], bad);
+    const float hi = (c + 1 < N) ? hi_bits(A[(c + 1) * N + i], bad) : 0.0f;
+    AH[k] = make_float2(lo, hi);
+  }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(range_flag, 1);
 }
 
 struct GcArgs {
-  const float* AH;                              // hi plane of A, column-major
+  const float2* AH;                             // hi plane of A in column pairs
   const double* dinv;
   int n, m, mc;                                 // order, restart length, iterations this cycle
   int gpb;                                      // row groups a block owns (at most)
   const double* V0;                             // v_0 (n)
-  float2* vs;                                   // hi/lo of Dinv v_j
+  float4* vsp;                                  // per column pair: hi of Dinv v_j, then negated
+  float2* vsl;                                  // per column pair: negated lo of Dinv v_j
   double* x;
-  double* P;                                    // partials: [2][grid][m+2]
+  float2* P;                                    // partials (double-float): [2][grid][m+2]
   unsigned* bar;                                // arrival counter, zeroed before each launch
   GmState* st;
   int* status;
@@ -283,83 +298,6 @@ __device__ bool gc_barrier(unsigned* bar, int* status, unsigned nb, unsigned arr
   return __syncthreads_and(ok) != 0;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// out[k] = sum over blocks of P[b * ld + k], k < cnt: one warp per k, fixed order
-__device__ void gc_sum_partials(const double* P, int ld, int cnt, double* out) {
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  for (int k = wp; k < cnt; k += GC_WARPS) {
-    double s = 0.0;
-    for (int b = lane; b < (int)gridDim.x; b += 32) s += P[(size_t)b * ld + k];
-    s = warp_sum(s);
-    if (lane == 0) out[k] = s;
-  }
-  __syncthreads();
-}
-
-// The block's rows of the basis live in shared memory: Vs[k * RB + r], r = q * 32 + lane for
-// the block's q-th row group (global row (blockIdx.x + q * grid) * 32 + lane; rows past n
-// hold 0), and w likewise in ws[r].
-struct GcRows {
-  double* Vs;
-  double* ws;
-  int RB;     // 32 * gpb
-  int nq;     // row groups this block owns
-};
-
-// this block's share of V_k . w (k <= j) into P[blockIdx.x * ld + k]; with `norm`, also w . w
-// into slot j + 1
-__device__ void gc_partial_dots(const GcRows& R, int j, bool norm, int ld, double* P, double* sh) {
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const int kmax = norm ? j + 1 : j;
-  for (int k = wp; k <= kmax; k += GC_WARPS) {
-    const double* vk = (k <= j) ? R.Vs + (size_t)k * R.RB : R.ws;
-    double s = 0.0;
-    for (int q = 0; q < R.nq; ++q) s = fma(vk[q * 32 + lane], R.ws[q * 32 + lane], s);
-    s = warp_sum(s);
-    if (lane == 0) sh[k] = s;
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k <= kmax; k += GC_THREADS) P[(size_t)blockIdx.x * ld + k] = sh[k];
-}
-
-// sum_{k <= j} V_k[r] c[k] for local row group q (warps split k, fixed-order sum); valid in
-// warp 0
-__device__ double gc_vsum(const GcRows& R, int j, int q, const double* c, double (*red)[32]) {
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  double s = 0.0;
-  for (int k = wp; k <= j; k += GC_WARPS) s = fma(R.Vs[(size_t)k * R.RB + q * 32 + lane], c[k], s);
-  red[wp][lane] = s;
-  __syncthreads();
-  double t = 0.0;
-  if (wp == 0)
-    for (int p = 0; p < GC_WARPS; ++p) t += red[p][lane];
-  __syncthreads();
-  return t;
-}
-
-__device__ __forceinline__ float2 split_f64(double v) {
-  const float hi = __double2float_rn(v);
-  return make_float2(hi, __double2float_rn(v - (double)hi));
-}
-
-// S + s += a * x in double-float, a = a.x + a.y and x = x.x + x.y (the a.y * x.y term, 2^-48
-// relative, is dropped); the product a.x * x.x is split exactly with an FMA and added to S with
-// Knuth's two-sum
-__device__ __forceinline__ void df_fma(float2 av, float2 xv, float& S, float& s) {
-  const float p = __fmul_rn(av.x, xv.x);
-  const float e = __fmaf_rn(av.x, xv.x, -p);
-  const float t = __fmaf_rn(av.x, xv.y, __fmaf_rn(av.y, xv.x, e));
-  const float u = __fadd_rn(S, p);
-  const float bv = __fsub_rn(u, S);
-  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bv)), __fsub_rn(p, bv));
-  S = u;
-  s = __fadd_rn(s, __fadd_rn(err, t));
-}
-
 // (S, s) += (T, t) in double-float: two-sum of the leading parts, the trailing parts added to
 // the error term
 __device__ __forceinline__ void df_add(float& S, float& s, float T, float t) {
@@ -370,46 +308,173 @@ __device__ __forceinline__ void df_add(float& S, float& s, float T, float t) {
   s = __fadd_rn(s, __fadd_rn(err, t));
 }
 
+// a * b = p + e exactly (FMA)
+__device__ __forceinline__ float2 two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return make_float2(p, __fmaf_rn(a, b, -p));
+}
+
+// x + y in double-float, renormalised so that |lo| stays below half an ulp of hi
+__device__ __forceinline__ float2 df_sum(float2 x, float2 y) {
+  float S = x.x, s = x.y;
+  df_add(S, s, y.x, y.y);
+  const float h = __fadd_rn(S, s);
+  return make_float2(h, __fsub_rn(s, __fsub_rn(h, S)));
+}
+
+// v * (c.hi + c.lo) in double-float (v FP32)
+__device__ __forceinline__ float2 df_scale(float v, float2 c) {
+  const float2 p = two_prod(v, c.x);
+  return make_float2(p.x, __fmaf_rn(v, c.y, p.y));
+}
+
+// (a.hi + a.lo) * (b.hi + b.lo) in double-float (the lo * lo term, 2^-48 relative, dropped)
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float2 p = two_prod(a.x, b.x);
+  return make_float2(p.x, __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, p.y)));
+}
+
+__device__ __forceinline__ float2 warp_sum_df(float2 v) {
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_sum(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o)));
+  return v;
+}
+
+// out[k] = sum over blocks of P[b * ld + k], k < cnt, in double-float: one warp per k; lane l
+// adds the blocks l, l + 32, ... in order, then a fixed shuffle tree, so the sum does not
+// depend on timing
+__device__ void gc_sum_partials(const float2* P, int ld, int cnt, float2* out) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  for (int k = wp; k < cnt; k += GC_WARPS) {
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int b = lane; b < (int)gridDim.x; b += 32) s = df_sum(s, P[(size_t)b * ld + k]);
+    s = warp_sum_df(s);
+    if (lane == 0) out[k] = s;
+  }
+  __syncthreads();
+}
+
+// The block's rows of the basis live in shared memory in double-float: Vs[k * RB + r], r =
+// q * 32 + lane for the block's q-th row group (global row (blockIdx.x + q * grid) * 32 + lane;
+// rows past n hold 0); w likewise in ws[r], the row's preconditioner (FP32) in ds[r].
+struct GcRows {
+  float2* Vs;
+  float2* ws;
+  float* ds;
+  int RB;     // 32 * gpb
+  int nq;     // row groups this block owns
+};
+
+// this block's share of V_k . w (k <= j) into P[blockIdx.x * ld + k], double-float; with
+// `norm`, also w . w into slot j + 1
+__device__ void gc_partial_dots(const GcRows& R, int j, bool norm, int ld, float2* P, float2* sh) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int kmax = norm ? j + 1 : j;
+  for (int k = wp; k <= kmax; k += GC_WARPS) {
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int q = 0; q < R.nq; ++q) {
+      const float2 w = R.ws[q * 32 + lane];
+      float2 t;
+      if (k <= j) {
+        t = df_mul(R.Vs[(size_t)k * R.RB + q * 32 + lane], w);
+      } else {                                   // w . w = hi^2 + 2 hi lo (+ lo^2, dropped)
+        t = two_prod(w.x, w.x);
+        t.y = __fmaf_rn(2.0f * w.x, w.y, t.y);
+      }
+      s = df_sum(s, t);
+    }
+    s = warp_sum_df(s);
+    if (lane == 0) sh[k] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= kmax; k += GC_THREADS) P[(size_t)blockIdx.x * ld + k] = sh[k];
+}
+
+// sum_{k <= j} V_k[r] c[k] for local row group q in double-float (warps split k, fixed-order
+// sum); valid in warp 0
+__device__ float2 gc_vsum(const GcRows& R, int j, int q, const float2* c, float2 (*red)[32]) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  float2 s = make_float2(0.0f, 0.0f);
+  for (int k = wp; k <= j; k += GC_WARPS) s = df_sum(s, df_mul(R.Vs[(size_t)k * R.RB + q * 32 + lane], c[k]));
+  red[wp][lane] = s;
+  __syncthreads();
+  float2 t = make_float2(0.0f, 0.0f);
+  if (wp == 0)
+    for (int p = 0; p < GC_WARPS; ++p) t = df_sum(t, red[p][lane]);
+  __syncthreads();
+  return t;
+}
+
+// Two columns at once (f32x2): (NS, Ns) -= a * (xh + xl) in double-float, kept negated so that
+// every subtraction is an FMA by -1.  np = a * (-xh) rounded is -p, e = a * xh + np is the
+// product's rounding error (exact, FMA); NS + np is split exactly by Knuth's two-sum, and the
+// trailing part collects err - e - a * xl (the a * xl term, 2^-24 of the product, is rounded).
+__device__ __forceinline__ void df2_acc(float2 a, float2 xh, float2 nxh, float2 nxl, float2& NS, float2& Ns) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 np = __fmul2_rn(a, nxh);
+  const float2 e = __ffma2_rn(a, xh, np);
+  const float2 u = __fadd2_rn(NS, np);
+  const float2 bv = __ffma2_rn(NS, m1, u);                     // u - NS
+  const float2 t1 = __ffma2_rn(bv, m1, u);                     // u - bv
+  const float2 err = __fadd2_rn(__ffma2_rn(t1, m1, NS), __ffma2_rn(bv, m1, np));
+  NS = u;
+  Ns = __ffma2_rn(a, nxl, __ffma2_rn(e, m1, __fadd2_rn(Ns, err)));
+}
+
 // One restart cycle of right-preconditioned GMRES(m) with CGS2, back substitution and the
 // update of x, in one cooperative launch.  Blocks own groups of 32 consecutive rows
-// (column-major A: a warp reads 128 contiguous bytes of the hi plane per column) and keep those
-// rows of the basis in shared memory; only the split vector Dinv v_j and the per-block partial
-// sums cross between blocks.  Iteration j:
+// (column-major A: a warp reads 256 contiguous bytes of the paired hi plane per column pair)
+// and keep those rows of the basis in shared memory; only the split vector Dinv v_j and the
+// per-block partial sums cross between blocks.  Iteration j:
 //   (1) w = A Dinv v_j on the owned rows; partial V^T w                         -> barrier
 //   (2) h = V^T w; w -= V h; partial V^T w and w^T w                            -> barrier
 //   (3) h2 = V^T w; ||w - V h2||^2 = w^T w - h2^T h2 (V orthonormal);
-//       v_{j+1} = (w - V h2) / ||.|| on the owned rows; H column h + h2; Givens   -> barrier
-// Every block keeps H, the rotations and g in shared memory and runs the (tiny) Givens and
-// back-substitution steps itself, so no step waits on one block; the rotations of column j
-// run on one warp during the product of step j+1 (FP64 latency on this GPU makes them slow,
-// not costly).  All sums over blocks run in block order, so the result does not depend on
-// timing.
+//       v_{j+1} = (w - V h2) / ||.|| on the owned rows; H column h + h2          -> barrier
+// The basis and the Gram-Schmidt arithmetic are double-float, as is the operator product; the
+// Hessenberg matrix, the Givens rotations, g and the back substitution are FP64.  Every block
+// keeps H, the rotations and g in shared memory: the rotations of column j-1 run on the last
+// warp during the product of step j, as a warp scan of their recurrence (FP64 latency on this
+// GPU makes a sequential chain of 2 j operations slow).  All sums over blocks run in a fixed
+// order, so the result does not depend on timing.
 __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs a) {
-  __shared__ double red[GC_WARPS][32];
+  __shared__ float2 redf[GC_WARPS][32];
   __shared__ double Hs[GC_MAXM][GC_MAXM + 1];   // Hs[j][k]: rotated column j (R factor)
-  __shared__ double h1[GC_MAXM + 2];
-  __shared__ double sh[GC_MAXM + 2];
+  __shared__ float2 h1[GC_MAXM + 2];
+  __shared__ float2 sh[GC_MAXM + 2];
+  __shared__ double yv[GC_MAXM];
   __shared__ double gs[GC_MAXM + 1];
   __shared__ double css[GC_MAXM], sns[GC_MAXM];
-  __shared__ double nrm_inv[2];
+  __shared__ float nrm_inv[2];
   __shared__ int sdone;
-  extern __shared__ double dyn[];
-  float2 (*redf)[32] = reinterpret_cast<float2 (*)[32]>(red);
+  extern __shared__ float dyn[];
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int ngroups = (a.n + 31) / 32;
+  const int npairs = (a.n + 1) / 2;
   const int ld = a.m + 2;
   GcRows R;
   R.RB = 32 * a.gpb;
-  R.Vs = dyn;
-  R.ws = dyn + (size_t)(a.m + 1) * R.RB;
+  R.Vs = reinterpret_cast<float2*>(dyn);
+  R.ws = R.Vs + (size_t)(a.m + 1) * R.RB;
+  R.ds = dyn + (size_t)2 * (a.m + 2) * R.RB;
   R.nq = ((int)blockIdx.x < ngroups) ? (ngroups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  double* P1 = a.P;
-  double* P2 = a.P + (size_t)gridDim.x * ld;
+  float2* P1 = a.P;
+  float2* P2 = a.P + (size_t)gridDim.x * ld;
   // the last warp applies the Givens rotations to column j-1 while the others form A Dinv v_j
   const bool gwarp = (wp == GC_WARPS - 1);
-  const int per = (a.n + GC_WARPS - 2) / (GC_WARPS - 1);
-  const int c0 = gwarp ? a.n : min(a.n, wp * per), c1 = gwarp ? a.n : min(a.n, c0 + per);
+  const int per = (npairs + GC_WARPS - 2) / (GC_WARPS - 1);
+  const int p0 = gwarp ? npairs : min(npairs, wp * per), p1 = gwarp ? npairs : min(npairs, p0 + per);
   auto row = [&](int q) { return ((int)blockIdx.x + q * (int)gridDim.x) * 32 + lane; };
+  // Dinv v for row i (v double-float, Dinv FP32) as hi + lo, stored with negations
+  auto put_split = [&](int i, float2 v, float d) {
+    const float2 z = df_scale(d, v);
+    const float p = z.x, e = z.y;
+    float* hp = reinterpret_cast<float*>(&a.vsp[i >> 1]);
+    float* lp = reinterpret_cast<float*>(&a.vsl[i >> 1]);
+    hp[i & 1] = p;
+    hp[2 + (i & 1)] = -p;
+    lp[i & 1] = -e;
+  };
   unsigned nb = 0;
 
   if (threadIdx.x == 0) {
@@ -417,60 +482,104 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     sdone = a.st->done;
   }
   for (int k = 1 + threadIdx.x; k <= GC_MAXM; k += GC_THREADS) gs[k] = 0.0;
-  // v_0 on the owned rows into shared memory; Dinv v_0 split for the operator product
+  // an odd order pads the last column pair with a zero column
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (a.n & 1)) {
+    a.vsp[a.n >> 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    a.vsl[a.n >> 1] = make_float2(0.0f, 0.0f);
+  }
+  // v_0 and Dinv on the owned rows into shared memory (FP32); Dinv v_0 split for the product
   if (wp == 0)
     for (int q = 0; q < R.nq; ++q) {
       const int i = row(q);
-      const double v = (i < a.n) ? a.V0[i] : 0.0;
+      const double vd = (i < a.n) ? a.V0[i] : 0.0;
+      const float vh = (float)vd;
+      const float2 v = make_float2(vh, (float)(vd - (double)vh));
+      const float d = (i < a.n) ? (float)a.dinv[i] : 0.0f;
       R.Vs[q * 32 + lane] = v;
-      if (i < a.n) a.vs[i] = split_f64(v * a.dinv[i]);
+      R.ds[q * 32 + lane] = d;
+      if (i < a.n) put_split(i, v, d);
     }
   if (!gc_barrier(a.bar, a.status, nb++)) return;
 
   int kd = 0;
   for (int j = 0;; ++j) {
-    if (gwarp && lane == 0 && j > 0) {
-      // column j-1 of H (assembled in step 3): previous rotations, a new one, g, convergence
-      const int jc = j - 1;
-      double* hc = Hs[jc];
-      for (int k = 0; k < jc; ++k) {
-        const double t = css[k] * hc[k] + sns[k] * hc[k + 1];
-        hc[k + 1] = -sns[k] * hc[k] + css[k] * hc[k + 1];
-        hc[k] = t;
+    if (gwarp && j > 0) {
+      // column j-1 of H (assembled in step 3): the K = j-1 earlier rotations as the affine
+      // recurrence x_{k+1} = -s_k x_k + c_k h_{k+1} (x_0 = h_0, x_k the value entering
+      // rotation k), scanned over the warp (two rotations per lane); then the new rotation, g
+      // and the convergence test
+      const int K = j - 1;
+      double* hc = Hs[K];
+      const int k0 = 2 * lane, k1 = k0 + 1;
+      double c0 = 1.0, s0 = 0.0, c1 = 1.0, s1 = 0.0, h0p = 0.0, h1p = 0.0;
+      if (k0 < K) { c0 = css[k0]; s0 = sns[k0]; h0p = hc[k0 + 1]; }
+      if (k1 < K) { c1 = css[k1]; s1 = sns[k1]; h1p = hc[k1 + 1]; }
+      const double a0 = -s0, b0 = c0 * h0p, a1 = -s1, b1 = c1 * h1p;
+      const double x0 = hc[0], xn = hc[K + 1];
+      double Ac = a1 * a0, Bc = fma(a1, b0, b1);         // f_{k1} o f_{k0}
+      for (int o = 1; o < 32; o <<= 1) {
+        const double Ap = __shfl_up_sync(FULL, Ac, o), Bp = __shfl_up_sync(FULL, Bc, o);
+        if (lane >= o) {
+          Bc = fma(Ac, Bp, Bc);
+          Ac = Ac * Ap;
+        }
       }
-      const double x0 = hc[jc], x1 = hc[jc + 1];
-      const double r = hypot(x0, x1);
-      const double c = (r == 0.0) ? 1.0 : x0 / r, sg = (r == 0.0) ? 0.0 : x1 / r;
-      css[jc] = c;
-      sns[jc] = sg;
-      hc[jc] = r;
-      hc[jc + 1] = 0.0;
-      gs[jc + 1] = -sg * gs[jc];
-      gs[jc] = c * gs[jc];
-      sdone = (fabs(gs[jc + 1]) <= a.st->tolcyc || x1 == 0.0) ? 1 : 0;
+      double Ae = __shfl_up_sync(FULL, Ac, 1), Be = __shfl_up_sync(FULL, Bc, 1);
+      if (lane == 0) { Ae = 1.0; Be = 0.0; }
+      const double xk0 = fma(Ae, x0, Be);                // x_{k0}
+      const double xk1 = fma(a0, xk0, b0);               // x_{k1}
+      const double xk2 = fma(a1, xk1, b1);               // x_{k1 + 1}
+      __syncwarp();
+      if (k0 < K) hc[k0] = fma(c0, xk0, s0 * h0p);
+      if (k1 < K) hc[k1] = fma(c1, xk1, s1 * h1p);
+      // x_K sits with element K-1: lane (K-1)/2, as xk1 (K-1 even) or xk2 (K-1 odd)
+      const double cand = ((K - 1) & 1) ? xk2 : xk1;
+      double xK = __shfl_sync(FULL, cand, K > 0 ? ((K - 1) >> 1) : 0);
+      if (K == 0) xK = x0;
+      if (lane == 0) {
+        const double r = hypot(xK, xn);
+        const double c = (r == 0.0) ? 1.0 : xK / r, sg = (r == 0.0) ? 0.0 : xn / r;
+        css[K] = c;
+        sns[K] = sg;
+        hc[K] = r;
+        hc[K + 1] = 0.0;
+        gs[K + 1] = -sg * gs[K];
+        gs[K] = c * gs[K];
+        sdone = (fabs(gs[K + 1]) <= a.st->tolcyc || xn == 0.0) ? 1 : 0;
+      }
     }
     const bool more = j < a.mc;
-    // (1) w = A Dinv v_j on the owned rows, double-float; columns split over the warps, the
-    //     warps' (S, s) pairs combined in double-float and converted to FP64 once per row
+    // (1) w = A Dinv v_j on the owned rows, double-float; column pairs split over the warps,
+    //     two independent f32x2 chains per lane, combined in double-float, rounded once
     for (int q = 0; q < R.nq && more; ++q) {
       const int i = row(q);
       const int ic = min(i, a.n - 1);            // rows past n compute a dummy sum, never stored
-      float S0 = 0.f, s0 = 0.f, S1 = 0.f, s1 = 0.f;
-      const float* col = a.AH + (size_t)c0 * a.n + ic;
-      int c = c0;
-#pragma unroll 8
-      for (; c + 1 < c1; c += 2, col += 2 * (size_t)a.n) {
-        df_fma(make_float2(__ldg(col), 0.0f), a.vs[c], S0, s0);
-        df_fma(make_float2(__ldg(col + a.n), 0.0f), a.vs[c + 1], S1, s1);
+      float2 NS0 = make_float2(0.f, 0.f), Ns0 = NS0, NS1 = NS0, Ns1 = NS0;
+      const float2* col = a.AH + (size_t)p0 * a.n + ic;
+      int cp = p0;
+#pragma unroll 4
+      for (; cp + 1 < p1; cp += 2, col += 2 * (size_t)a.n) {
+        const float2 A0 = __ldg(col), A1 = __ldg(col + a.n);
+        const float4 H0 = a.vsp[cp], H1 = a.vsp[cp + 1];
+        const float2 L0 = a.vsl[cp], L1 = a.vsl[cp + 1];
+        df2_acc(A0, make_float2(H0.x, H0.y), make_float2(H0.z, H0.w), L0, NS0, Ns0);
+        df2_acc(A1, make_float2(H1.x, H1.y), make_float2(H1.z, H1.w), L1, NS1, Ns1);
       }
-      if (c < c1) df_fma(make_float2(__ldg(col), 0.0f), a.vs[c], S0, s0);
-      df_add(S0, s0, S1, s1);
-      redf[wp][lane] = make_float2(S0, s0);
+      if (cp < p1) {
+        const float4 H0 = a.vsp[cp];
+        df2_acc(__ldg(col), make_float2(H0.x, H0.y), make_float2(H0.z, H0.w), a.vsl[cp], NS0, Ns0);
+      }
+      float S = NS0.x, s = Ns0.x;
+      df_add(S, s, NS0.y, Ns0.y);
+      df_add(S, s, NS1.x, Ns1.x);
+      df_add(S, s, NS1.y, Ns1.y);
+      redf[wp][lane] = make_float2(S, s);
       __syncthreads();
       if (wp == 0) {
         float2 t = redf[0][lane];
-        for (int p = 1; p < GC_WARPS; ++p) df_add(t.x, t.y, redf[p][lane].x, redf[p][lane].y);
-        R.ws[q * 32 + lane] = (i < a.n) ? (double)t.x + (double)t.y : 0.0;
+        for (int p = 1; p < GC_WARPS - 1; ++p) df_add(t.x, t.y, redf[p][lane].x, redf[p][lane].y);
+        const float h = -__fadd_rn(t.x, t.y);   // -(S + s), renormalised
+        R.ws[q * 32 + lane] = (i < a.n) ? make_float2(h, __fsub_rn(-t.y, __fadd_rn(h, t.x))) : make_float2(0.f, 0.f);
       }
       __syncthreads();
     }
@@ -484,8 +593,8 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     // (2)
     gc_sum_partials(P1, ld, j + 1, h1);
     for (int q = 0; q < R.nq; ++q) {
-      const double t = gc_vsum(R, j, q, h1, red);
-      if (wp == 0) R.ws[q * 32 + lane] -= t;
+      const float2 t = gc_vsum(R, j, q, h1, redf);
+      if (wp == 0) R.ws[q * 32 + lane] = df_sum(R.ws[q * 32 + lane], make_float2(-t.x, -t.y));
     }
     __syncthreads();
     gc_partial_dots(R, j, true, ld, P2, sh);
@@ -493,49 +602,73 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     // (3)
     gc_sum_partials(P2, ld, j + 2, sh);
     if (wp == 0) {
-      double s2 = 0.0;
-      for (int k = lane; k <= j; k += 32) s2 = fma(sh[k], sh[k], s2);
-      s2 = warp_sum(s2);
+      float s2 = 0.0f;
+      for (int k = lane; k <= j; k += 32) s2 = fmaf(sh[k].x, sh[k].x, s2);
+      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(FULL, s2, o);
       if (lane == 0) {
-        const double nrm2 = sh[j + 1] - s2;
-        const double nr = nrm2 > 0.0 ? sqrt(nrm2) : 0.0;
+        const float nrm2 = (sh[j + 1].x + sh[j + 1].y) - s2;
+        const float nr = nrm2 > 0.0f ? sqrtf(nrm2) : 0.0f;
         nrm_inv[0] = nr;
-        nrm_inv[1] = nr > 0.0 ? 1.0 / nr : 0.0;
+        nrm_inv[1] = nr > 0.0f ? 1.0f / nr : 0.0f;
       }
     }
     __syncthreads();
-    const double nrm = nrm_inv[0], inv = nrm_inv[1];
+    const float inv = nrm_inv[1];
     for (int q = 0; q < R.nq; ++q) {
-      const double t = gc_vsum(R, j, q, sh, red);
+      const float2 t = gc_vsum(R, j, q, sh, redf);
       if (wp == 0) {
         const int i = row(q);
-        const double v = (R.ws[q * 32 + lane] - t) * inv;
+        const float2 w2 = df_sum(R.ws[q * 32 + lane], make_float2(-t.x, -t.y));
+        const float2 v = df_scale(inv, w2);       // w2 * inv; H[j+1][j] = 1 / inv, so that
+                                                  // H[j+1][j] v_{j+1} = w2 to double-float
         R.Vs[(size_t)(j + 1) * R.RB + q * 32 + lane] = v;
-        if (i < a.n) a.vs[i] = split_f64(v * a.dinv[i]);
+        if (i < a.n) put_split(i, v, R.ds[q * 32 + lane]);
       }
     }
-    for (int k = threadIdx.x; k <= j; k += GC_THREADS) Hs[j][k] = h1[k] + sh[k];
-    if (threadIdx.x == 0) Hs[j][j + 1] = nrm;
+    for (int k = threadIdx.x; k <= j; k += GC_THREADS)
+      Hs[j][k] = ((double)h1[k].x + (double)sh[k].x) + ((double)h1[k].y + (double)sh[k].y);
+    if (threadIdx.x == 0) Hs[j][j + 1] = (inv > 0.0f) ? 1.0 / (double)inv : 0.0;
     if (!gc_barrier(a.bar, a.status, nb++)) return;
   }
-  // y = R^{-1} g (every block), then x += Dinv V y on the owned rows
-  if (threadIdx.x == 0) {
+  // y = R^{-1} g on one warp (every block): a column sweep from the last unknown, the
+  // reciprocals of the diagonal formed in parallel first; R[k][i] = Hs[i][k]
+  if (wp == 0) {
+    const int ia = lane, ib = lane + 32;
+    double t0 = (ia < kd) ? gs[ia] : 0.0, t1 = (ib < kd) ? gs[ib] : 0.0;
+    const double d0 = (ia < kd) ? 1.0 / Hs[ia][ia] : 0.0, d1 = (ib < kd) ? 1.0 / Hs[ib][ib] : 0.0;
     for (int i = kd - 1; i >= 0; --i) {
-      double t = gs[i];
-      for (int q = i + 1; q < kd; ++q) t -= Hs[q][i] * h1[q];
-      h1[i] = t / Hs[i][i];
-    }
-    if (blockIdx.x == 0) {
-      a.st->kdone = kd;
-      a.st->done = sdone;
+      const double ti = __shfl_sync(FULL, i < 32 ? t0 : t1, i & 31);
+      const double di = __shfl_sync(FULL, i < 32 ? d0 : d1, i & 31);
+      const double yi = ti * di;
+      if (lane == 0) yv[i] = yi;
+      if (ia < i) t0 = fma(-Hs[i][ia], yi, t0);
+      if (ib < i) t1 = fma(-Hs[i][ib], yi, t1);
     }
   }
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    a.st->kdone = kd;
+    a.st->done = sdone;
+  }
   __syncthreads();
+  // x += Dinv V y on the owned rows, in FP64: an FP32 rounding of the correction would come
+  // back in the next residual amplified by the condition number of A Dinv
+  double (*redd)[32] = reinterpret_cast<double (*)[32]>(redf);
   if (kd > 0)
     for (int q = 0; q < R.nq; ++q) {
-      const double t = gc_vsum(R, kd - 1, q, h1, red);
-      const int i = row(q);
-      if (wp == 0 && i < a.n) a.x[i] += t * a.dinv[i];
+      double t = 0.0;
+      for (int k = wp; k < kd; k += GC_WARPS) {
+        const float2 v = R.Vs[(size_t)k * R.RB + q * 32 + lane];
+        t = fma((double)v.x + (double)v.y, yv[k], t);
+      }
+      redd[wp][lane] = t;
+      __syncthreads();
+      if (wp == 0) {
+        double u = 0.0;
+        for (int p = 0; p < GC_WARPS; ++p) u += redd[p][lane];
+        const int i = row(q);
+        if (i < a.n) a.x[i] += u * (double)R.ds[q * 32 + lane];
+      }
+      __syncthreads();
     }
 }
 
@@ -613,7 +746,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   const int ngroups = (n + 31) / 32;
   const int gc_grid = std::min(ngroups, std::max(1, gc_occ) * ctx->num_sms);
   const int gc_gpb = (ngroups + gc_grid - 1) / gc_grid;
-  const size_t gc_smem = (size_t)(m + 2) * 32 * gc_gpb * sizeof(double);
+  const size_t gc_smem = (size_t)(2 * (m + 2) + 1) * 32 * gc_gpb * sizeof(float);
   bool fused = coop && gc_occ > 0 && m <= GC_MAXM && ctx->kernel_variant != OBS_VARIANT_GENERIC;
   if (fused) {
     cudaFuncAttributes fa{};
@@ -630,11 +763,13 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
       fused = occ2 * ctx->num_sms >= gc_grid;
     }
   }
+  const size_t NP2 = (N + 1) / 2;                  // column pairs
   const size_t o_gp = o_n + 256;
   const size_t o_gv = o_gp + al((size_t)2 * gc_grid * (m + 2) * 8);
-  const size_t o_gb = o_gv + al(N * 8);
+  const size_t o_gl = o_gv + al(NP2 * 16);
+  const size_t o_gb = o_gl + al(NP2 * 8);
   const size_t o_ap = o_gb + 256;
-  const size_t total = fused ? o_ap + al(N * N * 4) : o_gb + 256;
+  const size_t total = fused ? o_ap + al(NP2 * N * 8) : o_gb + 256;
   int s = ctx->work.ensure(total, ctx->stream);
   if (s) return s;
   GmState* st = ctx->work.as<GmState>(o_st);
@@ -649,10 +784,11 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   double* w = ctx->work.as<double>(o_w);
   double* part = ctx->work.as<double>(o_p);
   double* nrm = ctx->work.as<double>(o_n);
-  double* gpart = ctx->work.as<double>(o_gp);
-  float2* gvs = ctx->work.as<float2>(o_gv);
+  float2* gpart = ctx->work.as<float2>(o_gp);
+  float4* gvp = ctx->work.as<float4>(o_gv);
+  float2* gvl = ctx->work.as<float2>(o_gl);
   unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag, [2] x != 0
-  float* AH = fused ? ctx->work.as<float>(o_ap) : nullptr;
+  float2* AH = fused ? ctx->work.as<float2>(o_ap) : nullptr;
   cudaStream_t strm = ctx->stream;
   const int gb = (n + GM_THREADS - 1) / GM_THREADS;
   const dim3 ggrid(gb, nchunk);
@@ -665,7 +801,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
   launched(1);
   if (fused) {
-    split_hi_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, N * N, AH, reinterpret_cast<int*>(gbar + 1));
+    split_hi_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, n, AH, reinterpret_cast<int*>(gbar + 1));
     launched(1);
   }
   double bnorm = 0.0;
@@ -721,7 +857,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     const int mc = std::min(m, maxiter - total_it);
     if (fused) {
       if ((e = cudaMemsetAsync(gbar, 0, sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
-      GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvs, x, gpart, gbar, st, ctx->d_status};
+      GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvp, gvl, x, gpart, gbar, st, ctx->d_status};
       void* args[] = {&ga};
       e = cudaLaunchCooperativeKernel((const void*)gmres_cycle_kernel, dim3(gc_grid), dim3(GC_THREADS), args, gc_smem,
                                       strm);
