@@ -831,24 +831,21 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   int total_it = 0;
   double rel = 0.0, prev_rn = -1.0;
   for (;;) {
+    // one host round trip per cycle: the true residual norm, the cycle's iteration count and
+    // the status block (a barrier that gave up leaves its record there)
     double rn = 0.0;
+    int kd = 0, flag = 0;
     e = cudaMemcpyAsync(&rn, nrm, 8, cudaMemcpyDeviceToHost, strm);
+    if (e == cudaSuccess && total_it > 0) e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
+    if (e == cudaSuccess && total_it > 0) e = cudaMemcpyAsync(&flag, ctx->d_status, 4, cudaMemcpyDeviceToHost, strm);
     if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
     if (e != cudaSuccess) return cuda_status(e);
+    if (flag) return take_device_status(ctx);
+    if (total_it > 0) total_it += std::max(kd, 1) - 1;
     // a refinement cycle (FP32 plane) that did not halve the true residual: A is too
     // ill-conditioned for its FP32 entries, so finish with FP64 products throughout
     if (fused && prev_rn > 0.0 && !(rn < 0.5 * prev_rn)) fused = false;
     prev_rn = rn;
-    if (total_it > 0) {
-      // the cycle's iteration count; a barrier that gave up leaves its record in the status block
-      int kd = 0, flag = 0;
-      e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
-      if (e == cudaSuccess && fused) e = cudaMemcpyAsync(&flag, ctx->d_status, 4, cudaMemcpyDeviceToHost, strm);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
-      if (e != cudaSuccess) return cuda_status(e);
-      if (flag) return take_device_status(ctx);
-      total_it += std::max(kd, 1) - 1;
-    }
     rel = rn / bref;
     if (!(rn > tol * bref) || total_it >= maxiter) break;   // converged (or NaN) / out of budget
     cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m, fused ? kRefineEta : 0.0);

@@ -13,8 +13,9 @@
 //   plain       : FP32 accumulators per target (the drop-in);
 //   compensated : FP32 partials over COMP_BLOCK sources, folded into a (hi, lo) two-sum pair;
 //                 each item's result leaves the kernel as a double, and splits are summed in
-//                 FP64 in a fixed order: by p2p_reduce_kernel, or (packed velocity kernel) by
-//                 the last split of each target block to finish, in the same order.
+//                 FP64 in a fixed order by p2p_reduce_kernel; or (packed velocity kernel) as
+//                 (hi, lo) pairs summed in split order by the last split of each target block
+//                 to finish.
 #pragma once
 
 #include "obs_device.cuh"
@@ -47,10 +48,11 @@ struct P2PArgs {
   int direct;            // nsplit == 1: write outputs from the main kernel
   int finalize;          // apply fs + (1/2pi) in the epilogue
   double fsx, fsy;
-  // Non-null (packed velocity kernel, nsplit > 1): per target block arrival counts, zeroed
-  // before launch.  Items then run target-block-major, the partials' row stride is ntb * TB,
-  // and the last split of a block to finish sums the block's partials in split order (the sum
-  // p2p_reduce_kernel forms) and writes its targets; no reduction launch follows.
+  // Non-null (packed velocity kernel, 1 < nsplit <= 64): per target block arrival counts,
+  // zeroed before launch.  Items then run target-block-major, the partials' row stride is
+  // ntb * TB (compensated partials as (hi, lo) FP32 pairs), and the last split of a block to
+  // finish sums the block's partials in split order and writes its targets; no reduction
+  // launch follows.
   int* blkcnt;
 };
 

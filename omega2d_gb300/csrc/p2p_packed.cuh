@@ -231,13 +231,15 @@ __device__ __forceinline__ void general_block(const float4* __restrict__ blk, co
   }
 }
 
-// The last split of target block tb to finish: sum the block's partials in split order (the
-// order of p2p_reduce_kernel, so the bits do not depend on which split arrived last), write the
-// targets, then drop the consumed partial lines from L2 (discard.global.L2: no write-back), so
-// the partials stay an L2-resident exchange instead of HBM traffic.
+// The last split of target block tb to finish: sum the block's partials in split order (so
+// the bits do not depend on which split arrived last), write the targets, then drop the
+// consumed partial lines from L2 (discard.global.L2: no write-back), so the partials stay an
+// L2-resident exchange instead of HBM traffic.  Compensated partials are the items' (hi, lo)
+// FP32 pairs, summed with Knuth's two-sum on the FP32 pipes (FP64 once per target: this GPU
+// runs a dependent chain of FP64 adds many times slower); plain partials are FP32 sums.
 template <bool COMP, int TB>
 __device__ __noinline__ void split_block_reduce(const P2PArgs& a, int tb, size_t pst) {
-  using T = typename std::conditional<COMP, double, float>::type;
+  using T = typename std::conditional<COMP, float2, float>::type;
   static_assert((TB * sizeof(T)) % 128 == 0, "a block's partial row is whole L2 lines");
   const T* part = static_cast<const T*>(a.part);
   for (int j = threadIdx.x; j < TB; j += blockDim.x) {
@@ -247,9 +249,22 @@ __device__ __noinline__ void split_block_reduce(const P2PArgs& a, int tb, size_t
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const T* p = part + (size_t)q * a.nsplit * pst + i;
-      T s = 0;
-      for (int k = 0; k < a.nsplit; ++k) s += __ldcg(p + (size_t)k * pst);
-      c[q] = (double)s;
+      if constexpr (COMP) {
+        float S = 0.0f, e = 0.0f;
+        for (int k = 0; k < a.nsplit; ++k) {
+          const float2 v = __ldcg(p + (size_t)k * pst);
+          const float u = __fadd_rn(S, v.x);
+          const float bv = __fsub_rn(u, S);
+          const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bv)), __fsub_rn(v.x, bv));
+          S = u;
+          e = __fadd_rn(e, __fadd_rn(err, v.y));
+        }
+        c[q] = (double)S + (double)e;
+      } else {
+        float sum = 0.0f;
+        for (int k = 0; k < a.nsplit; ++k) sum += __ldcg(p + (size_t)k * pst);
+        c[q] = (double)sum;
+      }
     }
     store_target<RES_VEL>(a, i, c);
   }
@@ -426,6 +441,20 @@ p2p_packed_kernel(const P2PArgs a) {
       for (int h = 0; h < 2; ++h) {
         const int i = tb * TB + warp * WT + (2 * p + h) * 32 + lane;
         if (i >= a.nt) continue;
+        if (fused && !a.direct) {
+          // partials for the in-kernel reduction, no FP64 arithmetic: (hi, lo) pairs or sums
+          if (COMP) {
+            float2* qp = static_cast<float2*>(a.part);
+            qp[((size_t)0 * a.nsplit + sp) * pst + i] = h ? make_float2(hu[p].y, lu[p].y) : make_float2(hu[p].x, lu[p].x);
+            qp[((size_t)1 * a.nsplit + sp) * pst + i] =
+                h ? make_float2(-hv[p].y, -lv[p].y) : make_float2(-hv[p].x, -lv[p].x);
+          } else {
+            float* qp = static_cast<float*>(a.part);
+            qp[((size_t)0 * a.nsplit + sp) * pst + i] = h ? u[p].y : u[p].x;
+            qp[((size_t)1 * a.nsplit + sp) * pst + i] = -(h ? vn[p].y : vn[p].x);
+          }
+          continue;
+        }
         double c[2];
         if (COMP) {
           c[0] = (double)(h ? hu[p].y : hu[p].x) + (double)(h ? lu[p].y : lu[p].x);

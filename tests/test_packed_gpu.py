@@ -259,13 +259,15 @@ def test_packed_gradient_results_vs_generic_and_fp64(ctx, restatement, result, t
             assert rel_err(a[ok], b[ok]) < tol, (v, k)
 
 
-@pytest.mark.parametrize("ns,nt", [(200_000, 1000), (20_000, 70_001), (60_000, 513)])
+@pytest.mark.parametrize("ns,nt", [(300_000, 300_001), (200_000, 1000), (20_000, 70_001)])
 @pytest.mark.parametrize("accum", [og.PLAIN_F32, og.COMPENSATED])
 @pytest.mark.parametrize("variant", [og.VARIANT_PACKED2, og.VARIANT_PACKED4])
 def test_split_reduce_in_kernel_is_deterministic(ctx, restatement, ns, nt, accum, variant):
-    """Many source splits per target block, reduced inside the velocity kernel: the block's last
-    split to finish sums the partials in split order, so repeated calls give the same bits
-    whichever split arrives last; the sums match FP64, ragged last block included."""
+    """Many source splits per target block.  At 300k x 300k the partials exceed 64 MB and are
+    reduced inside the velocity kernel: the block's last split to finish sums them in split
+    order, so repeated calls give the same bits whichever split arrives last; the smaller
+    shapes take the separate reduction launch.  The sums match FP64, ragged last block
+    included."""
     rng = np.random.default_rng(ns + nt + 10 * accum + variant)
     sx, sy, sr, ss = cloud(rng, ns, True)
     tx, ty, tr, _ = cloud(rng, nt, True)
