@@ -262,34 +262,49 @@ __global__ void __launch_bounds__(TREE_WARPS * 32) tree_eval_kernel(const TreeAr
     } else if (lev == 0) {
       // direct sum over the leaf's sources (warp-broadcast loads): with the core, or -- when every
       // pair lies in the core's far regime, the leaf being too close for its expansion -- with
-      // the far form 1/d^2 the core takes there
+      // the far form 1/d^2 the core takes there.  Two sources per f32x2 operation: the leaf is
+      // staged as pairs, ps[2 kp] = (-x, -x', -y, -y'), ps[2 kp + 1] = (z, z', -G, -G') for
+      // sources 2 kp and 2 kp + 1 (one load per lane; padding past the leaf's end has G = 0)
       const int cnt = min(TREE_LEAF, a.ns - q * TREE_LEAF);
       __syncwarp();
-      leafs[w][lane] = a.sp4[q * TREE_LEAF + min(lane, cnt - 1)];   // staged: one load per lane
+      {
+        const float4 p = a.sp4[q * TREE_LEAF + min(lane, cnt - 1)];
+        float* st = reinterpret_cast<float*>(&leafs[w][0]) + (lane >> 1) * 8 + (lane & 1);
+        st[0] = -p.x;
+        st[2] = -p.y;
+        st[4] = p.z;
+        st[6] = (lane < cnt) ? -p.w : 0.0f;
+      }
       __syncwarp();
       const float4* ps = leafs[w];
-      float su = 0.0f, sv = 0.0f;
+      const int np2 = (cnt + 1) >> 1;
+      const float2 tx2 = f2(tx, tx), ty2 = f2(ty, ty);
+      float2 au = f2(0.0f, 0.0f), av = f2(0.0f, 0.0f);   // sum -G K dy (= u), sum -G K dx (= -v)
       if (tree_far<CORE>(dmin2, gn.w + ztmax)) {
 #pragma unroll 4
-        for (int k = 0; k < cnt; ++k) {
-          const float4 p = ps[k];
-          const float dx = tx - p.x, dy = ty - p.y;
-          const float f = p.w * rcp_a(dx * dx + dy * dy);
-          su = fmaf(-f, dy, su);
-          sv = fmaf(f, dx, sv);
+        for (int kp = 0; kp < np2; ++kp) {
+          const float4 P = ps[2 * kp], Q = ps[2 * kp + 1];
+          const float2 dx = __fadd2_rn(tx2, f2(P.x, P.y)), dy = __fadd2_rn(ty2, f2(P.z, P.w));
+          const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+          const float2 fn = __fmul2_rn(f2(Q.z, Q.w), f2(rcp_a(d2.x), rcp_a(d2.y)));
+          au = __ffma2_rn(fn, dy, au);
+          av = __ffma2_rn(fn, dx, av);
         }
       } else {
-#pragma unroll 4
-        for (int k = 0; k < cnt; ++k) {
-          const float4 p = ps[k];
-          const float dx = tx - p.x, dy = ty - p.y;
-          float K, B;
-          core_eval<CORE, THICK, false, false>(dx * dx + dy * dy, p.z, tz, 0.0f, 0.0f, K, B);
-          const float f = p.w * K;
-          su = fmaf(-f, dy, su);
-          sv = fmaf(f, dx, sv);
+#pragma unroll 2
+        for (int kp = 0; kp < np2; ++kp) {
+          const float4 P = ps[2 * kp], Q = ps[2 * kp + 1];
+          const float2 dx = __fadd2_rn(tx2, f2(P.x, P.y)), dy = __fadd2_rn(ty2, f2(P.z, P.w));
+          const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+          float K0, K1, B;
+          core_eval<CORE, THICK, false, false>(d2.x, Q.x, tz, 0.0f, 0.0f, K0, B);
+          core_eval<CORE, THICK, false, false>(d2.y, Q.y, tz, 0.0f, 0.0f, K1, B);
+          const float2 fn = __fmul2_rn(f2(Q.z, Q.w), f2(K0, K1));
+          au = __ffma2_rn(fn, dy, au);
+          av = __ffma2_rn(fn, dx, av);
         }
       }
+      const float su = au.x + au.y, sv = -(av.x + av.y);
       if (v) {
         two_sum_acc(hu, lu, su);
         two_sum_acc(hv, lv, sv);
