@@ -648,7 +648,7 @@ def solve_bem_bodies(vort: Points, bodies, fs=(0.0, 0.0), nunk: int = 2, env: Ex
     bodies[k].omega.  The reference rebuilds only the blocks of bodies in relative motion
     (:147-193); here the whole matrix is rebuilt unless reuse_matrix (no body moved, none
     rotating), since assembling it costs about 2 % of a BEM step (4096 unknowns: 0.05 ms of
-    2.7 ms)."""
+    2.5 ms)."""
     bodies = list(bodies)
     joined, offs = join_surfaces(bodies)
     if augmented is None or not any(augmented):

@@ -579,3 +579,69 @@ def test_bodies_augmented_solve(ctx, golden, restatement, augmented):
             assert abs(bodies[k].omega - unperm[npu + k]) < 3e-4 * max(1.0, abs(unperm[npu + k]))
         else:
             assert bodies[k].omega is None
+
+
+def test_bodies_augmented_matrix_vortex_only(ctx, golden):
+    """The vortex-only system (one unknown per panel, src/Coefficients.h:366-385) of the two
+    rotating bodies: its panel block is the vortex-on-tangential part of the two-unknown
+    matrix, its rotation rows the panel lengths under the vortex unknowns, its rotation
+    columns the tangential components -- the even rows and columns of the reference's
+    two-unknown assembly (golden bodies_aug.npz)."""
+    g, bodies, _ = _two_rotating_bodies(golden)
+    n0, n1 = bodies[0].npan, bodies[1].npan
+    A1, _ = og.panels_on_panels_coeff_bodies(bodies, [True, True], nunk=1, context=ctx)
+    # engine order: panels of body 0, of body 1, rotation 0, rotation 1 -> reference order
+    ref_idx = np.concatenate([2 * np.arange(n0), 2 * n0 + 1 + 2 * np.arange(n1), [2 * n0, 2 * n0 + 1 + 2 * n1]])
+    R = g["A"].astype(np.float64)[np.ix_(ref_idx, ref_idx)]
+    pan = np.arange(n0 + n1)
+    rot = np.array([n0 + n1, n0 + n1 + 1])
+    assert rel_err(R[np.ix_(pan, pan)], A1[np.ix_(pan, pan)]) < 2e-5
+    assert rel_err(R[np.ix_(pan, rot)], A1[np.ix_(pan, rot)]) < 2e-5
+    np.testing.assert_allclose(A1[rot, :], R[rot, :], rtol=0, atol=1e-6 * np.max(np.abs(R[rot, :])))
+
+
+def test_bodies_augmented_three_bodies_solve(ctx, restatement):
+    """Three bodies, the first and last rotating: the rotation unknowns follow the body order
+    of the rotating bodies only; the solve equals an FP64 solve of the engine's own augmented
+    matrix with the restated FP64 right-hand side and the prescribed circulations, and the
+    middle body gets no rotation rate."""
+    bodies = [og.circle_panels(40, 0.8, center=(0.0, 0.0)), og.circle_panels(24, 0.5, center=(1.6, 0.3)),
+              og.circle_panels(30, 0.6, center=(-0.4, 1.5))]
+    aug = [True, False, True]
+    A, geom = og.panels_on_panels_coeff_bodies(bodies, aug, nunk=2, context=ctx)
+    npu = 2 * sum(b.npan for b in bodies)
+    assert A.shape == (npu + 2, npu + 2)
+    # rotation rows: each rotating body's panel lengths under its own vortex unknowns only
+    offs = np.cumsum([0] + [b.npan for b in bodies])
+    for r, k in ((npu, 0), (npu + 1, 2)):
+        b = bodies[k]
+        L = np.hypot(np.diff(np.append(b.nx, b.nx[0])), np.diff(np.append(b.ny, b.ny[0])))
+        row = A[r, :npu]
+        np.testing.assert_allclose(row[2 * offs[k]:2 * offs[k + 1]:2], L, rtol=1e-6)
+        others = np.ones(npu, bool)
+        others[2 * offs[k]:2 * offs[k + 1]:2] = False
+        assert not row[others].any()
+        assert abs(A[r, r] - 2 * geom[k, 0]) < 1e-9 * abs(A[r, r])
+    rng = np.random.default_rng(43)
+    n = 3000
+    x, y = rng.uniform(-2.0, 3.0, (2, n))
+    inside = np.zeros(n, bool)
+    for b, c, d in zip(bodies, ((0.0, 0.0), (1.6, 0.3), (-0.4, 1.5)), (0.8, 0.5, 0.6)):
+        inside |= np.hypot(x - c[0], y - c[1]) < 0.5 * d + 0.08
+    x, y = x[~inside].astype(np.float32), y[~inside].astype(np.float32)
+    s = rng.normal(0, 1e-2, x.size).astype(np.float32)
+    circ = [0.25, 0.0, -0.4]
+    rel = og.solve_bem_bodies(og.Points(x, y, np.full(x.size, 0.01, np.float32), s), bodies, fs=(1.0, 0.0),
+                              nunk=2, env=og.ExecEnv(accum=og.COMPENSATED, context=ctx), augmented=aug, circ_rhs=circ)
+    assert rel < 1e-12
+    joined, _ = og.join_surfaces([og.Surfaces(b.nx, b.ny, b.idx) for b in bodies])
+    pu, pv = restatement.points_affect_panels(x, y, s, joined.nx, joined.ny, joined.idx, fp64=True)
+    pu, pv = 1.0 + pu / (2 * np.pi), pv / (2 * np.pi)
+    rhs = np.concatenate([restatement.vels_to_rhs_panels(2, joined.nx, joined.ny, joined.idx, pu, pv, fp64=True),
+                          [circ[0], circ[2]]])
+    xr = np.linalg.solve(A, rhs)
+    got = np.stack([np.concatenate([b.vs for b in bodies]), np.concatenate([b.ss for b in bodies])], 1).ravel()
+    assert rel_err(xr[:npu], got) < 3e-4
+    assert abs(bodies[0].omega - xr[npu]) < 3e-4 * max(1.0, abs(xr[npu]))
+    assert abs(bodies[2].omega - xr[npu + 1]) < 3e-4 * max(1.0, abs(xr[npu + 1]))
+    assert bodies[1].omega is None
