@@ -158,7 +158,9 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int nst = (rq.ns + SRC_TILE - 1) / SRC_TILE;
   const int want_items = 24 * slots;
   int nsplit = std::max(1, (want_items + ntb - 1) / ntb);
-  nsplit = std::min(nsplit, std::max(1, nst / 4));
+  // at least two source tiles per split (20k sources: 39 splits, 0.156 ms per sum against
+  // 0.165 ms with four tiles per split, which left a third of the CTA slots idle)
+  nsplit = std::min(nsplit, std::max(1, nst / 2));
   const int tps = (nst + nsplit - 1) / nsplit;
   nsplit = (nst + tps - 1) / tps;
   const int nitems = ntb * nsplit;
