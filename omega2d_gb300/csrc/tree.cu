@@ -76,6 +76,7 @@ struct TreeArgs {
   int finalize;
   double fsx, fsy;
   int* status;
+  const unsigned* meta;   // radius extrema: [2] ~min, [3] max of the sources; [4], [5] of the targets
 };
 
 __device__ __forceinline__ float warp_min(float v) {
@@ -216,6 +217,19 @@ __global__ void __launch_bounds__(TREE_WARPS * 32) tree_eval_kernel(const TreeAr
   const float inf = __int_as_float(0x7f800000);
   const float tx = v ? a.tx[i] : 0.0f, ty = v ? a.ty[i] : 0.0f;
   const float tz = (THICK && v) ? radius_term(CORE, a.tr[i]) : 0.0f;
+  // Gaussian with one radius for every source (and every target): the near leaf sums take the
+  // packed form below, with the core's cut-offs on t = -x log2(e), x = d^2 / s^2
+  bool gunif = false;
+  float gcf = 0.0f, gcfl = 0.0f;
+  if constexpr (CORE == CORE_GAUSS) {
+    gunif = (~a.meta[2] == a.meta[3]) && (!THICK || ~a.meta[4] == a.meta[5]);
+    if (gunif) {
+      const float us2 = radius_term(CORE, __uint_as_float(a.meta[3])) +
+                        (THICK ? radius_term(CORE, __uint_as_float(a.meta[5])) : 0.0f);
+      gcf = __frcp_rn(us2);
+      gcfl = -gcf * kLog2e;
+    }
+  }
   const float bx0 = warp_min(v ? tx : inf), bx1 = warp_max(v ? tx : -inf);
   const float by0 = warp_min(v ? ty : inf), by1 = warp_max(v ? ty : -inf);
   const float ztmax = warp_max(tz);
@@ -287,6 +301,25 @@ __global__ void __launch_bounds__(TREE_WARPS * 32) tree_eval_kernel(const TreeAr
           const float2 dx = __fadd2_rn(tx2, f2(P.x, P.y)), dy = __fadd2_rn(ty2, f2(P.z, P.w));
           const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
           const float2 fn = __fmul2_rn(f2(Q.z, Q.w), f2(rcp_a(d2.x), rcp_a(d2.y)));
+          au = __ffma2_rn(fn, dy, au);
+          av = __ffma2_rn(fn, dx, av);
+        }
+      } else if (CORE == CORE_GAUSS && gunif) {
+        // (1 - e^-x)/d^2; x > 16 -> 1/d^2; x < 0.001 -> 1/s^2 (src/CoreFunc.h:111-181)
+        const float thr_far = -16.0f * kLog2e, thr_small = -0.001f * kLog2e;
+        const float2 cfl2 = f2(gcfl, gcfl), m1 = f2(-1.0f, -1.0f), one = f2(1.0f, 1.0f);
+#pragma unroll 2
+        for (int kp = 0; kp < np2; ++kp) {
+          const float4 P = ps[2 * kp], Q = ps[2 * kp + 1];
+          const float2 dx = __fadd2_rn(tx2, f2(P.x, P.y)), dy = __fadd2_rn(ty2, f2(P.z, P.w));
+          const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+          const float2 t = __fmul2_rn(d2, cfl2);
+          const float2 ood2 = f2(rcp_a(d2.x), rcp_a(d2.y));
+          const float2 ome = __ffma2_rn(f2(ex2_a(t.x), ex2_a(t.y)), m1, one);
+          float2 k = __fmul2_rn(ood2, ome);
+          k.x = (t.x < thr_far) ? ood2.x : ((t.x > thr_small) ? gcf : k.x);
+          k.y = (t.y < thr_far) ? ood2.y : ((t.y > thr_small) ? gcf : k.y);
+          const float2 fn = __fmul2_rn(f2(Q.z, Q.w), k);
           au = __ffma2_rn(fn, dy, au);
           av = __ffma2_rn(fn, dx, av);
         }
@@ -383,7 +416,8 @@ int run_tree(obs_context* ctx, int core, int flags, double fsx, double fsy, doub
   const size_t o_geo = o_t + 3 * al256(T * 4);
   const size_t o_box = o_geo + al256((size_t)total * sizeof(float4));
   const size_t o_coef = o_box + al256((size_t)total * sizeof(float4));
-  const size_t bytes = o_coef + al256((size_t)total * TREE_PMAX * sizeof(float2));
+  const size_t o_meta = o_coef + al256((size_t)total * TREE_PMAX * sizeof(float2));
+  const size_t bytes = o_meta + 256;
   int s = ctx->work.ensure(bytes, ctx->stream);
   if (s) return s;
   char* W = ctx->work.as<char>();
@@ -445,6 +479,18 @@ int run_tree(obs_context* ctx, int core, int flags, double fsx, double fsy, doub
   a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
   a.fsx = fsx; a.fsy = fsy;
   a.status = ctx->d_status;
+  // radius extrema for the Gaussian's uniform-radius leaf sums (zeroed: "not uniform")
+  unsigned* meta = reinterpret_cast<unsigned*>(W + o_meta);
+  if ((e = cudaMemsetAsync(meta, 0, 6 * sizeof(unsigned), st)) != cudaSuccess) return cuda_status(e);
+  if (core == CORE_GAUSS && sr) {
+    if ((e = p2p_launch_target_meta(sr, ns, meta, st)) != cudaSuccess) return cuda_status(e);
+    ++launches;
+    if (tr) {
+      if ((e = p2p_launch_target_meta(tr, nt, meta + 2, st)) != cudaSuccess) return cuda_status(e);
+      ++launches;
+    }
+  }
+  a.meta = meta;
   const int nwarps = (nt + 31) / 32;
   e = tree_eval(core, tr != nullptr, a, (nwarps + TREE_WARPS - 1) / TREE_WARPS, st);
   ++launches;

@@ -47,6 +47,24 @@ def test_tree_matches_fp64_direct_sum(ctx, restatement, core, thick):
     assert rel_err(u, targ.u) < TOL and rel_err(v, targ.v) < TOL
 
 
+@pytest.mark.parametrize("thick", [True, False])
+def test_tree_gaussian_uniform_radii_fp64(ctx, restatement, thick):
+    """Every source (and target) with one radius: the Gaussian's near leaf sums take the packed
+    uniform form (cut-offs x > 16 and x < 0.001 on t = -x log2 e); coincident pairs exercise
+    the small-x branch."""
+    rng = np.random.default_rng(321 + thick)
+    sx, sy, sr, ss = patch(rng, 12000)
+    tx, ty, tr, _ = patch(rng, 3000)
+    tx[:100], ty[:100] = sx[:100], sy[:100]
+    src = og.Points(sx, sy, sr, ss)
+    targ = og.Points(tx, ty, tr if thick else None, None)
+    og.points_affect_points_tree(src, targ, og.ExecEnv(og.CORE_GAUSSIAN, og.COMPENSATED, ctx))
+    u, v, _ = restatement.points_affect_points(og.CORE_GAUSSIAN, po.VELONLY, sx, sy, sr, ss, tx, ty,
+                                               tr if thick else None, fp64=True)
+    assert np.isfinite(targ.u).all() and np.isfinite(targ.v).all()
+    assert rel_err(u, targ.u) < TOL and rel_err(v, targ.v) < TOL
+
+
 def test_tree_self_interaction_against_direct_engine(ctx):
     """200,000 particles of the Gaussian patch on themselves (a seven-level tree): the treecode
     against the engine's compensated direct sum (itself within 1e-7 of FP64)."""
