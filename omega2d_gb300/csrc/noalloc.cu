@@ -100,7 +100,7 @@ extern "C" int obs_points_affect_points_noalloc(void* cuda_stream, int core, int
   const int nc = p2p_ncomp(res);
   const size_t elem = comp ? sizeof(double) : sizeof(float);
   int nsplit = std::max(1, (24 * slots + ntb - 1) / ntb);
-  nsplit = std::min(nsplit, std::max(1, nst / 2));
+  nsplit = std::min(nsplit, std::max(1, std::min(nst / 2, 512)));
   const size_t fit = kPartialBytes / ((size_t)nc * (size_t)nt * elem);
   nsplit = std::max(1, std::min<int>(nsplit, (int)std::min<size_t>(fit, (size_t)nst)));
   const int tps = (nst + nsplit - 1) / nsplit;

@@ -159,8 +159,10 @@ int run_p2p(obs_context* ctx, const P2PRequest& rq) {
   const int want_items = 24 * slots;
   int nsplit = std::max(1, (want_items + ntb - 1) / ntb);
   // at least two source tiles per split (20k sources: 39 splits, 0.156 ms per sum against
-  // 0.165 ms with four tiles per split, which left a third of the CTA slots idle)
-  nsplit = std::min(nsplit, std::max(1, nst / 2));
+  // 0.165 ms with four tiles per split, which left a third of the CTA slots idle), and at most
+  // 512 splits: few targets against many sources (10k probes, 500k sources) otherwise make
+  // over a thousand splits whose partials and reduction chains cost more than they balance
+  nsplit = std::min(nsplit, std::max(1, std::min(nst / 2, 512)));
   const int tps = (nst + nsplit - 1) / nsplit;
   nsplit = (nst + tps - 1) / tps;
   const int nitems = ntb * nsplit;
