@@ -207,7 +207,8 @@ __global__ void diag_inv_kernel(const double* __restrict__ A, int n, double* __r
 // entries carry a relative error below 2^-23, and stops at a relative reduction of 2^-20; the
 // restart residual b - A x is formed with the FP64 matrix, so every restart corrects the
 // solution against A itself (iterative refinement): the final residual meets the FP64
-// tolerance.  Inside the cycle the basis, w, the Gram-Schmidt dot products, the sums over
+// tolerance.  A matrix whose entries are all exact in FP32 (bit 1 of the split's flag clear)
+// is its own plane: its cycles run to the tolerance.  Inside the cycle the basis, w, the Gram-Schmidt dot products, the sums over
 // blocks and the updates are double-float (hi + lo FP32 pairs, about 2^-48) on the FP32 pipes;
 // the preconditioner is Dinv rounded to FP32 (used alike in the operator and in the update of
 // x); the Hessenberg matrix, Givens rotations, back substitution and the update of x are FP64.
@@ -230,6 +231,8 @@ __device__ __forceinline__ float hi_bits(double a, int& bad) {
   const unsigned long long mant = u & ((1ull << 52) - 1);
   const unsigned sign = (unsigned)(u >> 63) << 31;
   bad |= (e != 0 && (e < 1023 - 99 || e > 1023 + 99)) || (e == 0 && mant != 0);
+  // bit 1: an entry the plane truncates (A_hi != A)
+  bad |= (mant & ((1ull << 29) - 1)) ? 2 : 0;
   if (e == 0) return __uint_as_float(sign);
   return __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
 }
@@ -247,7 +250,8 @@ __global__ void split_hi_kernel(const double* __restrict__ A, int n, float2* __r
     const float hi = (c + 1 < N) ? hi_bits(A[(c + 1) * N + i], bad) : 0.0f;
     AH[k] = make_float2(lo, hi);
   }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(range_flag, 1);
+  bad = __syncthreads_or(bad & 1) | (__syncthreads_or(bad & 2) ? 2 : 0);
+  if (bad && threadIdx.x == 0) atomicOr(range_flag, bad);
 }
 
 struct GcArgs {
@@ -811,7 +815,10 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   if (e == cudaSuccess) e = cudaMemcpyAsync(&x_nonzero, gbar + 2, 4, cudaMemcpyDeviceToHost, strm);
   if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
   if (e != cudaSuccess) return cuda_status(e);
-  if (range_bad) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
+  if (range_bad & 1) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
+  // every entry exact in FP32 (the engine's BEM matrices): the plane is A itself, so a cycle
+  // runs to the tolerance instead of stopping at the refinement target
+  const double eta_cycle = (range_bad & 2) ? kRefineEta : 0.0;
   const double bref = (bnorm == 0.0) ? 1.0 : bnorm;   // src/BEM.h:227-229 divides by 1 then
   GmState h0{0, 0, 0.0, tol * bref, tol * bref};
   if ((e = cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, strm)) != cudaSuccess) return cuda_status(e);
@@ -848,7 +855,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     prev_rn = rn;
     rel = rn / bref;
     if (!(rn > tol * bref) || total_it >= maxiter) break;   // converged (or NaN) / out of budget
-    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m, fused ? kRefineEta : 0.0);
+    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m, fused ? eta_cycle : 0.0);
     scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, nrm, V, nullptr);
     launched(2);
     const int mc = std::min(m, maxiter - total_it);
