@@ -369,21 +369,26 @@ struct GcRows {
   int nq;     // row groups this block owns
 };
 
-// this block's share of V_k . w (k <= j) into P[blockIdx.x * ld + k], double-float; with
-// `norm`, also w . w into slot j + 1
-__device__ void gc_partial_dots(const GcRows& R, int j, bool norm, int ld, float2* P, float2* sh) {
+// this block's partials of iteration j's dot products, double-float, into P[blockIdx.x * ld +
+// k]: k <= j: v_k . w; j < k <= 2j: v_(k-j-1) . v_j (the new column of the basis' Gram
+// matrix); 2j + 1: w . w; 2j + 2: v_j . v_j
+__device__ void gc_partial_dots_gram(const GcRows& R, int j, int ld, float2* P, float2* sh) {
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  const int kmax = norm ? j + 1 : j;
-  for (int k = wp; k <= kmax; k += GC_WARPS) {
+  const int cnt = 2 * j + 3;
+  for (int k = wp; k < cnt; k += GC_WARPS) {
     float2 s = make_float2(0.0f, 0.0f);
     for (int q = 0; q < R.nq; ++q) {
       const float2 w = R.ws[q * 32 + lane];
+      const float2 vj = R.Vs[(size_t)j * R.RB + q * 32 + lane];
       float2 t;
       if (k <= j) {
         t = df_mul(R.Vs[(size_t)k * R.RB + q * 32 + lane], w);
-      } else {                                   // w . w = hi^2 + 2 hi lo (+ lo^2, dropped)
-        t = two_prod(w.x, w.x);
-        t.y = __fmaf_rn(2.0f * w.x, w.y, t.y);
+      } else if (k <= 2 * j) {
+        t = df_mul(R.Vs[(size_t)(k - j - 1) * R.RB + q * 32 + lane], vj);
+      } else {
+        const float2 x = (k == 2 * j + 1) ? w : vj;   // x . x = hi^2 + 2 hi lo
+        t = two_prod(x.x, x.x);
+        t.y = __fmaf_rn(2.0f * x.x, x.y, t.y);
       }
       s = df_sum(s, t);
     }
@@ -391,7 +396,20 @@ __device__ void gc_partial_dots(const GcRows& R, int j, bool norm, int ld, float
     if (lane == 0) sh[k] = s;
   }
   __syncthreads();
-  for (int k = threadIdx.x; k <= kmax; k += GC_THREADS) P[(size_t)blockIdx.x * ld + k] = sh[k];
+  for (int k = threadIdx.x; k < cnt; k += GC_THREADS) P[(size_t)blockIdx.x * ld + k] = sh[k];
+}
+
+// out = G x over the first n entries (G the basis' Gram matrix, row-major with stride ldg, in
+// shared memory), double-float, one warp per row in a fixed order
+__device__ void gc_gram_matvec(const float2* G, int ldg, int n, const float2* x, float2* out) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  for (int k = wp; k < n; k += GC_WARPS) {
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int l = lane; l < n; l += 32) s = df_sum(s, df_mul(G[(size_t)k * ldg + l], x[l]));
+    s = warp_sum_df(s);
+    if (lane == 0) out[k] = s;
+  }
+  __syncthreads();
 }
 
 // sum_{k <= j} V_k[r] c[k] for local row group q in double-float (warps split k, fixed-order
@@ -430,10 +448,13 @@ __device__ __forceinline__ void df2_acc(float2 a, float2 xh, float2 nxh, float2 
 // (column-major A: a warp reads 256 contiguous bytes of the paired hi plane per column pair)
 // and keep those rows of the basis in shared memory; only the split vector Dinv v_j and the
 // per-block partial sums cross between blocks.  Iteration j:
-//   (1) w = A Dinv v_j on the owned rows; partial V^T w                         -> barrier
-//   (2) h = V^T w; w -= V h; partial V^T w and w^T w                            -> barrier
-//   (3) h2 = V^T w; ||w - V h2||^2 = w^T w - h2^T h2 (V orthonormal);
-//       v_{j+1} = (w - V h2) / ||.|| on the owned rows; H column h + h2          -> barrier
+//   (1) w = A Dinv v_j on the owned rows; partials of c = V^T w, of the Gram column V^T v_j,
+//       of w . w and v_j . v_j                                                      -> barrier
+//   (2) the Gram matrix G = V^T V gains its column j; classical Gram-Schmidt twice with the
+//       second pass from G (V^T (w - V c) = c - G c): h = 2 c - G c, ||w - V h||^2 =
+//       w.w - 2 h.c + h.G h; v_{j+1} = (w - V h) / ||.|| on the owned rows; H column h -> barrier
+// Two grid barriers per iteration (three with a second dot-product pass); orthogonality lost
+// in forming w - V h shows in the next Gram column and is projected out one iteration later.
 // The basis and the Gram-Schmidt arithmetic are double-float, as is the operator product; the
 // Hessenberg matrix, the Givens rotations, g and the back substitution are FP64.  Every block
 // keeps H, the rotations and g in shared memory: the rotations of column j-1 run on the last
@@ -444,7 +465,9 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
   __shared__ float2 redf[GC_WARPS][32];
   __shared__ double Hs[GC_MAXM][GC_MAXM + 1];   // Hs[j][k]: rotated column j (R factor)
   __shared__ float2 h1[GC_MAXM + 2];
-  __shared__ float2 sh[GC_MAXM + 2];
+  __shared__ float2 sh[2 * GC_MAXM + 3];
+  __shared__ float2 gx[GC_MAXM + 1];
+  __shared__ float2 wws;
   __shared__ double yv[GC_MAXM];
   __shared__ double gs[GC_MAXM + 1];
   __shared__ double css[GC_MAXM], sns[GC_MAXM];
@@ -455,15 +478,17 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int ngroups = (a.n + 31) / 32;
   const int npairs = (a.n + 1) / 2;
-  const int ld = a.m + 2;
+  const int ld = 2 * a.m + 3;
   GcRows R;
   R.RB = 32 * a.gpb;
   R.Vs = reinterpret_cast<float2*>(dyn);
   R.ws = R.Vs + (size_t)(a.m + 1) * R.RB;
   R.ds = dyn + (size_t)2 * (a.m + 2) * R.RB;
+  // the basis' Gram matrix G[k][l] = v_k . v_l (k, l <= j), double-float, symmetric
+  const int ldg = a.m + 1;
+  float2* gram = reinterpret_cast<float2*>(dyn + (size_t)(2 * (a.m + 2) + 1) * R.RB);
   R.nq = ((int)blockIdx.x < ngroups) ? (ngroups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   float2* P1 = a.P;
-  float2* P2 = a.P + (size_t)gridDim.x * ld;
   // the last warp applies the Givens rotations to column j-1 while the others form A Dinv v_j
   const bool gwarp = (wp == GC_WARPS - 1);
   const int per = (npairs + GC_WARPS - 2) / (GC_WARPS - 1);
@@ -592,25 +617,37 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
       kd = j;
       break;
     }
-    gc_partial_dots(R, j, false, ld, P1, sh);
+    // (2) one pass of dot products: c = V^T w, the Gram column of v_j, w . w, v_j . v_j
+    gc_partial_dots_gram(R, j, ld, P1, sh);
     if (!gc_barrier(a.bar, a.status, nb++)) return;
-    // (2)
-    gc_sum_partials(P1, ld, j + 1, h1);
-    for (int q = 0; q < R.nq; ++q) {
-      const float2 t = gc_vsum(R, j, q, h1, redf);
-      if (wp == 0) R.ws[q * 32 + lane] = df_sum(R.ws[q * 32 + lane], make_float2(-t.x, -t.y));
+    gc_sum_partials(P1, ld, 2 * j + 3, sh);
+    for (int k = threadIdx.x; k <= j; k += GC_THREADS) {
+      const float2 g = (k < j) ? sh[j + 1 + k] : sh[2 * j + 2];
+      gram[(size_t)k * ldg + j] = g;
+      gram[(size_t)j * ldg + k] = g;
+      h1[k] = sh[k];
     }
+    if (threadIdx.x == 0) wws = sh[2 * j + 1];
     __syncthreads();
-    gc_partial_dots(R, j, true, ld, P2, sh);
-    if (!gc_barrier(a.bar, a.status, nb++)) return;
-    // (3)
-    gc_sum_partials(P2, ld, j + 2, sh);
+    // (3) classical Gram-Schmidt twice, the second pass from the Gram matrix G = V^T V (which
+    //     equals V^T (w - V c) in exact arithmetic): h = c + (c - G c) = 2 c - G c, and
+    //     ||w - V h||^2 = w.w - 2 h.c + h.G h; then v_{j+1} = (w - V h) / ||.||
+    gc_gram_matvec(gram, ldg, j + 1, h1, gx);                                  // gx = G c
+    for (int k = threadIdx.x; k <= j; k += GC_THREADS)
+      gx[k] = df_sum(df_scale(2.0f, h1[k]), make_float2(-gx[k].x, -gx[k].y));   // gx = h
+    __syncthreads();
+    gc_gram_matvec(gram, ldg, j + 1, gx, sh);                                  // sh = G h
     if (wp == 0) {
-      float s2 = 0.0f;
-      for (int k = lane; k <= j; k += 32) s2 = fmaf(sh[k].x, sh[k].x, s2);
-      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(FULL, s2, o);
+      float2 hc = make_float2(0.0f, 0.0f), hgh = make_float2(0.0f, 0.0f);
+      for (int k = lane; k <= j; k += 32) {
+        hc = df_sum(hc, df_mul(gx[k], h1[k]));
+        hgh = df_sum(hgh, df_mul(gx[k], sh[k]));
+      }
+      hc = warp_sum_df(hc);
+      hgh = warp_sum_df(hgh);
       if (lane == 0) {
-        const float nrm2 = (sh[j + 1].x + sh[j + 1].y) - s2;
+        const float2 t = df_sum(df_sum(wws, df_scale(-2.0f, hc)), hgh);
+        const float nrm2 = t.x + t.y;
         const float nr = nrm2 > 0.0f ? sqrtf(nrm2) : 0.0f;
         nrm_inv[0] = nr;
         nrm_inv[1] = nr > 0.0f ? 1.0f / nr : 0.0f;
@@ -619,7 +656,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     __syncthreads();
     const float inv = nrm_inv[1];
     for (int q = 0; q < R.nq; ++q) {
-      const float2 t = gc_vsum(R, j, q, sh, redf);
+      const float2 t = gc_vsum(R, j, q, gx, redf);
       if (wp == 0) {
         const int i = row(q);
         const float2 w2 = df_sum(R.ws[q * 32 + lane], make_float2(-t.x, -t.y));
@@ -629,8 +666,7 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
         if (i < a.n) put_split(i, v, R.ds[q * 32 + lane]);
       }
     }
-    for (int k = threadIdx.x; k <= j; k += GC_THREADS)
-      Hs[j][k] = ((double)h1[k].x + (double)sh[k].x) + ((double)h1[k].y + (double)sh[k].y);
+    for (int k = threadIdx.x; k <= j; k += GC_THREADS) Hs[j][k] = (double)gx[k].x + (double)gx[k].y;
     if (threadIdx.x == 0) Hs[j][j + 1] = (inv > 0.0f) ? 1.0 / (double)inv : 0.0;
     if (!gc_barrier(a.bar, a.status, nb++)) return;
   }
@@ -750,7 +786,8 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   const int ngroups = (n + 31) / 32;
   const int gc_grid = std::min(ngroups, std::max(1, gc_occ) * ctx->num_sms);
   const int gc_gpb = (ngroups + gc_grid - 1) / gc_grid;
-  const size_t gc_smem = (size_t)(2 * (m + 2) + 1) * 32 * gc_gpb * sizeof(float);
+  const size_t gc_smem = (size_t)(2 * (m + 2) + 1) * 32 * gc_gpb * sizeof(float) +
+                         (size_t)(m + 1) * (m + 1) * sizeof(float2);
   bool fused = coop && gc_occ > 0 && m <= GC_MAXM && ctx->kernel_variant != OBS_VARIANT_GENERIC;
   if (fused) {
     cudaFuncAttributes fa{};
