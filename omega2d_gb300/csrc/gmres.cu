@@ -241,14 +241,21 @@ __device__ __forceinline__ float hi_bits(double a, int& bad) {
 // pads an odd order), so one 8-byte load feeds the f32x2 product of two columns
 __global__ void split_hi_kernel(const double* __restrict__ A, int n, float2* __restrict__ AH,
                                 int* __restrict__ range_flag) {
+  // column pairs over blockIdx.y (grid-stride), rows over the block's threads: coalesced reads
+  // of both columns and writes of the pair, no integer division per element
   int bad = 0;
-  const size_t N = (size_t)n, total = (N + 1) / 2 * N;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
-    const size_t cp = k / N, i = k - cp * N;
-    const size_t c = 2 * cp;
-    const float lo = hi_bits(A[c * N + i], bad);
-    const float hi = (c + 1 < N) ? hi_bits(A[(c + 1) * N + i], bad) : 0.0f;
-    AH[k] = make_float2(lo, hi);
+  const size_t N = (size_t)n;
+  const int npairs = (n + 1) / 2;
+  for (int cp = blockIdx.y; cp < npairs; cp += gridDim.y) {
+    const size_t c = 2 * (size_t)cp;
+    const double* a0 = A + c * N;
+    const double* a1 = A + (c + 1) * N;
+    const bool two = c + 1 < N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const float lo = hi_bits(a0[i], bad);
+      const float hi = two ? hi_bits(a1[i], bad) : 0.0f;
+      AH[(size_t)cp * N + i] = make_float2(lo, hi);
+    }
   }
   bad = __syncthreads_or(bad & 1) | (__syncthreads_or(bad & 2) ? 2 : 0);
   if (bad && threadIdx.x == 0) atomicOr(range_flag, bad);
@@ -842,7 +849,11 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
   launched(1);
   if (fused) {
-    split_hi_kernel<<<4 * ctx->num_sms, 256, 0, strm>>>(A, n, AH, reinterpret_cast<int*>(gbar + 1));
+    {
+      const int bx = std::max(1, std::min((n + 255) / 256, 16));
+      const int by = std::max(1, std::min((n + 1) / 2, (8 * ctx->num_sms + bx - 1) / bx));
+      split_hi_kernel<<<dim3(bx, by), 256, 0, strm>>>(A, n, AH, reinterpret_cast<int*>(gbar + 1));
+    }
     launched(1);
   }
   double bnorm = 0.0;
