@@ -98,6 +98,22 @@ __device__ __forceinline__ void panel_uv_star_fast2(float2 x0, float2 y0, float2
   const float2 dx1 = sub2(tx, x1), dy1 = sub2(ty, y1);
   const float2 cr = sub2(__fmul2_rn(dx0, py), __fmul2_rn(dy0, px));     // (t - p0) x (p1 - p0)
   const float2 dt = __ffma2_rn(dx0, dx1, __fmul2_rn(dy0, dy1));
+  // the half-log's operands: r1^2, r0^2 - r1^2 formed exactly, and r0^2 + r1^2
+  const float2 r1 = __ffma2_rn(dx1, dx1, __fmul2_rn(dy1, dy1));
+  const float2 diff = __ffma2_rn(px, __fadd2_rn(dx0, dx1), __fmul2_rn(py, __fadd2_rn(dy0, dy1)));
+  const float2 den = __ffma2_rn(f2(2.0f, 2.0f), r1, diff);
+  if (fabsf(cr.x) < 0.05f * dt.x && fabsf(cr.y) < 0.05f * dt.y && fabsf(diff.x) < 0.05f * den.x &&
+      fabsf(diff.y) < 0.05f * den.y) {
+    // both targets more than about twenty panel lengths away: the arctangent ratio and the
+    // atanh argument are below 0.05, where both odd series end at the 5th power (the next
+    // term is below 2.3e-9 relative)
+    const float2 r = __fmul2_rn(cr, f2(rcp_approx(dt.x), rcp_approx(dt.y)));
+    const float2 sv = __fmul2_rn(diff, f2(rcp_approx(den.x), rcp_approx(den.y)));
+    const float2 t = __fmul2_rn(r, r), ts = __fmul2_rn(sv, sv);
+    us = __ffma2_rn(__fmul2_rn(r, t), __ffma2_rn(t, f2(0.2f, 0.2f), f2(-1.0f / 3.0f, -1.0f / 3.0f)), r);
+    vs = __ffma2_rn(__fmul2_rn(sv, ts), __ffma2_rn(ts, f2(0.2f, 0.2f), f2(1.0f / 3.0f, 1.0f / 3.0f)), sv);
+    return;
+  }
   if (fabsf(cr.x) < 0.2f * dt.x && fabsf(cr.y) < 0.2f * dt.y) {
     // both targets see the panel under less than atan(0.2) from in front (every target more
     // than a few panel lengths away): atan of the signed ratio by its odd Taylor series to
@@ -127,9 +143,6 @@ __device__ __forceinline__ void panel_uv_star_fast2(float2 x0, float2 y0, float2
     us = f2(atan2_fix(p.x, cr.x, dt.x, ay0, ax0), atan2_fix(p.y, cr.y, dt.y, ay1, ax1));
   }
   // half-log: atanh series of (rho - 1)/(rho + 1)
-  const float2 r1 = __ffma2_rn(dx1, dx1, __fmul2_rn(dy1, dy1));
-  const float2 diff = __ffma2_rn(px, __fadd2_rn(dx0, dx1), __fmul2_rn(py, __fadd2_rn(dy0, dy1)));
-  const float2 den = __ffma2_rn(f2(2.0f, 2.0f), r1, diff);
   const float2 sv = __fmul2_rn(diff, f2(rcp_approx(den.x), rcp_approx(den.y)));
   const float2 ts = __fmul2_rn(sv, sv);
   float2 q = __ffma2_rn(ts, f2(1.0f / 9.0f, 1.0f / 9.0f), f2(1.0f / 7.0f, 1.0f / 7.0f));
