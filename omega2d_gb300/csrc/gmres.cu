@@ -37,12 +37,14 @@ struct GmState {
                    // products use the FP32 plane of A (iterative refinement)
 };
 
-// part[c][i] = sum_{j in chunk c} A[j*n + i] * (x[j] * dinv[j])   (column-major A)
+// part[c][i] = sum_{j in chunk c} A[j*n + i] * (x[j] * dinv[j])   (column-major A); nothing when
+// nz is given and *nz == 0 (x known to be zero)
 __global__ void __launch_bounds__(GM_THREADS) gemv_part_kernel(const double* __restrict__ A, int n,
                                                                const double* __restrict__ x,
                                                                const double* __restrict__ dinv,
-                                                               double* __restrict__ part, const GmState* st) {
-  if (st && st->done) return;
+                                                               double* __restrict__ part, const GmState* st,
+                                                               const unsigned* nz = nullptr) {
+  if ((st && st->done) || (nz && *nz == 0)) return;
   __shared__ double xs[GM_CHUNK];
   const int c = blockIdx.y;
   const int j0 = c * GM_CHUNK, j1 = min(n, j0 + GM_CHUNK);
@@ -57,12 +59,16 @@ __global__ void __launch_bounds__(GM_THREADS) gemv_part_kernel(const double* __r
   part[(size_t)c * n + i] = s;
 }
 
-// y = sum_c part[c]  (or y = b - sum when b is given)
+// y = sum_c part[c]  (or y = b - sum when b is given; y = b when nz is given and *nz == 0)
 __global__ void gemv_sum_kernel(const double* __restrict__ part, int nchunk, int n, const double* __restrict__ b,
-                                double* __restrict__ y, const GmState* st) {
+                                double* __restrict__ y, const GmState* st, const unsigned* nz = nullptr) {
   if (st && st->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (nz && *nz == 0) {
+    y[i] = b[i];
+    return;
+  }
   double s = 0.0;
   for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * n + i];
   y[i] = b ? b[i] - s : s;
@@ -112,10 +118,16 @@ __global__ void hadd_kernel(double* __restrict__ h, const double* __restrict__ h
   for (int k = threadIdx.x; k < cnt; k += blockDim.x) h[k] += h2[k];
 }
 
-// ||w|| into *out (one block)
+// ||w|| into *out (one block); *alt instead when nz is given and *nz == 0 (w a copy of the
+// vector whose norm *alt holds)
 __global__ void __launch_bounds__(1024) norm_kernel(const double* __restrict__ w, int n, double* out,
-                                                     const GmState* st) {
+                                                     const GmState* st, const unsigned* nz = nullptr,
+                                                     const double* alt = nullptr) {
   if (st && st->done) return;
+  if (nz && *nz == 0) {
+    if (threadIdx.x == 0) *out = *alt;
+    return;
+  }
   __shared__ double sh[32];
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(w[i], w[i], s);
@@ -138,13 +150,17 @@ __global__ void scale_kernel(const double* __restrict__ w, int n, const double* 
   if (i < n) v[i] = w[i] / *nrm;
 }
 
-// start of a cycle: beta = ||r||, g = (beta, 0, ...), V_0 = r / beta; done when beta is small;
-// the cycle's target is max(tolabs, eta * beta)
-__global__ void cycle_start_kernel(GmState* st, const double* nrm, double* g, int m, double eta) {
+// start of a cycle: beta = ||r||, g = (beta, 0, ...), V_0 = r / beta; done when beta is at most
+// tolabs = tol ||b|| (tol alone when b = 0, src/BEM.h:227-229); the cycle's target is
+// max(tolabs, eta beta), eta applying only when the plane's flag says that A's entries were
+// rounded to FP32 (bit 1)
+__global__ void cycle_start_kernel(GmState* st, const double* nrm, const double* bnrm, double tol, double* g, int m,
+                                   double eta, const unsigned* plane_flag) {
+  st->tolabs = tol * ((*bnrm == 0.0) ? 1.0 : *bnrm);
   st->beta = *nrm;
   st->kdone = 0;
   st->done = (*nrm <= st->tolabs) ? 1 : 0;
-  st->tolcyc = fmax(st->tolabs, eta * *nrm);
+  st->tolcyc = fmax(st->tolabs, ((*plane_flag & 2u) ? eta : 0.0) * *nrm);
   for (int k = 0; k <= m; ++k) g[k] = 0.0;
   g[0] = *nrm;
 }
@@ -272,6 +288,7 @@ struct GcArgs {
   double* x;
   float2* P;                                    // partials (double-float): [2][grid][m+2]
   unsigned* bar;                                // arrival counter, zeroed before each launch
+  const unsigned* plane_flag;                   // bit 0: entries out of the plane's range
   GmState* st;
   int* status;
 };
@@ -512,6 +529,11 @@ __global__ void __launch_bounds__(GC_THREADS, 1) gmres_cycle_kernel(const GcArgs
     lp[i & 1] = -e;
   };
   unsigned nb = 0;
+  // entries the plane cannot carry: nothing is done, and the host finishes with FP64 products
+  if (*a.plane_flag & 1u) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->kdone = 0;
+    return;
+  }
 
   if (threadIdx.x == 0) {
     gs[0] = a.st->beta;
@@ -842,8 +864,9 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   const dim3 ggrid(gb, nchunk);
   auto launched = [&](int k) { ctx->launches += k; };
 
+  // nrm[0]: the current residual norm; nrm[1]: ||b||
   diag_inv_kernel<<<gb, GM_THREADS, 0, strm>>>(A, n, dinv);
-  norm_kernel<<<1, 1024, 0, strm>>>(b, n, nrm, nullptr);
+  norm_kernel<<<1, 1024, 0, strm>>>(b, n, nrm + 1, nullptr);
   launched(2);
   if ((e = cudaMemsetAsync(gbar, 0, 3 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
   nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
@@ -856,60 +879,59 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     }
     launched(1);
   }
-  double bnorm = 0.0;
-  int range_bad = 0, x_nonzero = 0;
-  e = cudaMemcpyAsync(&bnorm, nrm, 8, cudaMemcpyDeviceToHost, strm);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&range_bad, gbar + 1, 4, cudaMemcpyDeviceToHost, strm);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&x_nonzero, gbar + 2, 4, cudaMemcpyDeviceToHost, strm);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
-  if (e != cudaSuccess) return cuda_status(e);
-  if (range_bad & 1) fused = false;   // entries the FP32 planes cannot carry: FP64 products throughout
-  // every entry exact in FP32 (the engine's BEM matrices): the plane is A itself, so a cycle
-  // runs to the tolerance instead of stopping at the refinement target
-  const double eta_cycle = (range_bad & 2) ? kRefineEta : 0.0;
-  const double bref = (bnorm == 0.0) ? 1.0 : bnorm;   // src/BEM.h:227-229 divides by 1 then
-  GmState h0{0, 0, 0.0, tol * bref, tol * bref};
-  if ((e = cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, strm)) != cudaSuccess) return cuda_status(e);
 
-  // r = b - A x in FP64 (the true residual), its norm into nrm
-  auto residual = [&]() {
-    gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, x, nullptr, part, nullptr);
-    gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, b, w, nullptr);
-    norm_kernel<<<1, 1024, 0, strm>>>(w, n, nrm, nullptr);
+  // r = b - A x in FP64 (the true residual) into w, its norm into nrm[0]; with nz, a zero x
+  // (known on the device only) gives r = b and ||b|| without the product
+  auto residual = [&](const unsigned* nz) {
+    gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, x, nullptr, part, nullptr, nz);
+    gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, b, w, nullptr, nz);
+    norm_kernel<<<1, 1024, 0, strm>>>(w, n, nrm, nullptr, nz, nrm + 1);
     launched(3);
   };
-  if (x_nonzero) {
-    residual();
-  } else {   // zero initial guess: r = b, and nrm already holds ||b||
-    if ((e = cudaMemcpyAsync(w, b, N * 8, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess) return cuda_status(e);
-  }
+  residual(gbar + 2);
+  // The first cycle is launched without a host round trip: its start kernel forms the tolerance
+  // from ||b|| and stops at once when the initial residual meets it, and the fused cycle returns
+  // at once when the plane cannot carry A (the loop then continues with FP64 products).  After
+  // each cycle one round trip reads the true residual norm, the cycle's start norm and
+  // iteration count, ||b||, the plane's flag and the status block (a barrier that gave up
+  // leaves its record there).
   int total_it = 0;
-  double rel = 0.0, prev_rn = -1.0;
-  for (;;) {
-    // one host round trip per cycle: the true residual norm, the cycle's iteration count and
-    // the status block (a barrier that gave up leaves its record there)
-    double rn = 0.0;
-    int kd = 0, flag = 0;
-    e = cudaMemcpyAsync(&rn, nrm, 8, cudaMemcpyDeviceToHost, strm);
-    if (e == cudaSuccess && total_it > 0) e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
-    if (e == cudaSuccess && total_it > 0) e = cudaMemcpyAsync(&flag, ctx->d_status, 4, cudaMemcpyDeviceToHost, strm);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
-    if (e != cudaSuccess) return cuda_status(e);
-    if (flag) return take_device_status(ctx);
-    if (total_it > 0) total_it += std::max(kd, 1) - 1;
-    // a refinement cycle (FP32 plane) that did not halve the true residual: A is too
-    // ill-conditioned for its FP32 entries, so finish with FP64 products throughout
-    if (fused && prev_rn > 0.0 && !(rn < 0.5 * prev_rn)) fused = false;
-    prev_rn = rn;
-    rel = rn / bref;
-    if (!(rn > tol * bref) || total_it >= maxiter) break;   // converged (or NaN) / out of budget
-    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, g, m, fused ? eta_cycle : 0.0);
+  double rel = 0.0;
+  for (bool check = false;; check = true) {
+    if (check) {
+      double rn = 0.0, bnorm = 0.0, beta = 0.0;
+      int kd = 0, flag = 0;
+      unsigned range_bad = 0;
+      e = cudaMemcpyAsync(&rn, nrm, 8, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&bnorm, nrm + 1, 8, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&beta, &st->beta, 8, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&kd, &st->kdone, 4, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&range_bad, gbar + 1, 4, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, ctx->d_status, 4, cudaMemcpyDeviceToHost, strm);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
+      if (e != cudaSuccess) return cuda_status(e);
+      if (flag) return take_device_status(ctx);
+      const double bref = (bnorm == 0.0) ? 1.0 : bnorm;   // src/BEM.h:227-229 divides by 1 then
+      rel = rn / bref;
+      bool stalled = false;
+      if (fused && (range_bad & 1u)) {
+        fused = false;   // entries the FP32 plane cannot carry: FP64 products throughout
+      } else {
+        total_it += kd;
+        stalled = kd <= 0;
+        // a refinement cycle (FP32 plane) that did not halve the true residual: A is too
+        // ill-conditioned for its FP32 entries, so finish with FP64 products throughout
+        if (fused && kd > 0 && !(rn < 0.5 * beta)) fused = false;
+      }
+      if (!(rn > tol * bref) || total_it >= maxiter || stalled) break;   // converged (or NaN) / budget
+    }
+    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, nrm + 1, tol, g, m, fused ? kRefineEta : 0.0, gbar + 1);
     scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, nrm, V, nullptr);
     launched(2);
     const int mc = std::min(m, maxiter - total_it);
     if (fused) {
       if ((e = cudaMemsetAsync(gbar, 0, sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
-      GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvp, gvl, x, gpart, gbar, st, ctx->d_status};
+      GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvp, gvl, x, gpart, gbar, gbar + 1, st, ctx->d_status};
       void* args[] = {&ga};
       e = cudaLaunchCooperativeKernel((const void*)gmres_cycle_kernel, dim3(gc_grid), dim3(GC_THREADS), args, gc_smem,
                                       strm);
@@ -936,8 +958,7 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
       xupdate_kernel<<<gb, GM_THREADS, 0, strm>>>(V, n, yv, dinv, x, st);
       launched(2);
     }
-    residual();
-    total_it += 1;   // completed below from kdone
+    residual(nullptr);
   }
   if (iters_out) *iters_out = total_it;
   if (rel_residual) *rel_residual = rel;
