@@ -603,17 +603,21 @@ def run_bem2048(args):
     IDX = torch.from_numpy(bd.idx.astype(np.int32)).to(dev)
     PX, PY, PS = [torch.from_numpy(a).to(dev) for a in (px, py, ps)]
     nunk, m = 2, 2 * npan
-    PU, PV = torch.zeros(npan, device=dev), torch.zeros(npan, device=dev)
+    # velocities of each (u, v) pair in one array, zeroed by one fill per step
+    PUV = torch.zeros(2, npan, device=dev)
+    PU, PV = PUV[0], PUV[1]
     RHS = torch.zeros(m, dtype=torch.float64, device=dev)
     A = torch.zeros(m * m, dtype=torch.float64, device=dev)
     SOL = torch.zeros(m, dtype=torch.float64, device=dev)
-    TU, TV = torch.zeros(npart, device=dev), torch.zeros(npart, device=dev)
+    TUV = torch.zeros(2, npart, device=dev)
+    TU, TV = TUV[0], TUV[1]
+    # the solution's (vortex, source) strength pairs as two FP32 rows, one conversion per step
+    STR = torch.zeros(2, npan, device=dev)
     acc = og.COMPENSATED
     box = {}
 
     def d3():
-        PU.zero_()
-        PV.zero_()
+        PUV.zero_()
         og.points_affect_panels_dev(ctx, acc, PX, PY, PS, NX, NY, IDX, PU, PV, finalize=True)
 
     def b2():
@@ -630,11 +634,9 @@ def run_bem2048(args):
         box["rel_lu"] = og.solve_dense_f64_dev(ctx, A, RHS, SOL)
 
     def d2():
-        TU.zero_()
-        TV.zero_()
-        vs = SOL[0::2].float()
-        ss = SOL[1::2].float()
-        og.panels_affect_points_dev(ctx, acc, NX, NY, IDX, vs, ss, PX, PY, TU, TV)
+        TUV.zero_()
+        STR.copy_(SOL.view(npan, 2).t())
+        og.panels_affect_points_dev(ctx, acc, NX, NY, IDX, STR[0], STR[1], PX, PY, TU, TV)
 
     def pipeline():
         d3(); b2(); b1(); solve(); d2()
@@ -665,8 +667,7 @@ def run_bem2048(args):
         og.vels_to_rhs_panels_dev(ctx, 1, NX, NY, IDX, PU, PV, None, None, RHS1)
         og.panels_on_panels_coeff_dev(ctx, 1, NX, NY, IDX, None, A1)
         solve1()
-        TU.zero_()
-        TV.zero_()
+        TUV.zero_()
         og.panels_affect_points_dev(ctx, acc, NX, NY, IDX, SOL1.float(), None, PX, PY, TU, TV)
     out = {"workload": "bem2048", "metric": "ms per BEM coupling step (2048 panels, 200k particles)",
            "unit": "ms", "higher_is_better": False, "data": "synthetic (seed 3)", "unknowns": m}

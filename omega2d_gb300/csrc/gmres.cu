@@ -59,16 +59,12 @@ __global__ void __launch_bounds__(GM_THREADS) gemv_part_kernel(const double* __r
   part[(size_t)c * n + i] = s;
 }
 
-// y = sum_c part[c]  (or y = b - sum when b is given; y = b when nz is given and *nz == 0)
+// y = sum_c part[c]  (or y = b - sum when b is given)
 __global__ void gemv_sum_kernel(const double* __restrict__ part, int nchunk, int n, const double* __restrict__ b,
-                                double* __restrict__ y, const GmState* st, const unsigned* nz = nullptr) {
+                                double* __restrict__ y, const GmState* st) {
   if (st && st->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (nz && *nz == 0) {
-    y[i] = b[i];
-    return;
-  }
   double s = 0.0;
   for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * n + i];
   y[i] = b ? b[i] - s : s;
@@ -118,28 +114,15 @@ __global__ void hadd_kernel(double* __restrict__ h, const double* __restrict__ h
   for (int k = threadIdx.x; k < cnt; k += blockDim.x) h[k] += h2[k];
 }
 
-// ||w|| into *out (one block); *alt instead when nz is given and *nz == 0 (w a copy of the
-// vector whose norm *alt holds)
+// ||w|| into *out (one block)
 __global__ void __launch_bounds__(1024) norm_kernel(const double* __restrict__ w, int n, double* out,
-                                                     const GmState* st, const unsigned* nz = nullptr,
-                                                     const double* alt = nullptr) {
+                                                     const GmState* st) {
   if (st && st->done) return;
-  if (nz && *nz == 0) {
-    if (threadIdx.x == 0) *out = *alt;
-    return;
-  }
   __shared__ double sh[32];
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(w[i], w[i], s);
   s = block_sum(s, sh);
   if (threadIdx.x == 0) *out = sqrt(s);
-}
-
-// *flag = 1 when any x[i] != 0
-__global__ void nonzero_kernel(const double* __restrict__ x, int n, int* flag) {
-  int nz = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) nz |= (x[i] != 0.0);
-  if (__syncthreads_or(nz) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
 // v = w / *nrm
@@ -150,19 +133,26 @@ __global__ void scale_kernel(const double* __restrict__ w, int n, const double* 
   if (i < n) v[i] = w[i] / *nrm;
 }
 
-// start of a cycle: beta = ||r||, g = (beta, 0, ...), V_0 = r / beta; done when beta is at most
+// start of a cycle, on thread 0: beta = ||r||, g = (beta, 0, ...); done when beta is at most
 // tolabs = tol ||b|| (tol alone when b = 0, src/BEM.h:227-229); the cycle's target is
 // max(tolabs, eta beta), eta applying only when the plane's flag says that A's entries were
-// rounded to FP32 (bit 1)
-__global__ void cycle_start_kernel(GmState* st, const double* nrm, const double* bnrm, double tol, double* g, int m,
-                                   double eta, const unsigned* plane_flag) {
-  st->tolabs = tol * ((*bnrm == 0.0) ? 1.0 : *bnrm);
-  st->beta = *nrm;
-  st->kdone = 0;
-  st->done = (*nrm <= st->tolabs) ? 1 : 0;
-  st->tolcyc = fmax(st->tolabs, ((*plane_flag & 2u) ? eta : 0.0) * *nrm);
-  for (int k = 0; k <= m; ++k) g[k] = 0.0;
-  g[0] = *nrm;
+// rounded to FP32 (bit 1); the grid barrier's arrival counter cleared for the cycle launch
+// that follows.  Over the grid: V_0 = r / beta.
+__global__ void cycle_start_scale_kernel(GmState* st, const double* nrm, const double* bnrm, double tol, double* g,
+                                         int m, double eta, const unsigned* plane_flag, const double* __restrict__ w,
+                                         int n, double* __restrict__ v, unsigned* bar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    st->tolabs = tol * ((*bnrm == 0.0) ? 1.0 : *bnrm);
+    st->beta = *nrm;
+    st->kdone = 0;
+    st->done = (*nrm <= st->tolabs) ? 1 : 0;
+    st->tolcyc = fmax(st->tolabs, ((*plane_flag & 2u) ? eta : 0.0) * *nrm);
+    for (int k = 0; k <= m; ++k) g[k] = 0.0;
+    g[0] = *nrm;
+    *bar = 0u;
+  }
+  if (i < n) v[i] = w[i] / *nrm;
 }
 
 // Givens: rotate column j of H (ldh = m+1) by the previous rotations, make a new one, update g
@@ -207,11 +197,76 @@ __global__ void xupdate_kernel(const double* __restrict__ V, int n, const double
   x[i] += dinv ? s * dinv[i] : s;
 }
 
-__global__ void diag_inv_kernel(const double* __restrict__ A, int n, double* __restrict__ dinv) {
+// The last block of a grid to arrive (a counter that it resets) sums the blocks' partials in
+// block order: the sum does not depend on timing.  Returns the total in thread 0 of that block.
+__device__ bool last_block_sum(double v, double* bpart, unsigned* cnt, double* sh, double* total) {
+  __shared__ bool last;
+  v = block_sum(v, sh);
+  if (threadIdx.x == 0) {
+    bpart[blockIdx.x] = v;
+    __threadfence();
+    last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += 32) t += __ldcg(bpart + k);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) {
+      *total = t;
+      *cnt = 0u;
+    }
+  }
+  return true;
+}
+
+// Start of a solve: Dinv = 1 / diag(A) (1 where the diagonal is 0), *nz = 1 when any x[i] != 0,
+// *bnrm = ||b||
+__global__ void __launch_bounds__(GM_THREADS) prep_kernel(const double* __restrict__ A, const double* __restrict__ b,
+                                                          const double* __restrict__ x, int n, double* __restrict__ dinv,
+                                                          double* bpart, unsigned* cnt, double* bnrm, unsigned* nz) {
+  __shared__ double sh[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double d = A[(size_t)i * n + i];
-  dinv[i] = (d != 0.0) ? 1.0 / d : 1.0;
+  double bb = 0.0;
+  int z = 0;
+  if (i < n) {
+    const double d = A[(size_t)i * n + i];
+    dinv[i] = (d != 0.0) ? 1.0 / d : 1.0;
+    bb = b[i] * b[i];
+    z = x[i] != 0.0;
+  }
+  if (__syncthreads_or(z) && threadIdx.x == 0) atomicOr(nz, 1u);
+  double t;
+  if (last_block_sum(bb, bpart, cnt, sh, &t) && threadIdx.x == 0) *bnrm = sqrt(t);
+}
+
+// y = b - sum_c part[c] (y = b when nz is given and *nz == 0) and *out = ||y|| (*alt then)
+__global__ void __launch_bounds__(GM_THREADS) gemv_sum_norm_kernel(const double* __restrict__ part, int nchunk, int n,
+                                                                   const double* __restrict__ b, double* __restrict__ y,
+                                                                   const unsigned* nz, double* bpart, unsigned* cnt,
+                                                                   double* out, const double* alt) {
+  __shared__ double sh[32];
+  const bool zero = nz && *nz == 0;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r = 0.0;
+  if (i < n) {
+    if (zero) {
+      r = b[i];
+    } else {
+      double s = 0.0;
+      for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * n + i];
+      r = b[i] - s;
+    }
+    y[i] = r;
+  }
+  if (zero) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = *alt;
+    return;
+  }
+  double t;
+  if (last_block_sum(r * r, bpart, cnt, sh, &t) && threadIdx.x == 0) *out = sqrt(t);
 }
 
 // ---------------------------------------------------------------- one restart cycle in one launch
@@ -834,7 +889,8 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
     }
   }
   const size_t NP2 = (N + 1) / 2;                  // column pairs
-  const size_t o_gp = o_n + 256;
+  const size_t o_bp = o_n + 256;                   // block partials of the fused norms
+  const size_t o_gp = o_bp + al((size_t)((n + GM_THREADS - 1) / GM_THREADS) * 8);
   const size_t o_gv = o_gp + al((size_t)2 * gc_grid * (m + 2) * 8);
   const size_t o_gl = o_gv + al(NP2 * 16);
   const size_t o_gb = o_gl + al(NP2 * 8);
@@ -857,7 +913,9 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   float2* gpart = ctx->work.as<float2>(o_gp);
   float4* gvp = ctx->work.as<float4>(o_gv);
   float2* gvl = ctx->work.as<float2>(o_gl);
-  unsigned* gbar = ctx->work.as<unsigned>(o_gb);   // [0] barrier arrivals, [1] plane range flag, [2] x != 0
+  double* bpart = ctx->work.as<double>(o_bp);
+  // [0] barrier arrivals, [1] plane range flag, [2] x != 0, [3] arrivals of the fused norms
+  unsigned* gbar = ctx->work.as<unsigned>(o_gb);
   float2* AH = fused ? ctx->work.as<float2>(o_ap) : nullptr;
   cudaStream_t strm = ctx->stream;
   const int gb = (n + GM_THREADS - 1) / GM_THREADS;
@@ -865,11 +923,8 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   auto launched = [&](int k) { ctx->launches += k; };
 
   // nrm[0]: the current residual norm; nrm[1]: ||b||
-  diag_inv_kernel<<<gb, GM_THREADS, 0, strm>>>(A, n, dinv);
-  norm_kernel<<<1, 1024, 0, strm>>>(b, n, nrm + 1, nullptr);
-  launched(2);
-  if ((e = cudaMemsetAsync(gbar, 0, 3 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
-  nonzero_kernel<<<std::min(gb, 4 * ctx->num_sms), GM_THREADS, 0, strm>>>(x, n, reinterpret_cast<int*>(gbar + 2));
+  if ((e = cudaMemsetAsync(gbar, 0, 4 * sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
+  prep_kernel<<<gb, GM_THREADS, 0, strm>>>(A, b, x, n, dinv, bpart, gbar + 3, nrm + 1, gbar + 2);
   launched(1);
   if (fused) {
     {
@@ -884,9 +939,8 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
   // (known on the device only) gives r = b and ||b|| without the product
   auto residual = [&](const unsigned* nz) {
     gemv_part_kernel<<<ggrid, GM_THREADS, 0, strm>>>(A, n, x, nullptr, part, nullptr, nz);
-    gemv_sum_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, b, w, nullptr, nz);
-    norm_kernel<<<1, 1024, 0, strm>>>(w, n, nrm, nullptr, nz, nrm + 1);
-    launched(3);
+    gemv_sum_norm_kernel<<<gb, GM_THREADS, 0, strm>>>(part, nchunk, n, b, w, nz, bpart, gbar + 3, nrm, nrm + 1);
+    launched(2);
   };
   residual(gbar + 2);
   // The first cycle is launched without a host round trip: its start kernel forms the tolerance
@@ -925,12 +979,11 @@ int gmres_f64(obs_context* ctx, int n, const double* A, const double* b, double*
       }
       if (!(rn > tol * bref) || total_it >= maxiter || stalled) break;   // converged (or NaN) / budget
     }
-    cycle_start_kernel<<<1, 1, 0, strm>>>(st, nrm, nrm + 1, tol, g, m, fused ? kRefineEta : 0.0, gbar + 1);
-    scale_kernel<<<gb, GM_THREADS, 0, strm>>>(w, n, nrm, V, nullptr);
-    launched(2);
+    cycle_start_scale_kernel<<<gb, GM_THREADS, 0, strm>>>(st, nrm, nrm + 1, tol, g, m, fused ? kRefineEta : 0.0,
+                                                          gbar + 1, w, n, V, gbar);
+    launched(1);
     const int mc = std::min(m, maxiter - total_it);
     if (fused) {
-      if ((e = cudaMemsetAsync(gbar, 0, sizeof(unsigned), strm)) != cudaSuccess) return cuda_status(e);
       GcArgs ga{AH, dinv, n, m, mc, gc_gpb, V, gvp, gvl, x, gpart, gbar, gbar + 1, st, ctx->d_status};
       void* args[] = {&ga};
       e = cudaLaunchCooperativeKernel((const void*)gmres_cycle_kernel, dim3(gc_grid), dim3(GC_THREADS), args, gc_smem,

@@ -181,6 +181,27 @@ __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, do
   a.out_v[i] = (float)(((double)a.out_v[i] + sv) * f + fy);
 }
 
+// The per-target steps after the sum over sources, then the store: (ux, uy) is the target
+// panel's unit tangent and tinv its inverse length (modes 1 and 2)
+__device__ __forceinline__ void pan_finish(const PanArgs& a, int i, double su, double sv, float tux, float tuy,
+                                           float tinv) {
+  if (a.mode == 1) {
+    // (sum w u*, sum w v*) -> velocity along the fixed tangent, times -1/len
+    const double ux = tux, uy = tuy;
+    const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
+    su = -vu * (double)tinv;
+    sv = -vv * (double)tinv;
+  } else if (a.mode == 2) {
+    // A = g tx + s ty, B = s tx - g ty: dL/dg = tx P + ty Q, dL/ds = ty P - tx Q, times the
+    // finalize factor 1/(2 pi) (the gradients are of the finalized velocities)
+    const double ux = tux, uy = tuy;
+    const double gg = (ux * su + uy * sv) * 0.15915494309189535, gs = (uy * su - ux * sv) * 0.15915494309189535;
+    su = gg;
+    sv = gs;
+  }
+  pan_store(a, i, su, sv);
+}
+
 // Two targets per thread (h = 0, 1: targets blockIdx.x PAN_TPB + h PAN_THREADS + tid) in
 // f32x2 register pairs; sources (panels or particles) staged through shared memory; grid =
 // (target blocks, source splits).  Compensated: FP32 partials over 32 sources folded into
@@ -291,93 +312,84 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
   for (int h = 0; h < 2; ++h) {
     const int i = ti[h];
     if (i >= a.nt) continue;
-    double su = COMP ? (double)(h ? hu.y : hu.x) + (double)(h ? lu.y : lu.x) : (double)(h ? au.y : au.x);
-    double sv = COMP ? (double)(h ? hv.y : hv.x) + (double)(h ? lv.y : lv.x) : (double)(h ? av.y : av.x);
-    if (a.mode == 1) {
-      // (sum w u*, sum w v*) -> velocity along the fixed tangent, times -1/len
-      const double ux = TQ[h].x, uy = TQ[h].y;
-      const double vu = su * ux - sv * uy, vv = su * uy + sv * ux;
-      su = -vu * (double)tinv[h];
-      sv = -vv * (double)tinv[h];
-    } else if (a.mode == 2) {
-      // A = g tx + s ty, B = s tx - g ty: dL/dg = tx P + ty Q, dL/ds = ty P - tx Q, times the
-      // finalize factor 1/(2 pi) (the gradients are of the finalized velocities)
-      const double ux = TQ[h].x, uy = TQ[h].y;
-      const double gg = (ux * su + uy * sv) * 0.15915494309189535, gs = (uy * su - ux * sv) * 0.15915494309189535;
-      su = gg;
-      sv = gs;
+    if (a.nsplit > 1) {
+      // this split's raw sums (double-float when compensated); the reduction applies the
+      // per-target steps below once to their total
+      if (COMP) {
+        float2* p = static_cast<float2*>(a.part);
+        p[(size_t)sp * a.nt + i] = make_float2(h ? hu.y : hu.x, h ? lu.y : lu.x);
+        p[((size_t)a.nsplit + sp) * a.nt + i] = make_float2(h ? hv.y : hv.x, h ? lv.y : lv.x);
+      } else {
+        float* p = static_cast<float*>(a.part);
+        p[(size_t)sp * a.nt + i] = h ? au.y : au.x;
+        p[((size_t)a.nsplit + sp) * a.nt + i] = h ? av.y : av.x;
+      }
+      continue;
     }
-    if (a.nsplit == 1) {
-      pan_store(a, i, su, sv);
-    } else if (COMP) {
-      double* p = static_cast<double*>(a.part);
-      p[(size_t)sp * a.nt + i] = su;
-      p[((size_t)a.nsplit + sp) * a.nt + i] = sv;
+    const double su = COMP ? (double)(h ? hu.y : hu.x) + (double)(h ? lu.y : lu.x) : (double)(h ? au.y : au.x);
+    const double sv = COMP ? (double)(h ? hv.y : hv.x) + (double)(h ? lv.y : lv.x) : (double)(h ? av.y : av.x);
+    pan_finish(a, i, su, sv, TQ[h].x, TQ[h].y, tinv[h]);
+  }
+}
+
+// Sum of the split partials: a block takes 32 consecutive targets (lane = target, so every
+// load of a warp is 256 contiguous bytes) and its warps take every PAN_RED_WARPS-th split,
+// double-float sums when compensated; the warps' sums are added in warp order (the result does
+// not depend on timing), then the per-target steps in FP64 and the store
+constexpr int PAN_RED_WARPS = 8;
+// (hi, lo) += (bh, bl) in double-float
+__device__ __forceinline__ void pan_df_add(float& hi, float& lo, float bh, float bl) {
+  two_sum_acc(hi, lo, bh);
+  lo += bl;
+}
+template <bool COMP>
+__global__ void __launch_bounds__(32 * PAN_RED_WARPS) pan_reduce_kernel(const PanArgs a) {
+  __shared__ float4 red[PAN_RED_WARPS][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  const int ic = i < a.nt ? i : a.nt - 1;
+  float hu = 0.0f, lu = 0.0f, hv = 0.0f, lv = 0.0f;
+  if (COMP) {
+    const float2* p = static_cast<const float2*>(a.part);
+#pragma unroll 4
+    for (int k = wp; k < a.nsplit; k += PAN_RED_WARPS) {
+      const float2 u = p[(size_t)k * a.nt + ic], v = p[((size_t)a.nsplit + k) * a.nt + ic];
+      pan_df_add(hu, lu, u.x, u.y);
+      pan_df_add(hv, lv, v.x, v.y);
+    }
+  } else {
+    const float* p = static_cast<const float*>(a.part);
+#pragma unroll 4
+    for (int k = wp; k < a.nsplit; k += PAN_RED_WARPS) {
+      hu += p[(size_t)k * a.nt + ic];
+      hv += p[((size_t)a.nsplit + k) * a.nt + ic];
+    }
+  }
+  red[wp][lane] = make_float4(hu, lu, hv, lv);
+  __syncthreads();
+  if (wp != 0 || i >= a.nt) return;
+  float4 t = red[0][lane];
+  for (int w = 1; w < PAN_RED_WARPS; ++w) {
+    const float4 q = red[w][lane];
+    if (COMP) {
+      pan_df_add(t.x, t.y, q.x, q.y);
+      pan_df_add(t.z, t.w, q.z, q.w);
     } else {
-      float* p = static_cast<float*>(a.part);
-      p[(size_t)sp * a.nt + i] = (float)su;
-      p[((size_t)a.nsplit + sp) * a.nt + i] = (float)sv;
+      t.x += q.x;
+      t.z += q.z;
     }
   }
+  const double su = (double)t.x + (double)t.y, sv = (double)t.z + (double)t.w;
+  float tux = 0.0f, tuy = 0.0f, tinv = 0.0f;
+  if (a.mode != 0) {
+    const float4 q = a.Q[i];
+    tux = q.x;
+    tuy = q.y;
+    if (a.mode == 1) tinv = 1.0f / a.plen[i];
+  }
+  pan_finish(a, i, su, sv, tux, tuy, tinv);
 }
 
-template <bool COMP>
-__global__ void pan_reduce_kernel(const PanArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.nt) return;
-  double su = 0.0, sv = 0.0;
-  if (COMP) {
-    const double* p = static_cast<const double*>(a.part);
-    for (int k = 0; k < a.nsplit; ++k) {
-      su += p[(size_t)k * a.nt + i];
-      sv += p[((size_t)a.nsplit + k) * a.nt + i];
-    }
-  } else {
-    const float* p = static_cast<const float*>(a.part);
-    float fu = 0.0f, fv = 0.0f;
-    for (int k = 0; k < a.nsplit; ++k) {
-      fu += p[(size_t)k * a.nt + i];
-      fv += p[((size_t)a.nsplit + k) * a.nt + i];
-    }
-    su = fu;
-    sv = fv;
-  }
-  pan_store(a, i, su, sv);
-}
-
-// The same reduction with one warp per target, for many splits: lanes take every 32nd split,
-// then a shuffle tree (FP64 adds are slow on this GPU, so the serial chain is kept short)
-template <bool COMP>
-__global__ void pan_reduce_warp_kernel(const PanArgs a) {
-  const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (i >= a.nt) return;
-  double su = 0.0, sv = 0.0;
-  if (COMP) {
-    const double* p = static_cast<const double*>(a.part);
-    for (int k = lane; k < a.nsplit; k += 32) {
-      su += p[(size_t)k * a.nt + i];
-      sv += p[((size_t)a.nsplit + k) * a.nt + i];
-    }
-  } else {
-    const float* p = static_cast<const float*>(a.part);
-    float fu = 0.0f, fv = 0.0f;
-    for (int k = lane; k < a.nsplit; k += 32) {
-      fu += p[(size_t)k * a.nt + i];
-      fv += p[((size_t)a.nsplit + k) * a.nt + i];
-    }
-    su = fu;
-    sv = fv;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    su += __shfl_xor_sync(0xffffffffu, su, o);
-    sv += __shfl_xor_sync(0xffffffffu, sv, o);
-  }
-  if (lane == 0) pan_store(a, i, su, sv);
-}
-
-// Points with their velocity cotangents -> float4 (x, y, lu, lv), padded with zero cotangents
-// far away.
 __global__ void pack_cotangents_kernel(const float* __restrict__ x, const float* __restrict__ y,
                                        const float* __restrict__ lu, const float* __restrict__ lv, int n, int n_pad,
                                        float4* __restrict__ out) {
@@ -548,15 +560,10 @@ int launch_pan(obs_context* ctx, PanArgs& a, bool comp) {
   ctx->launches++;
   timing_main_end(ctx);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && a.nsplit > 16) {
-    const unsigned blocks = (unsigned)(((size_t)a.nt * 32 + 255) / 256);
-    if (comp) pan_reduce_warp_kernel<true><<<blocks, 256, 0, ctx->stream>>>(a);
-    else pan_reduce_warp_kernel<false><<<blocks, 256, 0, ctx->stream>>>(a);
-    ctx->launches++;
-    e = cudaGetLastError();
-  } else if (e == cudaSuccess && a.nsplit > 1) {
-    if (comp) pan_reduce_kernel<true><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
-    else pan_reduce_kernel<false><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
+  if (e == cudaSuccess && a.nsplit > 1) {
+    const unsigned blocks = (unsigned)((a.nt + 31) / 32);
+    if (comp) pan_reduce_kernel<true><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
+    else pan_reduce_kernel<false><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
     ctx->launches++;
     e = cudaGetLastError();
   }
