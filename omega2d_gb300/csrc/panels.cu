@@ -154,10 +154,19 @@ __device__ __forceinline__ void panel_uv_star_fast2(float2 x0, float2 y0, float2
 }
 
 struct PanArgs {
-  const float4* P;      // packed panels
-  const float4* Q;
-  const float* plen;    // panel lengths (points -> panels)
-  const float4* pts;    // packed particles (x, y, z, strength) for points -> panels
+  const float* gx;      // the panel set: node coordinates, node-index pairs (mode 0: the
+  const float* gy;      //   sources, padded to nsrc with far panels of zero strength; modes 1
+  const unsigned* gidx; //   and 2: the targets)
+  int nnodes;
+  int npan;
+  const float* gvs;     // vortex and source strengths (mode 0; either may be null)
+  const float* gss;
+  int* status;
+  const float4* pts;    // packed cotangent points (x, y, lu, lv) for mode 2
+  const float* sx;      // the particles of mode 1, read directly (nreal of them; the padding
+  const float* sy;      //   up to nsrc is far away with zero strength)
+  const float* ss;
+  int nreal;
   int nsrc;             // panels (pan->pt) or particles (pt->pan), padded count
   int nblk;             // 32-source blocks (nsrc / 32)
   const float* tx;
@@ -173,6 +182,28 @@ struct PanArgs {
   int mode;             // 0: panels -> points, 1: points -> panels, 2: VJP of mode 0 w.r.t. the
                         //    panel strengths (sources = points with their cotangents)
 };
+
+// Panel j of the set as pack_panels_kernel forms it: P = (x0, y0, x1, y1), Q = (unit tangent,
+// strengths), len; an index past npan is a far panel of zero strength, a node index out of
+// range records DEV_ERR_BOUNDS (code 301) and gives the same far panel
+__device__ __forceinline__ void panel_geom(const PanArgs& a, int j, float4& P, float4& Q, float& len) {
+  P = make_float4(1.0e6f, 1.0e6f, 1.0e6f + 1.0f, 1.0e6f);
+  Q = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  len = 1.0f;
+  if (j >= a.npan) return;
+  const unsigned j0 = a.gidx[2 * j], j1 = a.gidx[2 * j + 1];
+  if (j0 >= (unsigned)a.nnodes || j1 >= (unsigned)a.nnodes) {
+    record_failure(a.status, DEV_ERR_BOUNDS, 301, j, (int)max(j0, j1));
+    return;
+  }
+  const float x0 = a.gx[j0], y0 = a.gy[j0], x1 = a.gx[j1], y1 = a.gy[j1];
+  const float px = x1 - x0, py = y1 - y0;
+  const float panl = px * px + py * py;
+  const float m = 1.0f / sqrtf(panl);
+  P = make_float4(x0, y0, x1, y1);
+  Q = make_float4(px * m, py * m, a.gvs ? a.gvs[j] : 0.0f, a.gss ? a.gss[j] : 0.0f);
+  len = sqrtf(panl);
+}
 
 __device__ __forceinline__ void pan_store(const PanArgs& a, int i, double su, double sv) {
   const double f = a.finalize ? 0.15915494309189535 : 1.0;
@@ -229,9 +260,9 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
       tx[h] = a.tx[ic];
       ty[h] = a.ty[ic];
     } else {
-      TP[h] = a.P[ic];
-      TQ[h] = a.Q[ic];
-      tinv[h] = 1.0f / a.plen[ic];
+      float len;
+      panel_geom(a, ic, TP[h], TQ[h], len);
+      tinv[h] = 1.0f / len;
     }
   }
   const float2 T2x = f2(tx[0], tx[1]), T2y = f2(ty[0], ty[1]);
@@ -249,7 +280,9 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
     for (int k = threadIdx.x; k < ns; k += PAN_THREADS) {
       const int j = base * PAN_COMP_BLOCK + k;
       if (a.mode == 0) {
-        const float4 P = a.P[j], Q = a.Q[j];
+        float4 P, Q;
+        float len;
+        panel_geom(a, j, P, Q, len);
         const float px = P.z - P.x, py = P.w - P.y;
         const float A = Q.z * Q.x + Q.w * Q.y, B = Q.w * Q.x - Q.z * Q.y;
         sE[k][0] = make_float4(P.x, P.x, P.y, P.y);
@@ -257,7 +290,10 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
         sE[k][2] = make_float4(px, px, py, py);
         sE[k][3] = make_float4(A, A, B, B);
       } else {
-        const float4 q = a.pts[j];   // (x, y, 0, strength) or, mode 2, (x, y, lu, lv)
+        // (x, y, 0, strength) or, mode 2, (x, y, lu, lv)
+        const float4 q = (a.mode == 2) ? a.pts[j]
+                         : (j < a.nreal) ? make_float4(a.sx[j], a.sy[j], 0.0f, a.ss[j])
+                                         : make_float4(1.0e6f, 1.0e6f, 0.0f, 0.0f);
         sE[k][0] = make_float4(q.x, q.x, q.y, q.y);
         sE[k][1] = (a.mode == 1) ? make_float4(q.w, q.w, 0.0f, 0.0f) : make_float4(q.z, q.z, q.w, q.w);
       }
@@ -382,10 +418,12 @@ __global__ void __launch_bounds__(32 * PAN_RED_WARPS) pan_reduce_kernel(const Pa
   const double su = (double)t.x + (double)t.y, sv = (double)t.z + (double)t.w;
   float tux = 0.0f, tuy = 0.0f, tinv = 0.0f;
   if (a.mode != 0) {
-    const float4 q = a.Q[i];
-    tux = q.x;
-    tuy = q.y;
-    if (a.mode == 1) tinv = 1.0f / a.plen[i];
+    float4 P, Q;
+    float len;
+    panel_geom(a, i, P, Q, len);
+    tux = Q.x;
+    tuy = Q.y;
+    if (a.mode == 1) tinv = 1.0f / len;
   }
   pan_finish(a, i, su, sv, tux, tuy, tinv);
 }
@@ -399,13 +437,6 @@ __global__ void pack_cotangents_kernel(const float* __restrict__ x, const float*
 }
 
 // Particles -> float4 (x, y, 0, strength), padded with zero-strength particles far away.
-__global__ void pack_points_kernel(const float* __restrict__ x, const float* __restrict__ y,
-                                   const float* __restrict__ s, int n, int n_pad, float4* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
-  out[i] = i < n ? make_float4(x[i], y[i], 0.0f, s[i]) : make_float4(1.0e6f, 1.0e6f, 0.0f, 0.0f);
-}
-
 // float -> double from the bits (exact): float->double conversions run on the slow FP64 path of
 // this GPU; zero and normal values are rebiased with integer operations, anything else (a
 // subnormal, infinity or NaN) takes the hardware conversion
@@ -490,21 +521,34 @@ __global__ void coeff_kernel(const float4* __restrict__ SP, const float4* __rest
   }
 }
 
-// vels_to_rhs_panels (src/RHS.h:54-115): rhs = -u.t (and -u.n + bc_n for two unknowns)
-template <class T>
-__global__ void rhs_kernel(const float4* __restrict__ Q, const float* __restrict__ pu,
+// vels_to_rhs_panels (src/RHS.h:54-115): rhs = -u.t (and -u.n + bc_n for two unknowns), into
+// rhs32 and / or rhs64; the unit tangent formed from the panel's nodes as pack_panels_kernel
+// forms it
+__global__ void rhs_kernel(const float* __restrict__ nx, const float* __restrict__ ny,
+                           const unsigned* __restrict__ idx, int nnodes, const float* __restrict__ pu,
                            const float* __restrict__ pv, const float* __restrict__ bcn, int np, int nunk,
-                           T* __restrict__ rhs) {
+                           float* __restrict__ rhs32, double* __restrict__ rhs64, int* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
-  const float4 q = Q[i];
-  const float t = -(pu[i] * q.x + pv[i] * q.y);
-  if (nunk == 1) {
-    rhs[i] = (T)t;
+  const unsigned j0 = idx[2 * i], j1 = idx[2 * i + 1];
+  float qx = 1.0f, qy = 0.0f;
+  if (j0 >= (unsigned)nnodes || j1 >= (unsigned)nnodes) {
+    record_failure(status, DEV_ERR_BOUNDS, 301, i, (int)max(j0, j1));
   } else {
-    const float n = -(pu[i] * (-q.y) + pv[i] * q.x) + (bcn ? bcn[i] : 0.0f);
-    rhs[2 * i] = (T)t;
-    rhs[2 * i + 1] = (T)n;
+    const float px = nx[j1] - nx[j0], py = ny[j1] - ny[j0];
+    const float panl = px * px + py * py;
+    const float m = 1.0f / sqrtf(panl);
+    qx = px * m;
+    qy = py * m;
+  }
+  const float t = -(pu[i] * qx + pv[i] * qy);
+  if (nunk == 1) {
+    if (rhs32) rhs32[i] = t;
+    if (rhs64) rhs64[i] = (double)t;
+  } else {
+    const float n = -(pu[i] * (-qy) + pv[i] * qx) + (bcn ? bcn[i] : 0.0f);
+    if (rhs32) { rhs32[2 * i] = t; rhs32[2 * i + 1] = n; }
+    if (rhs64) { rhs64[2 * i] = (double)t; rhs64[2 * i + 1] = (double)n; }
   }
 }
 
@@ -530,6 +574,12 @@ int plan_splits(obs_context* ctx, int nblk, int tblocks) {
   const int want = 8 * 4 * ctx->num_sms;
   const int nsplit = std::max(1, (want + tblocks - 1) / tblocks);
   return std::min(nsplit, std::max(1, nblk));
+}
+
+void set_panels(PanArgs& a, const PanelSet& ps, const float* vs, const float* ss, obs_context* ctx) {
+  a.gx = ps.nx; a.gy = ps.ny; a.gidx = ps.idx; a.nnodes = ps.nnodes; a.npan = ps.npan;
+  a.gvs = vs; a.gss = ss;
+  a.status = ctx->d_status;
 }
 
 int run_pan(obs_context* ctx, PanArgs& a, bool comp, size_t scratch_off) {
@@ -578,8 +628,7 @@ int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* 
   const bool comp = accum == OBS_COMPENSATED;
   const int ntiles = (ps.npan + PAN_TILE - 1) / PAN_TILE;
   const int np_pad = ntiles * PAN_TILE;
-  const size_t hdr = 256, pbytes = (size_t)np_pad * sizeof(float4);
-  const size_t off_part = hdr + 2 * pbytes;
+  const size_t off_part = 256;
   PanArgs a;
   std::memset(&a, 0, sizeof(a));
   a.nsrc = np_pad; a.nblk = np_pad / PAN_COMP_BLOCK;
@@ -588,16 +637,13 @@ int run_panels_affect_points(obs_context* ctx, const PanelSet& ps, const float* 
   a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
   a.fsx = fsx; a.fsy = fsy;
   a.mode = 0;
+  set_panels(a, ps, vs, ss, ctx);
   int s = ctx->work.ensure(off_part, ctx->stream);
   if (!s) s = run_pan(ctx, a, comp, off_part);
   if (s) return s;
-  float4* P = ctx->work.as<float4>(hdr);
-  float4* Q = ctx->work.as<float4>(hdr + pbytes);
-  a.P = P; a.Q = Q;
   if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
   timing_begin(ctx);
-  s = pack_panels(ctx, ps, vs, ss, P, Q, nullptr, np_pad);
-  if (!s) s = launch_pan(ctx, a, comp);
+  s = launch_pan(ctx, a, comp);
   timing_end(ctx);
   return s;
 }
@@ -610,37 +656,23 @@ int run_points_affect_panels(obs_context* ctx, int ns, const float* sx, const fl
   const bool comp = accum == OBS_COMPENSATED;
   const int ntiles = (ns + PAN_TILE - 1) / PAN_TILE;
   const int ns_pad = ntiles * PAN_TILE;
-  const int np = ps.npan;
-  const size_t hdr = 256;
-  const size_t pbytes = ((size_t)np * sizeof(float4) + 255) & ~(size_t)255;
-  const size_t lbytes = ((size_t)np * sizeof(float) + 255) & ~(size_t)255;
-  const size_t off_pts = hdr + 2 * pbytes + lbytes;
-  const size_t off_part = off_pts + (size_t)ns_pad * sizeof(float4);
+  const size_t off_part = 256;
   PanArgs a;
   std::memset(&a, 0, sizeof(a));
   a.nsrc = ns_pad; a.nblk = ns_pad / PAN_COMP_BLOCK;
-  a.nt = np;
+  a.nt = ps.npan;
   a.out_u = pu; a.out_v = pv;
   a.finalize = (flags & OBS_FLAG_FINALIZE) ? 1 : 0;
   a.fsx = fsx; a.fsy = fsy;
   a.mode = 1;
+  set_panels(a, ps, nullptr, nullptr, ctx);
+  a.sx = sx; a.sy = sy; a.ss = ss; a.nreal = ns;
   int s = ctx->work.ensure(off_part, ctx->stream);
   if (!s) s = run_pan(ctx, a, comp, off_part);
   if (s) return s;
-  float4* P = ctx->work.as<float4>(hdr);
-  float4* Q = ctx->work.as<float4>(hdr + pbytes);
-  float* L = ctx->work.as<float>(hdr + 2 * pbytes);
-  float4* pts = ctx->work.as<float4>(off_pts);
-  a.P = P; a.Q = Q; a.plen = L; a.pts = pts;
   if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
   timing_begin(ctx);
-  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, L, np);
-  if (!s) {
-    pack_points_kernel<<<(ns_pad + 255) / 256, 256, 0, ctx->stream>>>(sx, sy, ss, ns, ns_pad, pts);
-    ctx->launches++;
-    s = cuda_status(cudaGetLastError());
-  }
-  if (!s) s = launch_pan(ctx, a, comp);
+  s = launch_pan(ctx, a, comp);
   timing_end(ctx);
   return s;
 }
@@ -656,9 +688,8 @@ int run_panels_affect_points_vjp(obs_context* ctx, const PanelSet& ps, int nt, c
   const int nt_pad = ntiles * PAN_TILE;
   const int np = ps.npan;
   const size_t hdr = 256;
-  const size_t pbytes = ((size_t)np * sizeof(float4) + 255) & ~(size_t)255;
   const size_t lbytes = ((size_t)np * sizeof(float) + 255) & ~(size_t)255;
-  const size_t off_pts = hdr + 2 * pbytes + 2 * lbytes;
+  const size_t off_pts = hdr + lbytes;
   const size_t off_part = off_pts + (size_t)nt_pad * sizeof(float4);
   PanArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -666,21 +697,19 @@ int run_panels_affect_points_vjp(obs_context* ctx, const PanelSet& ps, int nt, c
   a.nt = np;
   a.finalize = 0;
   a.mode = 2;
+  set_panels(a, ps, nullptr, nullptr, ctx);
   int s = ctx->work.ensure(off_part, ctx->stream);
   if (!s) s = run_pan(ctx, a, comp, off_part);
   if (s) return s;
-  float4* P = ctx->work.as<float4>(hdr);
-  float4* Q = ctx->work.as<float4>(hdr + pbytes);
-  float* L = ctx->work.as<float>(hdr + 2 * pbytes);
-  float* sink = ctx->work.as<float>(hdr + 2 * pbytes + lbytes);   // dL/dsigma when not wanted
+  float* sink = ctx->work.as<float>(hdr);   // dL/dsigma when not wanted
   float4* pts = ctx->work.as<float4>(off_pts);
-  a.P = P; a.Q = Q; a.plen = L; a.pts = pts;
+  a.pts = pts;
   a.out_u = gvs;
   a.out_v = gss ? gss : sink;
   if (a.nsplit > 1) a.part = ctx->work.as<char>(off_part);
   timing_begin(ctx);
-  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, L, np);
-  if (!s && !gss) s = cuda_status(cudaMemsetAsync(sink, 0, (size_t)np * sizeof(float), ctx->stream));
+  s = OBS_OK;
+  if (!gss) s = cuda_status(cudaMemsetAsync(sink, 0, (size_t)np * sizeof(float), ctx->stream));
   if (!s) {
     pack_cotangents_kernel<<<(nt_pad + 255) / 256, 256, 0, ctx->stream>>>(tx, ty, lu, lv, nt, nt_pad, pts);
     ctx->launches++;
@@ -709,9 +738,17 @@ int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const Pane
   float4* TP = ctx->work.as<float4>(off); off += tp;
   float4* TQ = ctx->work.as<float4>(off); off += tp;
   float* TL = ctx->work.as<float>(off);
+  // a self block packs its one panel set once
+  const bool same = src.nx == targ.nx && src.ny == targ.ny && src.idx == targ.idx && src.npan == targ.npan &&
+                    src.nnodes == targ.nnodes;
+  if (same) {
+    TP = SP;
+    TQ = SQ;
+    TL = SL;
+  }
   timing_begin(ctx);
   s = pack_panels(ctx, src, nullptr, nullptr, SP, SQ, SL, src.npan);
-  if (!s) s = pack_panels(ctx, targ, nullptr, nullptr, TP, TQ, TL, targ.npan);
+  if (!s && !same) s = pack_panels(ctx, targ, nullptr, nullptr, TP, TQ, TL, targ.npan);
   if (s) return s;
   dim3 grid((targ.npan + 127) / 128, src.npan);
   timing_main_begin(ctx);
@@ -724,18 +761,11 @@ int run_panels_on_panels_coeff(obs_context* ctx, const PanelSet& src, const Pane
 
 int run_vels_to_rhs(obs_context* ctx, const PanelSet& ps, int nunk, const float* pu, const float* pv,
                     const float* bcn, float* rhs32, double* rhs64) {
-  if (ps.npan == 0) return OBS_OK;
-  const size_t hdr = 256;
-  const size_t pb = ((size_t)ps.npan * sizeof(float4) + 255) & ~(size_t)255;
-  int s = ctx->work.ensure(hdr + 2 * pb, ctx->stream);
-  if (s) return s;
-  float4* P = ctx->work.as<float4>(hdr);
-  float4* Q = ctx->work.as<float4>(hdr + pb);
-  s = pack_panels(ctx, ps, nullptr, nullptr, P, Q, nullptr, ps.npan);
-  if (s) return s;
+  if (ps.npan == 0 || (!rhs32 && !rhs64)) return OBS_OK;
   const int blocks = (ps.npan + 255) / 256;
-  if (rhs32) { rhs_kernel<float><<<blocks, 256, 0, ctx->stream>>>(Q, pu, pv, bcn, ps.npan, nunk, rhs32); ctx->launches++; }
-  if (rhs64) { rhs_kernel<double><<<blocks, 256, 0, ctx->stream>>>(Q, pu, pv, bcn, ps.npan, nunk, rhs64); ctx->launches++; }
+  rhs_kernel<<<blocks, 256, 0, ctx->stream>>>(ps.nx, ps.ny, ps.idx, ps.nnodes, pu, pv, bcn, ps.npan, nunk, rhs32, rhs64,
+                                              ctx->d_status);
+  ctx->launches++;
   return cuda_status(cudaGetLastError());
 }
 
