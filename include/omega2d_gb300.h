@@ -417,7 +417,10 @@ int obs_advect_vjp_dev(obs_context* ctx, int core, int accum, int order, int n, 
  *   - At most OBS_NOALLOC_MAX_SOURCES sources; more returns OBS_ERR_SCRATCH_LIMIT.  Targets are
  *     unlimited (fewer source splits are used when the partial sums would not fit).
  *   - The first call on each device looks up the scratch's device address (once per device,
- *     with that device current); make that first call before any stream capture.
+ *     with that device current).
+ *   - Every call ends by synchronizing its stream, so it cannot be recorded into a CUDA graph:
+ *     called while its stream is being captured it does nothing and returns
+ *     OBS_ERR_UNSUPPORTED.
  *   - Every call shares the one scratch array: calls that overlap on the GPU (other streams,
  *     other host threads) race and corrupt each other's results.
  */

@@ -77,12 +77,15 @@ extern "C" int obs_points_affect_points_noalloc(void* cuda_stream, int core, int
   for (int k = 0; k < nextra; ++k)
     if (nt > 0 && !extra[k]) return OBS_ERR_ARG;
   if (ns == 0 || nt == 0) return OBS_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  // the call ends by synchronizing its stream, which a stream capture does not allow
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return OBS_ERR_UNSUPPORTED;
 
   void* base = nullptr;
   int nsm = 0;
   int s = scratch_on_current_device(&base, &nsm);
   if (s) return s;
-  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
   const bool thick = tr != nullptr;
   const bool comp = accum == OBS_COMPENSATED;
   const int res = result;

@@ -135,3 +135,32 @@ def test_noalloc_allocates_no_device_memory():
             assert rel_err(a, b) < TOL[accum]
         if result == og.PSIONLY:
             assert not got[0].cpu().numpy().any() and not got[1].cpu().numpy().any()   # velocity untouched
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """Every call ends by synchronizing its stream, which a stream capture does not allow: on a
+    stream that is being captured the call does nothing and returns OBS_ERR_UNSUPPORTED."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    rng = np.random.default_rng(79)
+    sx, sy, sr, ss = _cloud(rng, 4_000, torch, dev)
+    tx, ty, tr, _ = _cloud(rng, 2_000, torch, dev)
+    tu, tv = torch.zeros(2_000, device=dev), torch.zeros(2_000, device=dev)
+    L = og.lib()
+    P = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        try:
+            st = L.obs_points_affect_points_noalloc(
+                ctypes.c_void_p(s.cuda_stream), ctypes.c_int(og.CORE_GAUSSIAN), ctypes.c_int(og.VELONLY),
+                ctypes.c_int(og.COMPENSATED), ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_double(0.0),
+                ctypes.c_int(sx.numel()), P(sx), P(sy), P(sr), P(ss),
+                ctypes.c_int(tx.numel()), P(tx), P(ty), P(tr), P(tu), P(tv), None, None, None, None)
+        finally:
+            g.capture_end()
+    torch.cuda.synchronize()
+    assert st == -7, og.STATUS.get(st, st)
+    assert not bool(tu.any()) and not bool(tv.any())
