@@ -737,7 +737,42 @@ def run_bem2048(args):
                            "clear_inner_layer_pairs_per_s": sub.size * npan / t_cl,
                            "sample": "FP64 restatement of the full particles-on-panels sum and matrix; "
                                      "clear_inner_layer on 4096 of the particles"}
+    out["bodies4"] = run_bem_bodies(torch, og, dev, ctx, stream, flush, args, npan)
     return out
+
+
+def run_bem_bodies(torch, og, dev, ctx, stream, flush, args, npan):
+    """Four circles of `npan` panels, centres (+-1.5, +-1.5), joined into one system of
+    8 npan unknowns: the joined matrix rebuilt in full (the engine's choice where the reference
+    rebuilds only the blocks of bodies in relative motion, src/BEMHelper.h:147-221) against
+    the FP64 GMRES solve of the same system, right-hand side A x for a seeded x."""
+    bodies = [og.circle_panels(npan, center=c) for c in ((-1.5, -1.5), (1.5, -1.5), (-1.5, 1.5), (1.5, 1.5))]
+    J, _ = og.join_surfaces(bodies)
+    NX, NY = torch.from_numpy(J.nx).to(dev), torch.from_numpy(J.ny).to(dev)
+    IDX = torch.from_numpy(J.idx.astype(np.int32)).to(dev)
+    m = 2 * J.npan
+    A = torch.zeros(m * m, dtype=torch.float64, device=dev)
+    og.panels_on_panels_coeff_dev(ctx, 2, NX, NY, IDX, None, A)
+    ctx.synchronize()
+    xt = torch.from_numpy(np.random.default_rng(41).normal(size=m)).to(dev)
+    rhs = A.view(m, m).t() @ xt            # A is column-major
+    X = torch.zeros(m, dtype=torch.float64, device=dev)
+    box = {}
+
+    def build():
+        og.panels_on_panels_coeff_dev(ctx, 2, NX, NY, IDX, None, A)
+
+    def solve():
+        X.zero_()
+        box["it"], box["rel"] = og.solve_gmres_f64_dev(ctx, A, rhs, X)
+
+    t_build = _event_time(torch, stream, flush, build, args.steps, args.warmup)
+    t_solve = _event_time(torch, stream, flush, solve, args.steps, args.warmup)
+    err = float((X - xt).abs().max() / xt.abs().max())
+    return {"bodies": 4, "panels": J.npan, "unknowns": m, "matrix_gb": m * m * 8 / 1e9,
+            "matrix_ms": t_build, "gmres_ms": t_solve, "gmres_iterations": box.get("it"),
+            "relative_residual": box.get("rel"), "solution_max_rel_error": err,
+            "matrix_share": t_build / (t_build + t_solve)}
 
 
 def two_patches(n, seed=5):
