@@ -368,18 +368,58 @@ __global__ void __launch_bounds__(PAN_THREADS) pan_kernel(const PanArgs a) {
   }
 }
 
-// Sum of the split partials: a block takes 32 consecutive targets (lane = target, so every
-// load of a warp is 256 contiguous bytes) and its warps take every PAN_RED_WARPS-th split,
-// double-float sums when compensated; the warps' sums are added in warp order (the result does
-// not depend on timing), then the per-target steps in FP64 and the store
-constexpr int PAN_RED_WARPS = 8;
 // (hi, lo) += (bh, bl) in double-float
 __device__ __forceinline__ void pan_df_add(float& hi, float& lo, float bh, float bl) {
   two_sum_acc(hi, lo, bh);
   lo += bl;
 }
+
+// the per-target steps of pan_finish for the target panel of modes 1 and 2 (mode 0: none)
+__device__ __forceinline__ void pan_finish_sum(const PanArgs& a, int i, float4 t) {
+  const double su = (double)t.x + (double)t.y, sv = (double)t.z + (double)t.w;
+  float tux = 0.0f, tuy = 0.0f, tinv = 0.0f;
+  if (a.mode != 0) {
+    float4 P, Q;
+    float len;
+    panel_geom(a, i, P, Q, len);
+    tux = Q.x;
+    tuy = Q.y;
+    if (a.mode == 1) tinv = 1.0f / len;
+  }
+  pan_finish(a, i, su, sv, tux, tuy, tinv);
+}
+
+// Sum of the split partials in split order, one thread per target (consecutive threads read
+// consecutive targets): double-float sums when compensated; for a few splits
 template <bool COMP>
-__global__ void __launch_bounds__(32 * PAN_RED_WARPS) pan_reduce_kernel(const PanArgs a) {
+__global__ void pan_reduce_kernel(const PanArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nt) return;
+  float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (COMP) {
+    const float2* p = static_cast<const float2*>(a.part);
+    for (int k = 0; k < a.nsplit; ++k) {
+      const float2 u = p[(size_t)k * a.nt + i], v = p[((size_t)a.nsplit + k) * a.nt + i];
+      pan_df_add(t.x, t.y, u.x, u.y);
+      pan_df_add(t.z, t.w, v.x, v.y);
+    }
+  } else {
+    const float* p = static_cast<const float*>(a.part);
+    for (int k = 0; k < a.nsplit; ++k) {
+      t.x += p[(size_t)k * a.nt + i];
+      t.z += p[((size_t)a.nsplit + k) * a.nt + i];
+    }
+  }
+  pan_finish_sum(a, i, t);
+}
+
+// The same for many splits (few targets): a block takes 32 consecutive targets (lane = target,
+// so every load of a warp is 256 contiguous bytes) and its PAN_RED_WARPS warps take every
+// PAN_RED_WARPS-th split; the warps' sums are added in warp order, so the result does not
+// depend on timing
+constexpr int PAN_RED_WARPS = 32;
+template <bool COMP>
+__global__ void __launch_bounds__(32 * PAN_RED_WARPS) pan_reduce_wide_kernel(const PanArgs a) {
   __shared__ float4 red[PAN_RED_WARPS][32];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
@@ -415,17 +455,7 @@ __global__ void __launch_bounds__(32 * PAN_RED_WARPS) pan_reduce_kernel(const Pa
       t.z += q.z;
     }
   }
-  const double su = (double)t.x + (double)t.y, sv = (double)t.z + (double)t.w;
-  float tux = 0.0f, tuy = 0.0f, tinv = 0.0f;
-  if (a.mode != 0) {
-    float4 P, Q;
-    float len;
-    panel_geom(a, i, P, Q, len);
-    tux = Q.x;
-    tuy = Q.y;
-    if (a.mode == 1) tinv = 1.0f / len;
-  }
-  pan_finish(a, i, su, sv, tux, tuy, tinv);
+  pan_finish_sum(a, i, t);
 }
 
 __global__ void pack_cotangents_kernel(const float* __restrict__ x, const float* __restrict__ y,
@@ -610,10 +640,15 @@ int launch_pan(obs_context* ctx, PanArgs& a, bool comp) {
   ctx->launches++;
   timing_main_end(ctx);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && a.nsplit > 1) {
+  if (e == cudaSuccess && a.nsplit > 16) {
     const unsigned blocks = (unsigned)((a.nt + 31) / 32);
-    if (comp) pan_reduce_kernel<true><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
-    else pan_reduce_kernel<false><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
+    if (comp) pan_reduce_wide_kernel<true><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
+    else pan_reduce_wide_kernel<false><<<blocks, 32 * PAN_RED_WARPS, 0, ctx->stream>>>(a);
+    ctx->launches++;
+    e = cudaGetLastError();
+  } else if (e == cudaSuccess && a.nsplit > 1) {
+    if (comp) pan_reduce_kernel<true><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
+    else pan_reduce_kernel<false><<<(a.nt + 255) / 256, 256, 0, ctx->stream>>>(a);
     ctx->launches++;
     e = cudaGetLastError();
   }
