@@ -201,69 +201,69 @@ __device__ __forceinline__ void pa_block(const float4* __restrict__ blk, const P
                                          float us2, float ucf) {
   if constexpr (MODE == PA_SELF && FAST) {
     pa_block_self_far<NP, COMP>(blk, w, acc);
-    return;
-  }
+  } else {
 #pragma unroll 2
-  for (int jj = 0; jj < PA_BLK; ++jj) {
-    const float4 E0 = blk[PA_ELEM * jj];
-    const float4 E1 = blk[PA_ELEM * jj + 1];
-    const float4 E2 = blk[PA_ELEM * jj + 2];
-    const float2 ex = f2(E0.x, E0.y), ey = f2(E0.z, E0.w);
-    const float2 P = f2(E1.x, E1.y), M = f2(E1.z, E1.w);     // lv, -lu
+    for (int jj = 0; jj < PA_BLK; ++jj) {
+      const float4 E0 = blk[PA_ELEM * jj];
+      const float4 E1 = blk[PA_ELEM * jj + 1];
+      const float4 E2 = blk[PA_ELEM * jj + 2];
+      const float2 ex = f2(E0.x, E0.y), ey = f2(E0.z, E0.w);
+      const float2 P = f2(E1.x, E1.y), M = f2(E1.z, E1.w);     // lv, -lu
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const float2 dx = __fadd2_rn(ex, w[p].c0);
-      const float2 dy = __fadd2_rn(ey, w[p].c1);
-      float2 d2 = __fmul2_rn(dy, dy);
-      d2 = __ffma2_rn(dx, dx, d2);
-      float2 K, B;
-      if constexpr (FAST) {
-        K = f2(rcp_a(d2.x), rcp_a(d2.y));
-        B = K;   // unused
-      } else {
-        const float z = blk[PA_ELEM * jj + 3].x;
-        float k0, k1, b0, b1;
-        if constexpr (MODE == PA_SRC) {
-          core_eval<CORE_GAUSS, THICK, true, UNIF>(d2.x, w[p].z.x, z, us2, ucf, k0, b0);
-          core_eval<CORE_GAUSS, THICK, true, UNIF>(d2.y, w[p].z.y, z, us2, ucf, k1, b1);
-        } else {
-          core_eval<CORE_GAUSS, true, true, UNIF>(d2.x, z, w[p].z.x, us2, ucf, k0, b0);
-          core_eval<CORE_GAUSS, true, true, UNIF>(d2.y, z, w[p].z.y, us2, ucf, k1, b1);
-        }
-        if constexpr (UNIF) {
-          b0 = (d2.x * ucf > 16.0f) ? -2.0f * k0 * k0 : b0;
-          b1 = (d2.y * ucf > 16.0f) ? -2.0f * k1 * k1 : b1;
-        }
-        K = f2(k0, k1);
-        // ADJ_SRC: scaled so that B * q2 = B q (q2 = -2 q from the element); ADJ_SELF forms q itself
-        B = (MODE == PA_SRC) ? f2(-0.5f * b0, -0.5f * b1) : f2(b0, b1);
-      }
-      if constexpr (MODE == PA_SRC) {
-        const float2 Q1 = f2(E2.x, E2.y), Q2 = f2(E2.z, E2.w);    // -2 lv, 2 lu
-        const float2 q2 = __ffma2_rn(dx, Q1, __fmul2_rn(dy, Q2));
+      for (int p = 0; p < NP; ++p) {
+        const float2 dx = __fadd2_rn(ex, w[p].c0);
+        const float2 dy = __fadd2_rn(ey, w[p].c1);
+        float2 d2 = __fmul2_rn(dy, dy);
+        d2 = __ffma2_rn(dx, dx, d2);
+        float2 K, B;
         if constexpr (FAST) {
-          const float2 h = __fmul2_rn(K, q2);
-          acc[p].ah = __fadd2_rn(acc[p].ah, h);
-          acc[p].ax = __ffma2_rn(K, __ffma2_rn(h, dx, P), acc[p].ax);
-          acc[p].ay = __ffma2_rn(K, __ffma2_rn(h, dy, M), acc[p].ay);
+          K = f2(rcp_a(d2.x), rcp_a(d2.y));
+          B = K;   // unused
         } else {
-          acc[p].ah = __ffma2_rn(K, q2, acc[p].ah);
-          const float2 bq = __fmul2_rn(B, q2);
-          acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, P, acc[p].ax));
-          acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, M, acc[p].ay));
+          const float z = blk[PA_ELEM * jj + 3].x;
+          float k0, k1, b0, b1;
+          if constexpr (MODE == PA_SRC) {
+            core_eval<CORE_GAUSS, THICK, true, UNIF>(d2.x, w[p].z.x, z, us2, ucf, k0, b0);
+            core_eval<CORE_GAUSS, THICK, true, UNIF>(d2.y, w[p].z.y, z, us2, ucf, k1, b1);
+          } else {
+            core_eval<CORE_GAUSS, true, true, UNIF>(d2.x, z, w[p].z.x, us2, ucf, k0, b0);
+            core_eval<CORE_GAUSS, true, true, UNIF>(d2.y, z, w[p].z.y, us2, ucf, k1, b1);
+          }
+          if constexpr (UNIF) {
+            b0 = (d2.x * ucf > 16.0f) ? -2.0f * k0 * k0 : b0;
+            b1 = (d2.y * ucf > 16.0f) ? -2.0f * k1 * k1 : b1;
+          }
+          K = f2(k0, k1);
+          // ADJ_SRC: scaled so that B * q2 = B q (q2 = -2 q from the element); ADJ_SELF forms q itself
+          B = (MODE == PA_SRC) ? f2(-0.5f * b0, -0.5f * b1) : f2(b0, b1);
         }
-      } else {
-        // full form (the far blocks of ADJ_SELF run pa_block_self_far)
-        const float2 G = f2(E2.x, E2.y);
-        const float2 qe = __ffma2_rn(dx, P, __fmul2_rn(dy, M));             // dx lv_j - dy lu_j
-        const float2 qo = __ffma2_rn(dx, w[p].lvk, __fmul2_rn(dy, w[p].nluk));
-        const float2 q = __ffma2_rn(G, qo, __fmul2_rn(w[p].ng, qe));        // G_j qo - G_k qe
-        acc[p].ah = __ffma2_rn(K, qe, acc[p].ah);
-        const float2 wv = __ffma2_rn(G, w[p].lvk, __fmul2_rn(w[p].ng, P));
-        const float2 nwu = __ffma2_rn(G, w[p].nluk, __fmul2_rn(w[p].ng, M));
-        const float2 bq = __fmul2_rn(B, q);
-        acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, wv, acc[p].ax));
-        acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, nwu, acc[p].ay));
+        if constexpr (MODE == PA_SRC) {
+          const float2 Q1 = f2(E2.x, E2.y), Q2 = f2(E2.z, E2.w);    // -2 lv, 2 lu
+          const float2 q2 = __ffma2_rn(dx, Q1, __fmul2_rn(dy, Q2));
+          if constexpr (FAST) {
+            const float2 h = __fmul2_rn(K, q2);
+            acc[p].ah = __fadd2_rn(acc[p].ah, h);
+            acc[p].ax = __ffma2_rn(K, __ffma2_rn(h, dx, P), acc[p].ax);
+            acc[p].ay = __ffma2_rn(K, __ffma2_rn(h, dy, M), acc[p].ay);
+          } else {
+            acc[p].ah = __ffma2_rn(K, q2, acc[p].ah);
+            const float2 bq = __fmul2_rn(B, q2);
+            acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, P, acc[p].ax));
+            acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, M, acc[p].ay));
+          }
+        } else {
+          // full form (the far blocks of ADJ_SELF run pa_block_self_far)
+          const float2 G = f2(E2.x, E2.y);
+          const float2 qe = __ffma2_rn(dx, P, __fmul2_rn(dy, M));             // dx lv_j - dy lu_j
+          const float2 qo = __ffma2_rn(dx, w[p].lvk, __fmul2_rn(dy, w[p].nluk));
+          const float2 q = __ffma2_rn(G, qo, __fmul2_rn(w[p].ng, qe));        // G_j qo - G_k qe
+          acc[p].ah = __ffma2_rn(K, qe, acc[p].ah);
+          const float2 wv = __ffma2_rn(G, w[p].lvk, __fmul2_rn(w[p].ng, P));
+          const float2 nwu = __ffma2_rn(G, w[p].nluk, __fmul2_rn(w[p].ng, M));
+          const float2 bq = __fmul2_rn(B, q);
+          acc[p].ax = __ffma2_rn(bq, dx, __ffma2_rn(K, wv, acc[p].ax));
+          acc[p].ay = __ffma2_rn(bq, dy, __ffma2_rn(K, nwu, acc[p].ay));
+        }
       }
     }
   }
