@@ -645,3 +645,51 @@ def test_bodies_augmented_three_bodies_solve(ctx, restatement):
     assert abs(bodies[0].omega - xr[npu]) < 3e-4 * max(1.0, abs(xr[npu]))
     assert abs(bodies[2].omega - xr[npu + 1]) < 3e-4 * max(1.0, abs(xr[npu + 1]))
     assert bodies[1].omega is None
+
+
+@pytest.mark.parametrize("call", ["panels_on_points", "points_on_panels", "panel_vjp", "rhs"])
+def test_device_panel_node_index_out_of_range_is_reported(call):
+    """A node index past the node count in a device panel set (the host entry points check
+    indices before any launch; device arrays can only be checked on the device): the kernels
+    check every index before they read the nodes, take that panel as a far panel of zero
+    strength and record the failure, which the next synchronizing call reports (OBS_ERR_ARG,
+    record code 301); the context then computes a correct sum."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    ctx = og.Context()
+    bd = og.circle_panels(256)
+    good = torch.from_numpy(bd.idx.astype(np.int32)).to(dev)
+    bad = good.clone()
+    bad[2 * 17 + 1] = bd.nnodes + 5
+    NX, NY = torch.from_numpy(bd.nx).to(dev), torch.from_numpy(bd.ny).to(dev)
+    rng = np.random.default_rng(11)
+    px, py = rng.uniform(-2.0, 2.0, (2, 5000)).astype(np.float32)
+    ps = rng.normal(0.0, 1e-2, 5000).astype(np.float32)
+    PX, PY, PS = [torch.from_numpy(a).to(dev) for a in (px, py, ps)]
+    VS = torch.ones(bd.npan, device=dev)
+    TU, TV = torch.zeros(5000, device=dev), torch.zeros(5000, device=dev)
+    PU, PV = torch.zeros(bd.npan, device=dev), torch.zeros(bd.npan, device=dev)
+    RHS = torch.zeros(2 * bd.npan, dtype=torch.float64, device=dev)
+
+    def run(idx):
+        if call == "panels_on_points":
+            og.panels_affect_points_dev(ctx, og.COMPENSATED, NX, NY, idx, VS, None, PX, PY, TU, TV)
+        elif call == "points_on_panels":
+            og.points_affect_panels_dev(ctx, og.COMPENSATED, PX, PY, PS, NX, NY, idx, PU, PV, finalize=True)
+        elif call == "panel_vjp":
+            og.panels_affect_points_vjp_dev(ctx, og.COMPENSATED, NX, NY, idx, PX, PY, PS, PS, PU, PV)
+        else:
+            og.vels_to_rhs_panels_dev(ctx, 2, NX, NY, idx, PU, PV, None, None, RHS)
+
+    run(bad)
+    with pytest.raises(og.EngineError) as ei:
+        ctx.synchronize()
+    assert ei.value.status == -1
+    bits, code, _, _ = ctx.last_failure()
+    assert bits & 4 and code == 301
+    # the same context afterwards: a valid call completes and reports nothing
+    for t in (TU, TV, PU, PV, RHS):
+        t.zero_()
+    run(good)
+    ctx.synchronize()
+    ctx.close()
