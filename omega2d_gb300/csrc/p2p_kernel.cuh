@@ -278,27 +278,41 @@ p2p_kernel(const P2PArgs a) {
 
 // Sum the split partials of each target in a fixed order (FP64 for compensated, FP32 for
 // plain) and store like the direct epilogue.
+constexpr int P2P_RED_SUB = 4;   // threads per target in the compensated split reduction
 template <int RES, bool COMP>
 __global__ void p2p_reduce_kernel(const P2PArgs a) {
   constexpr int NC = NComp<RES>::v;
+  if (COMP) {
+    // FP64 adds issue at about 2 per SM-clock on this GPU: P2P_RED_SUB consecutive threads share
+    // a target, each summing every P2P_RED_SUB-th split in order, then a fixed shuffle tree
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / P2P_RED_SUB, sub = t % P2P_RED_SUB;
+    const bool live = i < a.nt;
+    const int ic = live ? i : a.nt - 1;
+    double c[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const double* p = static_cast<const double*>(a.part) + (size_t)q * a.nsplit * a.nt + ic;
+      double s = 0.0;
+#pragma unroll 4
+      for (int k = sub; k < a.nsplit; k += P2P_RED_SUB) s += p[(size_t)k * a.nt];
+#pragma unroll
+      for (int o = 1; o < P2P_RED_SUB; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      c[q] = s;
+    }
+    if (live && sub == 0) store_target<RES>(a, i, c);
+    return;
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nt) return;
   double c[NC];
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
-    if (COMP) {
-      const double* p = static_cast<const double*>(a.part) + (size_t)q * a.nsplit * a.nt + i;
-      double s = 0.0;
+    const float* p = static_cast<const float*>(a.part) + (size_t)q * a.nsplit * a.nt + i;
+    float s = 0.0f;
 #pragma unroll 8
-      for (int k = 0; k < a.nsplit; ++k) s += p[(size_t)k * a.nt];
-      c[q] = s;
-    } else {
-      const float* p = static_cast<const float*>(a.part) + (size_t)q * a.nsplit * a.nt + i;
-      float s = 0.0f;
-#pragma unroll 8
-      for (int k = 0; k < a.nsplit; ++k) s += p[(size_t)k * a.nt];
-      c[q] = (double)s;
-    }
+    for (int k = 0; k < a.nsplit; ++k) s += p[(size_t)k * a.nt];
+    c[q] = (double)s;
   }
   store_target<RES>(a, i, c);
 }

@@ -28,8 +28,9 @@ cudaError_t p2p_dispatch_blobvort(bool comp, const P2PArgs* a, int grid, cudaStr
 cudaError_t p2p_reduce(int res, bool comp, const P2PArgs& a, cudaStream_t st) {
   const int threads = 256;
   const int blocks = (a.nt + threads - 1) / threads;
+  const int cblocks = (int)(((size_t)a.nt * P2P_RED_SUB + threads - 1) / threads);
 #define OBS_RED(R) \
-  case R: if (comp) p2p_reduce_kernel<R, true><<<blocks, threads, 0, st>>>(a); \
+  case R: if (comp) p2p_reduce_kernel<R, true><<<cblocks, threads, 0, st>>>(a); \
           else p2p_reduce_kernel<R, false><<<blocks, threads, 0, st>>>(a); break;
   switch (res) {
     OBS_RED(RES_VEL) OBS_RED(RES_GRAD) OBS_RED(RES_PSI) OBS_RED(RES_VORT) OBS_RED(RES_SHEAR) OBS_RED(RES_BLOBVORT)
